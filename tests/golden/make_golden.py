@@ -1,0 +1,596 @@
+"""Generate the golden fixtures in this directory by running the reference SophT code.
+
+Run in a container that has the reference checkout (read-only) at
+``/root/reference``::
+
+    python tests/golden/make_golden.py [/path/to/reference]
+
+The reference is imported through the test-only stand-ins in ``ref_shims.py``
+(pystencils kernels evaluated with numpy, pyfftw replaced by scipy.fft, numba's
+``njit`` as identity, pyelastica helper functions restated).  Every case uses a
+``numpy.random.default_rng`` with a fixed seed, and writes inputs and the
+reference outputs to ``golden_<group>_<precision>.npz``.  The fixtures are small
+(grids of at most a few thousand cells) so the CPU test suite loads them in
+milliseconds.  Nothing at test time reads the reference checkout.
+"""
+
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+import ref_shims  # noqa: E402
+
+
+def _import_reference(ref_root: str):
+    ref_shims.install()
+    sys.path.insert(0, ref_root)
+    import sopht.numeric.eulerian_grid_ops as spne
+    import sopht.numeric.immersed_boundary_ops as spib
+    import sopht.simulator as sps
+    return spne, spib, sps
+
+
+PRECISIONS = {"single": np.float32, "double": np.float64}
+
+
+class _Recorder:
+    def __init__(self) -> None:
+        self.data: dict[str, np.ndarray] = {}
+
+    def put(self, key: str, value) -> None:
+        self.data[key] = np.array(value, copy=True)
+
+
+# ----------------------------------------------------------------------------
+# 2D stencil operators
+# ----------------------------------------------------------------------------
+
+
+def stencils_2d(spne, real_t, rec: _Recorder, seed: int) -> None:
+    rng = np.random.default_rng(seed)
+    for tag, shape in (("sq", (16, 16)), ("rect", (12, 20))):
+        ny, nx = shape
+        field = rng.standard_normal(shape).astype(real_t)
+        vel = rng.standard_normal((2, *shape)).astype(real_t)
+        forcing = rng.standard_normal((2, *shape)).astype(real_t)
+        rec.put(f"{tag}/field", field)
+        rec.put(f"{tag}/velocity", vel)
+        rec.put(f"{tag}/forcing", forcing)
+        # ENO3 flux (advection_flux_2d.py:12-165)
+        flux = np.zeros_like(field)
+        k = spne.gen_advection_flux_conservative_eno3_pyst_kernel_2d(real_t=real_t)
+        k(advection_flux=flux, field=field, velocity=vel, inv_dx=real_t(0.1))
+        rec.put(f"{tag}/eno3_flux", flux)
+        # advection timestep (advection_timestep_2d.py:10-55)
+        out = field.copy()
+        buf = rng.standard_normal(shape).astype(real_t)  # garbage buffer: must be reset
+        k = spne.gen_advection_timestep_euler_forward_conservative_eno3_pyst_kernel_2d(real_t=real_t)
+        k(field=out, advection_flux=buf, velocity=vel, dt_by_dx=real_t(0.3))
+        rec.put(f"{tag}/advection_step", out)
+        # diffusion flux / timestep (diffusion_flux_2d.py, diffusion_timestep_2d.py)
+        dflux = rng.standard_normal(shape).astype(real_t)
+        k = spne.gen_diffusion_flux_pyst_kernel_2d(real_t=real_t)
+        k(diffusion_flux=dflux, field=field, prefactor=real_t(0.1))
+        rec.put(f"{tag}/diffusion_flux", dflux)
+        out = field.copy()
+        k = spne.gen_diffusion_timestep_euler_forward_pyst_kernel_2d(real_t=real_t)
+        k(field=out, diffusion_flux=np.zeros_like(field), nu_dt_by_dx2=real_t(0.2))
+        rec.put(f"{tag}/diffusion_step", out)
+        # outplane curl (outplane_field_curl_2d.py)
+        curl = rng.standard_normal((2, *shape)).astype(real_t)
+        k = spne.gen_outplane_field_curl_pyst_kernel_2d(real_t=real_t)
+        k(curl=curl, field=field, prefactor=real_t(0.7))
+        rec.put(f"{tag}/outplane_curl", curl)
+        # forcing curl update (update_vorticity_from_velocity_forcing_2d.py:12-71)
+        out = field.copy()
+        k = spne.gen_update_vorticity_from_velocity_forcing_pyst_kernel_2d(real_t=real_t)
+        k(vorticity_field=out, velocity_forcing_field=forcing, prefactor=real_t(0.4))
+        rec.put(f"{tag}/forcing_curl_update", out)
+        # penalise (penalise_field_boundary_2d.py:12-142) at widths 0, 2, 3
+        dx = real_t(1.0 / nx)
+        x = np.linspace(dx / 2, 1.0 - dx / 2, nx).astype(real_t)
+        y_range = 1.0 * ny / nx
+        y = np.linspace(dx / 2, y_range - dx / 2, ny).astype(real_t)
+        pos = np.flipud(np.array(np.meshgrid(y, x, indexing="ij")))
+        rec.put(f"{tag}/position", pos)
+        for width in (0, 2, 3):
+            out = field.copy()
+            k = spne.gen_penalise_field_boundary_pyst_kernel_2d(
+                width=width, dx=dx, x_grid_field=pos[0], y_grid_field=pos[1], real_t=real_t)
+            k(field=out)
+            rec.put(f"{tag}/penalise_w{width}", out)
+        # elementwise: add fixed value (vector), set fixed value (vector)
+        out = vel.copy()
+        k = spne.gen_add_fixed_val_pyst_kernel_2d(real_t=real_t, field_type="vector")
+        k(sum_field=out, vector_field=out, fixed_vals=[1.5, -0.25])
+        rec.put(f"{tag}/add_fixed_val", out)
+
+
+def poisson_2d(spne, real_t, rec: _Recorder, seed: int) -> None:
+    rng = np.random.default_rng(seed)
+    for tag, (ny, nx, x_range) in (("sq", (16, 16, 1.0)), ("rect", (12, 24, 2.0)), ("r3", (6, 12, 1.0))):
+        rhs = rng.standard_normal((ny, nx)).astype(real_t)
+        solver = spne.UnboundedPoissonSolverPYFFTW2D(
+            grid_size_y=ny, grid_size_x=nx, x_range=x_range, real_t=real_t)
+        sol = np.zeros_like(rhs)
+        solver.solve(solution_field=sol, rhs_field=rhs)
+        rec.put(f"{tag}/rhs", rhs)
+        rec.put(f"{tag}/solution", sol)
+        rec.put(f"{tag}/meta", [ny, nx, x_range])
+        rec.put(f"{tag}/greens_hat_dx2", solver.fourier_greens_function_times_dx_squared)
+
+
+def ns_2d(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """One full with-forcing step of the 2D simulator (navier_stokes_flow_simulators.py:200-209)."""
+    rng = np.random.default_rng(seed)
+    cases = (
+        ("a", (16, 16), 1.0, 1e-2, True, 1.0, 2),
+        ("b", (12, 24), 1.0, 1e-3, True, 0.1, 2),
+        ("c", (16, 32), 2.0, 5e-3, False, 1.0, 3),
+    )
+    for tag, grid, x_range, nu, free_stream, rho, width in cases:
+        sim = sps.UnboundedNavierStokesFlowSimulator2D(
+            grid_size=grid, x_range=x_range, kinematic_viscosity=nu, real_t=real_t,
+            time=0.5, with_forcing=True, with_free_stream_flow=free_stream,
+            flow_density=rho, penalty_zone_width=width)
+        sim.vorticity_field[...] = rng.standard_normal(grid).astype(real_t)
+        sim.velocity_field[...] = rng.standard_normal((2, *grid)).astype(real_t)
+        sim.eul_grid_forcing_field[...] = rng.standard_normal((2, *grid)).astype(real_t)
+        rec.put(f"{tag}/vorticity_in", sim.vorticity_field)
+        rec.put(f"{tag}/velocity_in", sim.velocity_field)
+        rec.put(f"{tag}/forcing_in", sim.eul_grid_forcing_field)
+        dt = sim.compute_stable_timestep()
+        rec.put(f"{tag}/stable_dt", dt)
+        rec.put(f"{tag}/stable_dt_prefac", sim.compute_stable_timestep(dt_prefac=0.25))
+        dt = 0.5 * dt
+        u_inf = np.array([0.7, -0.2])
+        sim.time_step(dt=dt, free_stream_velocity=u_inf)
+        rec.put(f"{tag}/meta", [grid[0], grid[1], x_range, nu, float(free_stream), rho, width, dt,
+                                u_inf[0], u_inf[1]])
+        rec.put(f"{tag}/vorticity_out", sim.vorticity_field)
+        rec.put(f"{tag}/velocity_out", sim.velocity_field)
+        rec.put(f"{tag}/stream_func_out", sim.stream_func_field)
+        rec.put(f"{tag}/forcing_out", sim.eul_grid_forcing_field)
+        rec.put(f"{tag}/time_out", sim.time)
+        # the no-forcing variant (navier_stokes_flow_simulators.py:171-198)
+        sim2 = sps.UnboundedNavierStokesFlowSimulator2D(
+            grid_size=grid, x_range=x_range, kinematic_viscosity=nu, real_t=real_t,
+            with_forcing=False, with_free_stream_flow=free_stream, penalty_zone_width=width)
+        sim2.vorticity_field[...] = rec.data[f"{tag}/vorticity_in"]
+        sim2.velocity_field[...] = rec.data[f"{tag}/velocity_in"]
+        sim2.time_step(dt=dt, free_stream_velocity=u_inf)
+        rec.put(f"{tag}/noforce_vorticity_out", sim2.vorticity_field)
+        rec.put(f"{tag}/noforce_velocity_out", sim2.velocity_field)
+
+
+# ----------------------------------------------------------------------------
+# 3D operators
+# ----------------------------------------------------------------------------
+
+
+def stencils_3d(spne, real_t, rec: _Recorder, seed: int) -> None:
+    rng = np.random.default_rng(seed)
+    for tag, shape in (("cube", (10, 10, 10)), ("rect", (8, 10, 12))):
+        nz, ny, nx = shape
+        vec = rng.standard_normal((3, *shape)).astype(real_t)
+        vec2 = rng.standard_normal((3, *shape)).astype(real_t)
+        rec.put(f"{tag}/field", vec)
+        rec.put(f"{tag}/field2", vec2)
+        out = rng.standard_normal((3, *shape)).astype(real_t)
+        spne.gen_curl_pyst_kernel_3d(real_t=real_t)(curl=out, field=vec, prefactor=real_t(0.6))
+        rec.put(f"{tag}/curl", out)
+        out = vec.copy()
+        spne.gen_update_vorticity_from_velocity_forcing_pyst_kernel_3d(real_t=real_t)(
+            vorticity_field=out, velocity_forcing_field=vec2, prefactor=real_t(0.3))
+        rec.put(f"{tag}/forcing_curl_update", out)
+        out = np.zeros_like(vec)
+        spne.gen_elementwise_cross_product_pyst_kernel_3d(real_t=real_t)(
+            result_field=out, field_1=vec, field_2=vec2)
+        rec.put(f"{tag}/cross", out)
+        out = vec.copy()
+        spne.gen_diffusion_timestep_euler_forward_pyst_kernel_3d(real_t=real_t, field_type="vector")(
+            vector_field=out, diffusion_flux=np.zeros(shape, real_t), nu_dt_by_dx2=real_t(0.1))
+        rec.put(f"{tag}/diffusion_step", out)
+        div = np.zeros(shape, real_t)
+        spne.gen_divergence_pyst_kernel_3d(real_t=real_t)(divergence=div, field=vec, inv_dx=real_t(3.0))
+        rec.put(f"{tag}/divergence", div)
+        dx = real_t(1.0 / nx)
+        x = np.linspace(dx / 2, 1.0 - dx / 2, nx).astype(real_t)
+        y = np.linspace(dx / 2, ny / nx - dx / 2, ny).astype(real_t)
+        z = np.linspace(dx / 2, nz / nx - dx / 2, nz).astype(real_t)
+        pos = np.flipud(np.array(np.meshgrid(z, y, x, indexing="ij")))
+        rec.put(f"{tag}/position", pos)
+        for width in (0, 2):
+            out = vec.copy()
+            spne.gen_penalise_field_boundary_pyst_kernel_3d(
+                width=width, dx=dx, x_grid_field=pos[0], y_grid_field=pos[1],
+                z_grid_field=pos[2], real_t=real_t, field_type="vector")(vector_field=out)
+            rec.put(f"{tag}/penalise_w{width}", out)
+        for ftype, order in (("multiplicative", 2), ("convolution", 1), ("convolution", 3)):
+            out = vec.copy()
+            flux_buf = rng.standard_normal(shape).astype(real_t)
+            field_buf = rng.standard_normal(shape).astype(real_t)
+            spne.gen_laplacian_filter_kernel_3d(
+                filter_order=order, filter_flux_buffer=flux_buf, field_buffer=field_buf,
+                real_t=real_t, field_type="vector", filter_type=ftype)(vector_field=out)
+            rec.put(f"{tag}/filter_{ftype}_{order}", out)
+
+
+def poisson_3d(spne, real_t, rec: _Recorder, seed: int) -> None:
+    rng = np.random.default_rng(seed)
+    for tag, (nz, ny, nx, x_range) in (("cube", (8, 8, 8, 1.0)), ("rect", (6, 8, 12, 1.5))):
+        rhs = rng.standard_normal((3, nz, ny, nx)).astype(real_t)
+        solver = spne.UnboundedPoissonSolverPYFFTW3D(
+            grid_size_z=nz, grid_size_y=ny, grid_size_x=nx, x_range=x_range, real_t=real_t)
+        sol = np.zeros_like(rhs)
+        solver.vector_field_solve(solution_vector_field=sol, rhs_vector_field=rhs)
+        rec.put(f"{tag}/rhs", rhs)
+        rec.put(f"{tag}/solution", sol)
+        rec.put(f"{tag}/meta", [nz, ny, nx, x_range])
+
+
+def ns_3d(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """One full step of the 3D simulator (navier_stokes_flow_simulators.py:449-498)."""
+    rng = np.random.default_rng(seed)
+    cases = (
+        ("a", (10, 10, 10), 1.0, 1e-2, True, 1.0, None),
+        ("b", (8, 10, 12), 1.0, 2e-3, True, 0.5, None),
+        ("c", (8, 8, 12), 1.5, 1e-2, False, 1.0, {"order": 2, "type": "multiplicative"}),
+        ("d", (10, 10, 10), 1.0, 1e-2, True, 1.0, {"order": 3, "type": "convolution"}),
+    )
+    for tag, grid, x_range, nu, free_stream, rho, filt in cases:
+        kwargs = {}
+        if filt is not None:
+            kwargs = {"filter_vorticity": True, "filter_setting_dict": filt}
+        sim = sps.UnboundedNavierStokesFlowSimulator3D(
+            grid_size=grid, x_range=x_range, kinematic_viscosity=nu, real_t=real_t,
+            with_forcing=True, with_free_stream_flow=free_stream, flow_density=rho, **kwargs)
+        sim.vorticity_field[...] = rng.standard_normal((3, *grid)).astype(real_t)
+        sim.velocity_field[...] = rng.standard_normal((3, *grid)).astype(real_t)
+        sim.eul_grid_forcing_field[...] = rng.standard_normal((3, *grid)).astype(real_t)
+        rec.put(f"{tag}/vorticity_in", sim.vorticity_field)
+        rec.put(f"{tag}/velocity_in", sim.velocity_field)
+        rec.put(f"{tag}/forcing_in", sim.eul_grid_forcing_field)
+        rec.put(f"{tag}/divergence_l2", sim.get_vorticity_divergence_l2_norm())
+        dt = sim.compute_stable_timestep()
+        rec.put(f"{tag}/stable_dt", dt)
+        dt = 0.5 * dt
+        u_inf = np.array([0.6, -0.1, 0.3])
+        sim.time_step(dt=dt, free_stream_velocity=u_inf)
+        order = -1 if filt is None else filt["order"]
+        ftype = 0 if filt is None else (1 if filt["type"] == "multiplicative" else 2)
+        rec.put(f"{tag}/meta", [*grid, x_range, nu, float(free_stream), rho, dt, *u_inf, order, ftype])
+        rec.put(f"{tag}/vorticity_out", sim.vorticity_field)
+        rec.put(f"{tag}/velocity_out", sim.velocity_field)
+        rec.put(f"{tag}/stream_func_out", sim.stream_func_field)
+
+
+# ----------------------------------------------------------------------------
+# immersed boundary
+# ----------------------------------------------------------------------------
+
+
+def ib_ops(spib, real_t, rec: _Recorder, seed: int) -> None:
+    """VirtualBoundaryForcing on random markers (VirtualBoundaryForcing.py:20-283)."""
+    rng = np.random.default_rng(seed)
+    for dim, grid in ((2, (16, 20)), (3, (12, 12, 14))):
+        nx = grid[-1]
+        dx = real_t(1.0 / nx)
+        n_lag = 7
+        extent = np.array([g * dx for g in grid[::-1]])  # (x, y[, z]) extents
+        for kernel in ("cosine", "peskin"):
+            tag = f"d{dim}_{kernel}"
+            vbf = spib.VirtualBoundaryForcing(
+                virtual_boundary_stiffness_coeff=-3.0e2, virtual_boundary_damping_coeff=-1.5,
+                grid_dim=dim, dx=dx, num_lag_nodes=n_lag, real_t=real_t,
+                enable_eul_grid_forcing_reset=False)
+            if kernel == "peskin":
+                comm = vbf.eul_lag_grid_communicator
+                mod = sys.modules[type(comm).__module__]
+                gen = getattr(mod, f"generate_peskin_interpolation_weights_kernel_{dim}d")
+                comm.interpolation_weights_kernel = gen(dx=dx, interp_kernel_width=2, real_t=real_t)
+            pos = (0.3 + 0.4 * rng.random((dim, n_lag))) * extent.reshape(dim, 1)
+            pos[:, 0] = (np.array([5, 6, 5][:dim]) + 0.5) * dx  # exactly on a node
+            lag_vel = rng.standard_normal((dim, n_lag))
+            eul_vel = rng.standard_normal((dim, *grid)).astype(real_t)
+            eul_force = rng.standard_normal((dim, *grid)).astype(real_t)
+            vbf.lag_grid_position_mismatch_field[...] = rng.standard_normal((dim, n_lag))
+            rec.put(f"{tag}/position", pos)
+            rec.put(f"{tag}/lag_velocity", lag_vel)
+            rec.put(f"{tag}/eul_velocity", eul_vel)
+            rec.put(f"{tag}/eul_forcing_in", eul_force)
+            rec.put(f"{tag}/position_mismatch_in", vbf.lag_grid_position_mismatch_field)
+            vbf.compute_interaction_forcing(
+                eul_grid_forcing_field=eul_force, eul_grid_velocity_field=eul_vel,
+                lag_grid_position_field=pos, lag_grid_velocity_field=lag_vel)
+            rec.put(f"{tag}/nearest_index", vbf.nearest_eul_grid_index_to_lag_grid)
+            rec.put(f"{tag}/weights", vbf.interp_weights)
+            rec.put(f"{tag}/lag_flow_velocity", vbf.lag_grid_flow_velocity_field)
+            rec.put(f"{tag}/velocity_mismatch", vbf.lag_grid_velocity_mismatch_field)
+            rec.put(f"{tag}/lag_forcing", vbf.lag_grid_forcing_field)
+            rec.put(f"{tag}/eul_forcing_out", eul_force)
+            vbf.time_step(dt=0.01)
+            rec.put(f"{tag}/position_mismatch_out", vbf.lag_grid_position_mismatch_field)
+            rec.put(f"{tag}/meta", [dim, *grid, n_lag, -3.0e2, -1.5, 0.01])
+
+
+class _FakeCylinder:
+    """Fixed cylinder with the attributes the reference forcing grid reads."""
+
+    def __init__(self, centre, radius) -> None:
+        self.position_collection = np.array(centre, dtype=float).reshape(3, 1)
+        self.director_collection = np.eye(3).reshape(3, 3, 1)
+        self.velocity_collection = np.zeros((3, 1))
+        self.omega_collection = np.zeros((3, 1))
+        self.radius = radius
+
+
+def cylinder_2d(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """A few coupled steps of the flow-past-cylinder loop (flow_past_cylinder.py:129-136)."""
+    rng = np.random.default_rng(seed)
+    grid = (32, 64)
+    x_range = 1.0
+    radius = 0.08
+    nu = 2.0 * radius * 1.0 / 200.0
+    sim = sps.UnboundedNavierStokesFlowSimulator2D(
+        grid_size=grid, x_range=x_range, kinematic_viscosity=nu, real_t=real_t,
+        with_forcing=True, with_free_stream_flow=True)
+    sim.vorticity_field[...] = (1e-3 * rng.standard_normal(grid)).astype(real_t)
+    cyl = _FakeCylinder([0.25, 0.25, 0.0], radius)
+    n_markers = 24
+    inter = sps.RigidBodyFlowInteraction(
+        rigid_body=cyl, eul_grid_forcing_field=sim.eul_grid_forcing_field,
+        eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=-5e4,
+        virtual_boundary_damping_coeff=-20.0, dx=sim.dx, grid_dim=2, real_t=real_t,
+        forcing_grid_cls=sps.CircularCylinderForcingGrid, num_forcing_points=n_markers)
+    rec.put("vorticity_init", sim.vorticity_field)
+    rec.put("marker_position", inter.forcing_grid.position_field)
+    u_inf = np.array([1.0, 0.0])
+    dts, drags = [], []
+    for step in range(4):
+        dt = sim.compute_stable_timestep()
+        inter.time_step(dt=dt)
+        inter()
+        sim.time_step(dt=dt, free_stream_velocity=u_inf)
+        dts.append(dt)
+        drags.append(np.sum(inter.lag_grid_forcing_field[0]))
+        rec.put(f"step{step}/vorticity", sim.vorticity_field)
+        rec.put(f"step{step}/velocity", sim.velocity_field)
+        rec.put(f"step{step}/lag_forcing", inter.lag_grid_forcing_field)
+        rec.put(f"step{step}/position_mismatch", inter.lag_grid_position_mismatch_field)
+    rec.put("dt", dts)
+    rec.put("drag", drags)
+    rec.put("grid_deviation", inter.get_grid_deviation_error_l2_norm())
+    inter.compute_flow_forces_and_torques()
+    rec.put("body_forces", inter.body_flow_forces)
+    rec.put("body_torques", inter.body_flow_torques)
+    rec.put("meta", [grid[0], grid[1], x_range, nu, radius, n_markers, 0.25, 0.25, -5e4, -20.0])
+
+
+class _FakeRod:
+    """Straight rod with the attributes the reference rod forcing grids read."""
+
+    def __init__(self, rng, n_elems: int) -> None:
+        self.n_elems = n_elems
+        s = np.linspace(0.0, 0.3, n_elems + 1)
+        self.position_collection = np.stack(
+            [0.35 + 0.01 * np.sin(7 * s), 0.5 + 0.0 * s, 0.35 + s])
+        self.position_collection += 1e-3 * rng.standard_normal(self.position_collection.shape)
+        self.velocity_collection = 0.1 * rng.standard_normal((3, n_elems + 1))
+        self.mass = 1.0 + 0.1 * rng.random(n_elems + 1)
+        self.lengths = np.linalg.norm(np.diff(self.position_collection, axis=1), axis=0)
+        th = 0.2 * rng.standard_normal(n_elems)
+        d = np.zeros((3, 3, n_elems))
+        d[0, 0] = np.cos(th)
+        d[0, 1] = np.sin(th)
+        d[1, 0] = -np.sin(th)
+        d[1, 1] = np.cos(th)
+        d[2, 2] = 1.0
+        self.director_collection = d
+
+
+def rod_3d(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """Rod forcing grids (cosserat_rod_forcing_grids.py:10-130) on a random 3D flow."""
+    rng = np.random.default_rng(seed)
+    grid = (16, 16, 16)
+    dx = real_t(1.0 / 16)
+    eul_vel = rng.standard_normal((3, *grid)).astype(real_t)
+    rec.put("eul_velocity", eul_vel)
+    for name, cls in (("nodal", sps.CosseratRodNodalForcingGrid),
+                      ("element", sps.CosseratRodElementCentricForcingGrid)):
+        rod = _FakeRod(rng, 10)
+        force = np.zeros((3, *grid), dtype=real_t)
+        inter = sps.CosseratRodFlowInteraction(
+            cosserat_rod=rod, eul_grid_forcing_field=force, eul_grid_velocity_field=eul_vel,
+            virtual_boundary_stiffness_coeff=-2e4, virtual_boundary_damping_coeff=-1e2, dx=dx,
+            grid_dim=3, real_t=real_t, forcing_grid_cls=cls)
+        rec.put(f"{name}/rod_position", rod.position_collection)
+        rec.put(f"{name}/rod_velocity", rod.velocity_collection)
+        rec.put(f"{name}/rod_mass", rod.mass)
+        rec.put(f"{name}/rod_directors", rod.director_collection)
+        inter.time_step(dt=1e-3)
+        inter()
+        rec.put(f"{name}/eul_forcing_out", force)
+        rec.put(f"{name}/lag_forcing", inter.lag_grid_forcing_field)
+        inter.lag_grid_position_mismatch_field[...] = 1e-3 * rng.standard_normal(
+            inter.lag_grid_position_mismatch_field.shape)
+        rec.put(f"{name}/position_mismatch_in", inter.lag_grid_position_mismatch_field)
+        inter.compute_flow_forces_and_torques()
+        rec.put(f"{name}/body_forces", inter.body_flow_forces)
+        rec.put(f"{name}/body_torques", inter.body_flow_torques)
+        rec.put(f"{name}/lag_forcing_after", inter.lag_grid_forcing_field)
+
+
+GROUPS = {
+    "stencils2d": ("spne", stencils_2d, 11),
+    "poisson2d": ("spne", poisson_2d, 12),
+    "ns2d": ("sps", ns_2d, 13),
+    "stencils3d": ("spne", stencils_3d, 21),
+    "poisson3d": ("spne", poisson_3d, 22),
+    "ns3d": ("sps", ns_3d, 23),
+    "ib": ("spib", ib_ops, 31),
+    "cylinder2d": ("sps", cylinder_2d, 32),
+    "rod3d": ("sps", rod_3d, 33),
+}
+
+
+def _load_test_restatements(ref_root: str, rel: str) -> dict:
+    """Load the numpy restatement functions from one reference test file.
+
+    Only top-level ``def``s that are not ``test_*`` are executed, with numpy,
+    scipy.fft and the reference's precision helpers in scope; the pytest
+    fixtures and sopht imports of the file are skipped.
+    """
+    import ast
+
+    from scipy.fft import irfftn, rfftn
+
+    src = (Path(ref_root) / "tests" / rel).read_text()
+    ns = {"np": np, "rfftn": rfftn, "irfftn": irfftn}
+    for node in ast.parse(src).body:
+        if isinstance(node, ast.FunctionDef) and not node.name.startswith("test_"):
+            exec(compile(ast.Module([node], []), rel, "exec"), ns)
+    return ns
+
+
+def validate_shims(ref_root: str, spne) -> None:
+    """Check the stand-ins against the reference tests' own numpy restatements.
+
+    Each reference kernel run through ``ref_shims`` must agree with the
+    restatement in the corresponding reference test file to the tolerance those
+    tests use (1e3 machine epsilons, absolute).
+    """
+    t2 = "test_numeric/test_eulerian_grid_ops/test_stencil_ops_2d/"
+    t3 = "test_numeric/test_eulerian_grid_ops/test_stencil_ops_3d/"
+    rng = np.random.default_rng(42)
+    checked = 0
+    for real_t in (np.float32, np.float64):
+        tol = real_t(1e3) * np.finfo(real_t).eps
+        n = 16
+        f = rng.standard_normal((n, n)).astype(real_t)
+        v = rng.standard_normal((2, n, n)).astype(real_t)
+
+        def close(a, b):
+            nonlocal checked
+            np.testing.assert_allclose(a, b, atol=tol)
+            checked += 1
+
+        ns = _load_test_restatements(ref_root, t2 + "test_advection_flux_2d.py")
+        out = np.zeros_like(f)
+        spne.gen_advection_flux_conservative_eno3_pyst_kernel_2d(real_t=real_t)(
+            advection_flux=out, field=f, velocity=v, inv_dx=real_t(0.1))
+        close(out, ns["advection_flux_conservative_eno_ord3_reference"](f, v[0], v[1], real_t(0.1), real_t))
+        ns = _load_test_restatements(ref_root, t2 + "test_diffusion_timestep_2d.py")
+        ns.update(_load_test_restatements(ref_root, t2 + "test_diffusion_flux_2d.py"))
+        out = f.copy()
+        spne.gen_diffusion_timestep_euler_forward_pyst_kernel_2d(real_t=real_t)(
+            field=out, diffusion_flux=np.zeros_like(f), nu_dt_by_dx2=real_t(0.1))
+        close(out, ns["diffusion_timestep_euler_forward_reference"](f, real_t(0.1), real_t))
+        ns = _load_test_restatements(ref_root, t2 + "test_outplane_field_curl_2d.py")
+        out = np.zeros_like(v)
+        spne.gen_outplane_field_curl_pyst_kernel_2d(real_t=real_t)(curl=out, field=f, prefactor=real_t(0.3))
+        close(out, ns["outplane_curl_reference"](f, real_t(0.3), real_t))
+        ns = _load_test_restatements(ref_root, t2 + "test_update_vorticity_from_velocity_forcing_2d.py")
+        out = f.copy()
+        spne.gen_update_vorticity_from_velocity_forcing_pyst_kernel_2d(real_t=real_t)(
+            vorticity_field=out, velocity_forcing_field=v, prefactor=real_t(0.2))
+        close(out[1:-1, 1:-1], ns["update_vorticity_from_velocity_forcing_reference"](f, v, real_t(0.2))[1:-1, 1:-1])
+        ns = _load_test_restatements(ref_root, t2 + "test_penalise_field_boundary_2d.py")
+        dx = real_t(1.0 / n)
+        x = np.linspace(dx / 2, 1 - dx / 2, n).astype(real_t)
+        pos = np.flipud(np.array(np.meshgrid(x, x, indexing="ij")))
+        for width in (2, 3):
+            out = f.copy()
+            spne.gen_penalise_field_boundary_pyst_kernel_2d(
+                width=width, dx=dx, x_grid_field=pos[0], y_grid_field=pos[1], real_t=real_t)(field=out)
+            ref = f.copy()
+            ns["penalise_field_boundary_reference"](ref, f, pos[0], pos[1], width, dx)
+            close(out, ref)
+        # 3D
+        m = 8
+        w3 = rng.standard_normal((3, m, m, m)).astype(real_t)
+        g3 = rng.standard_normal((3, m, m, m)).astype(real_t)
+        ns = _load_test_restatements(ref_root, t3 + "test_curl_3d.py")
+        out = np.zeros_like(w3)
+        spne.gen_curl_pyst_kernel_3d(real_t=real_t)(curl=out, field=w3, prefactor=real_t(0.5))
+        close(out, np.stack(ns["curl_reference"](w3[0], w3[1], w3[2], real_t(0.5))))
+        ns = _load_test_restatements(ref_root, t3 + "test_diffusion_timestep_3d.py")
+        out = w3.copy()
+        spne.gen_diffusion_timestep_euler_forward_pyst_kernel_3d(real_t=real_t, field_type="vector")(
+            vector_field=out, diffusion_flux=np.zeros_like(w3[0]), nu_dt_by_dx2=real_t(0.1))
+        close(out, np.stack([ns["diffusion_timestep_euler_forward_reference"](c, real_t(0.1), real_t) for c in w3]))
+        ns = _load_test_restatements(ref_root, t3 + "test_divergence_3d.py")
+        out = np.zeros_like(w3[0])
+        spne.gen_divergence_pyst_kernel_3d(real_t=real_t)(divergence=out, field=w3, inv_dx=real_t(2.0))
+        close(out, ns["divergence_reference"](w3, real_t(2.0)))
+        ns = _load_test_restatements(ref_root, t3 + "test_update_vorticity_from_velocity_forcing_3d.py")
+        out = w3.copy()
+        spne.gen_update_vorticity_from_velocity_forcing_pyst_kernel_3d(real_t=real_t)(
+            vorticity_field=out, velocity_forcing_field=g3, prefactor=real_t(0.2))
+        ref = ns["update_vorticity_from_velocity_forcing_reference_3d"](w3, g3, real_t(0.2))
+        close(out[:, 1:-1, 1:-1, 1:-1], ref[:, 1:-1, 1:-1, 1:-1])
+        ns = _load_test_restatements(ref_root, t3 + "test_penalise_field_boundary_3d.py")
+        dx = real_t(1.0 / m)
+        x = np.linspace(dx / 2, 1 - dx / 2, m).astype(real_t)
+        pos3 = np.flipud(np.array(np.meshgrid(x, x, x, indexing="ij")))
+        out = w3[0].copy()
+        spne.gen_penalise_field_boundary_pyst_kernel_3d(
+            width=2, dx=dx, x_grid_field=pos3[0], y_grid_field=pos3[1], z_grid_field=pos3[2],
+            real_t=real_t)(field=out)
+        ref = w3[0].copy()
+        ns["penalise_field_boundary_reference_3d"](ref, w3[0], pos3[0], pos3[1], pos3[2], 2, dx)
+        close(out, ref)
+        ns = _load_test_restatements(ref_root, t3 + "test_laplacian_filter_3d.py")
+        for ftype, order in (("multiplicative", 2), ("convolution", 3)):
+            out = w3.copy()
+            spne.gen_laplacian_filter_kernel_3d(
+                filter_order=order, filter_flux_buffer=np.zeros_like(w3[0]),
+                field_buffer=np.zeros_like(w3[0]), real_t=real_t, field_type="vector",
+                filter_type=ftype)(vector_field=out)
+            ref = w3.copy()
+            ns["vector_laplacian_filter"](ref, order, ftype)
+            close(out, ref)
+        # Poisson 2D: the reference test's scipy restatement
+        ns = _load_test_restatements(
+            ref_root, "test_numeric/test_eulerian_grid_ops/test_poisson_solver_2d/test_unbounded_poisson_solver_2d.py")
+        rhs = rng.standard_normal((8, 16)).astype(real_t)
+        solver = spne.UnboundedPoissonSolverPYFFTW2D(grid_size_y=8, grid_size_x=16, x_range=1.0, real_t=real_t)
+        out = np.zeros_like(rhs)
+        solver.solve(solution_field=out, rhs_field=rhs)
+        from scipy.fft import irfftn, rfftn
+        dx = real_t(1.0 / 16)
+        xd = np.linspace(0, 2 - dx, 32).astype(real_t)
+        yd = np.linspace(0, 1 - dx, 16).astype(real_t)
+        xg, yg = np.meshgrid(xd, yd)
+        r = np.sqrt(np.minimum(xg, 2 - xg) ** 2 + np.minimum(yg, 1 - yg) ** 2)
+        with np.errstate(divide="ignore"):
+            g = -np.log(r) / (2 * np.pi)
+        g[0, 0] = -(2 * np.log(dx / np.sqrt(np.pi)) - 1) / (4 * np.pi)
+        big = np.zeros((16, 32), real_t)
+        big[:8, :16] = rhs
+        ref = irfftn(rfftn(big) * rfftn(g) * dx**2)[:8, :16]
+        close(out, ref)
+    print(f"shim validation: {checked} reference-test restatements agree")
+
+
+def main(ref_root: str = "/root/reference") -> None:
+    spne, spib, sps = _import_reference(ref_root)
+    validate_shims(ref_root, spne)
+    mods = {"spne": spne, "spib": spib, "sps": sps}
+    for group, (modname, fn, seed) in GROUPS.items():
+        for prec, real_t in PRECISIONS.items():
+            rec = _Recorder()
+            fn(mods[modname], real_t, rec, seed)
+            out = HERE / f"golden_{group}_{prec}.npz"
+            np.savez_compressed(out, **rec.data)
+            print(f"{out.name}: {len(rec.data)} arrays, {out.stat().st_size / 1024:.1f} KiB")
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])
