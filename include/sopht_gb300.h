@@ -1,0 +1,210 @@
+/*
+ * sopht_gb300.h — C ABI of the GB300-native SophT flow-step library.
+ *
+ * Scope: the flow-step hot path of SophT — the Eulerian grid operators of the
+ * unbounded vorticity Navier-Stokes step (2D: forcing curl, ENO3 conservative
+ * advection, diffusion, boundary penalisation, velocity recovery; 3D: forcing
+ * curl, rotational-form u x w update, diffusion, optional Laplacian filter,
+ * penalisation, velocity recovery), the unbounded domain-doubled FFT Poisson
+ * solve, and the immersed-boundary interpolation/spreading with
+ * virtual-boundary forcing.
+ *
+ * Conventions
+ *  - Every function returns SG_OK (0) or an SG_ERR_* code; sg_last_error()
+ *    returns a thread-local message for the last failure.
+ *  - Pointers are raw CUDA device pointers unless stated otherwise.  Arrays are
+ *    C-ordered: 2D (ny, nx), 3D (nz, ny, nx); vector fields put the component
+ *    first with component 0 = x (sopht/utils/field.py).
+ *  - `dtype` selects the real type of every Eulerian/Lagrangian field of the
+ *    call: SG_F32 (float) or SG_F64 (double).  Marker positions and body
+ *    velocities are always double, as the reference's forcing grids hold them.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Only the *_create functions allocate device memory (and synchronise).
+ *    Step and operator calls never allocate and never synchronise, so they can
+ *    be recorded in a CUDA graph.
+ *
+ * Each declaration cites the reference interface it replaces (file:line within
+ * the SophT repository).
+ */
+#ifndef SOPHT_GB300_H
+#define SOPHT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SG_OK 0
+#define SG_ERR_INVALID_ARG 1   /* bad dtype, null pointer, bad flag          */
+#define SG_ERR_SHAPE 2         /* grid too small / unsupported extent        */
+#define SG_ERR_CUDA 3          /* a CUDA runtime call failed                 */
+#define SG_ERR_UNSUPPORTED 4   /* FFT length with a prime factor above 7     */
+#define SG_ERR_OUT_OF_DOMAIN 5 /* an IB marker support leaves the grid       */
+
+#define SG_F32 0
+#define SG_F64 1
+
+typedef struct sg_poisson_plan_s* sg_poisson_plan;
+typedef struct sg_flow_plan_s* sg_flow_plan;
+
+/* Per-step scalar prefactors, rounded to the field precision by the caller
+ * exactly as the reference computes them (navier_stokes_flow_simulators.py:
+ * 175-186, 203-207, 461-471).  Fields unused by a call are ignored. */
+typedef struct sg_step_scalars {
+    double dt;              /* time step                                        */
+    double forcing_prefac;  /* dt / (2 dx rho)            (forcing curl update)  */
+    double advection_prefac;/* 2D: dt / dx (ENO3);  3D: dt / (2 dx) (u x w curl) */
+    double diffusion_prefac;/* nu dt / dx^2                                      */
+    double free_stream[3];  /* free-stream velocity added after the curl         */
+} sg_step_scalars;
+
+/* ---------------------------------------------------------------- general */
+const char* sg_last_error(void);
+int sg_version(void);
+
+/* ------------------------------------------------- unbounded Poisson solve */
+/* Replaces UnboundedPoissonSolverPYFFTW2D.__init__ (poisson_solver_2d/
+ * UnboundedPoissonSolverPYFFTW2D.py:11-45) and UnboundedPoissonSolverPYFFTW3D.
+ * __init__ (poisson_solver_3d/UnboundedPoissonSolverPYFFTW3D.py:12-54): builds
+ * the Green's function table in FP64 on the GPU and the FFT workspace for up to
+ * `max_comp` components.  dim = 2 ignores nz.  nx must be even; nx, 2*ny and
+ * 2*nz must factor into 2, 3, 5 and 7. */
+int sg_poisson_plan_create(int dim, int nz, int ny, int nx, double x_range, int dtype,
+                           int max_comp, sg_poisson_plan* plan_out);
+int sg_poisson_plan_destroy(sg_poisson_plan plan);
+/* Device bytes held by the plan (workspace + tables). */
+int64_t sg_poisson_plan_bytes(sg_poisson_plan plan);
+/* Replaces UnboundedPoissonSolverPYFFTW2D.solve (:95-129), ...3D.solve
+ * (:111-149) and ...3D.vector_field_solve (:151-172): solves -lap(sol) = rhs
+ * on the unbounded domain for `ncomp` components spaced `comp_stride` elements
+ * apart in both rhs and sol. */
+int sg_poisson_solve(sg_poisson_plan plan, const void* rhs, void* sol, int ncomp,
+                     int64_t comp_stride, void* stream);
+
+/* --------------------------------------------------------- flow step plan */
+/* Replaces the kernel compilation of UnboundedNavierStokesFlowSimulator2D/3D
+ * (navier_stokes_flow_simulators.py:89-162, 327-440).  pen_coef_{x,y,z} are
+ * host arrays of length nx, ny, nz holding the penalisation factor of each
+ * index (sin ramp inside the band, exactly 1 outside), computed by the caller
+ * as penalise_field_boundary_{2,3}d.py does; NULL means no penalisation.
+ * filter_type: 0 none, 1 multiplicative, 2 convolution (laplacian_filter_3d.py).
+ */
+int sg_flow_plan_create(int dim, int nz, int ny, int nx, double x_range, int dtype,
+                        int penalty_width, const void* pen_coef_x, const void* pen_coef_y,
+                        const void* pen_coef_z, int filter_type, int filter_order,
+                        sg_flow_plan* plan_out);
+int sg_flow_plan_destroy(sg_flow_plan plan);
+int64_t sg_flow_plan_bytes(sg_flow_plan plan);
+/* Measurement hook (no reference counterpart): arms `n_events` (<= 16)
+ * cudaEvent_t handles that the next sg_flow_step records between its passes,
+ * event i before pass i and the last one after the final pass.  2D passes:
+ * sweep, Poisson load, column convolution, row C2R, curl (6 events).  3D
+ * passes: forcing curl, u x w update, diffusion(+filter), Poisson load, y FFT,
+ * z convolution, y IFFT, x C2R, curl (10 events).  One-shot. */
+int sg_flow_set_timing_events(sg_flow_plan plan, int n_events, void* const* events);
+
+/* One flow time step, in place on the caller's fields.  Replaces
+ * _navier_stokes_with_forcing_time_step / _navier_stokes_time_step
+ * (navier_stokes_flow_simulators.py:171-209 in 2D, :449-498 in 3D).
+ * forcing may be NULL (no body forcing); it is read, then set to zero.
+ * Scalars come from `scalars` or, when `dev_scalars` is not NULL, from that
+ * device struct (written by sg_flow_device_dt).  The max over cells of
+ * sum_d |u_d| of the new velocity is left in the plan for sg_flow_device_dt. */
+int sg_flow_step(sg_flow_plan plan, void* vorticity, void* velocity, void* forcing,
+                 void* stream_func, const sg_step_scalars* scalars,
+                 const sg_step_scalars* dev_scalars, void* stream);
+
+/* max over cells of sum_d |u_d| (passive_transport_flow_simulators.py:149-151).
+ * Written as a double to the device pointer `out` (an 8-byte slot).  */
+int sg_max_abs_sum(int dtype, int dim, int64_t n_cells, const void* velocity, double* out,
+                   void* stream);
+/* Device-resident stable dt: recomputes the plan's max from `velocity` when it
+ * is not NULL, then evaluates compute_advection_diffusion_stable_timestep
+ * (passive_transport_flow_simulators.py:139-155) times dt_prefac, and the step
+ * prefactors, into the plan's device scalar struct.  *dev_scalars_out receives
+ * its device address. */
+int sg_flow_device_dt(sg_flow_plan plan, const void* velocity, double cfl, double nu,
+                      double flow_density, double dt_prefac, const double* free_stream,
+                      const sg_step_scalars** dev_scalars_out, void* stream);
+
+/* ------------------------------------------------ single operators (2D) */
+/* stencil_ops_2d/advection_timestep_2d.py:10-55 (flux buffer internal). */
+int sg_advection_eno3_step_2d(int dtype, int ny, int nx, const void* field_in, void* field_out,
+                              const void* velocity, double dt_by_dx, void* stream);
+/* stencil_ops_2d/diffusion_timestep_2d.py:10-43 */
+int sg_diffusion_step_2d(int dtype, int ny, int nx, const void* field_in, void* field_out,
+                         double nu_dt_by_dx2, void* stream);
+/* stencil_ops_2d/update_vorticity_from_velocity_forcing_2d.py:12-71 */
+int sg_forcing_curl_update_2d(int dtype, int ny, int nx, const void* field_in, void* field_out,
+                              const void* forcing, double prefactor, void* stream);
+/* stencil_ops_2d/outplane_field_curl_2d.py:13-100 */
+int sg_outplane_curl_2d(int dtype, int ny, int nx, const void* psi, void* curl,
+                        double prefactor, void* stream);
+/* stencil_ops_2d/penalise_field_boundary_2d.py:12-142 (out of place) */
+int sg_penalise_2d(int dtype, int ny, int nx, const void* field_in, void* field_out,
+                   int width, const void* coef_x, const void* coef_y, void* stream);
+
+/* ------------------------------------------------ single operators (3D) */
+/* stencil_ops_3d/curl_3d.py:13-132 */
+int sg_curl_3d(int dtype, int nz, int ny, int nx, const void* field, void* curl,
+               double prefactor, void* stream);
+/* stencil_ops_3d/update_vorticity_from_velocity_forcing_3d.py:12-132 */
+int sg_forcing_curl_update_3d(int dtype, int nz, int ny, int nx, const void* field_in,
+                              void* field_out, const void* forcing, double prefactor,
+                              void* stream);
+/* stencil_ops_3d/elementwise_ops_3d.py:390-449 */
+int sg_cross_3d(int dtype, int64_t n_cells, const void* a, const void* b, void* out,
+                void* stream);
+/* stencil_ops_3d/diffusion_timestep_3d.py:12-80 (vector field) */
+int sg_diffusion_step_3d(int dtype, int nz, int ny, int nx, const void* field_in,
+                         void* field_out, double nu_dt_by_dx2, void* stream);
+/* stencil_ops_3d/divergence_3d.py */
+int sg_divergence_3d(int dtype, int nz, int ny, int nx, const void* field, void* div,
+                     double inv_dx, void* stream);
+/* stencil_ops_3d/penalise_field_boundary_3d.py:13-240 (vector field, out of place) */
+int sg_penalise_3d(int dtype, int nz, int ny, int nx, const void* field_in, void* field_out,
+                   int width, const void* coef_x, const void* coef_y, const void* coef_z,
+                   void* stream);
+/* stencil_ops_3d/laplacian_filter_3d.py:13-194 (vector field, in place; the
+ * two scratch buffers hold one scalar field each) */
+int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* field, int filter_type,
+                           int filter_order, void* scratch_a, void* scratch_b, void* stream);
+
+/* ------------------------------------------------------ immersed boundary */
+/* Replaces VirtualBoundaryForcing.compute_interaction_force_on_lag_grid
+ * (immersed_boundary_ops/VirtualBoundaryForcing.py:187-230) with the
+ * support/weights/interpolation kernels of EulerianLagrangianGridCommunicator
+ * {2,3}D.py.  Optionally first applies VirtualBoundaryForcing.time_step
+ * (:276-283), xi += dt * dU, with dt taken from `xi_dt` or from
+ * dev_scalars->dt.
+ *   position, body_velocity: (dim, n_lag) double.
+ *   nearest (dim, n_lag) int32 and weights ((2w)^dim, n_lag) are outputs kept
+ *   for the spreading call; flow_velocity, velocity_mismatch, forcing are
+ *   (dim, n_lag) real outputs; position_mismatch (dim, n_lag) is in/out.
+ *   kernel_type: 0 cosine, 1 Peskin.  Markers whose support leaves the grid
+ *   are skipped and reported with SG_ERR_OUT_OF_DOMAIN through *status_dev. */
+int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, double dx, double shift,
+                      int n_lag, int kernel_type, const double* position,
+                      const double* body_velocity, const void* eul_velocity,
+                      int32_t* nearest, void* weights, void* flow_velocity,
+                      void* velocity_mismatch, void* position_mismatch, void* forcing,
+                      double stiffness, double damping, int do_xi_step, double xi_dt,
+                      const sg_step_scalars* dev_scalars, int32_t* status_dev, void* stream);
+/* Replaces the Lagrangian-to-Eulerian spreading of VirtualBoundaryForcing
+ * (:232-274) and EulerianLagrangianGridCommunicator{2,3}D
+ * (lagrangian_to_eulerian_grid_interpolation_kernel): eul_forcing += sum_i
+ * F_i phi_i, each cell summing its markers in index order (deterministic, no
+ * atomics).  reset != 0 zeroes eul_forcing first (the *_with_eul_grid_forcing_
+ * reset variant). */
+int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag,
+                 const int32_t* nearest, const void* weights, const void* forcing,
+                 void* eul_forcing, int reset, void* stream);
+/* VirtualBoundaryForcing.time_step (:276-283): xi += dt * dU. */
+int sg_ib_mismatch_step(int dtype, int n, void* position_mismatch,
+                        const void* velocity_mismatch, double dt, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOPHT_GB300_H */

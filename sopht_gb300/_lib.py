@@ -1,0 +1,121 @@
+"""ctypes binding of the C ABI in ``include/sopht_gb300.h``.
+
+The library is built in-tree (``sopht_gb300/libsopht_gb300.so``) by
+``sopht_gb300.build``.  There is no fallback: if the library cannot be loaded
+every operator raises, so a missing build can never silently run elsewhere.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libsopht_gb300.so"
+
+SG_OK = 0
+SG_ERR_INVALID_ARG = 1
+SG_ERR_SHAPE = 2
+SG_ERR_CUDA = 3
+SG_ERR_UNSUPPORTED = 4
+SG_ERR_OUT_OF_DOMAIN = 5
+SG_F32 = 0
+SG_F64 = 1
+
+
+class StepScalars(ctypes.Structure):
+    """Mirror of ``sg_step_scalars``."""
+
+    _fields_ = [
+        ("dt", c_double),
+        ("forcing_prefac", c_double),
+        ("advection_prefac", c_double),
+        ("diffusion_prefac", c_double),
+        ("free_stream", c_double * 3),
+    ]
+
+
+_SIGNATURES = {
+    "sg_last_error": (c_char_p, []),
+    "sg_version": (c_int, []),
+    "sg_poisson_plan_create": (c_int, [c_int, c_int, c_int, c_int, c_double, c_int, c_int, POINTER(c_void_p)]),
+    "sg_poisson_plan_destroy": (c_int, [c_void_p]),
+    "sg_poisson_plan_bytes": (c_int64, [c_void_p]),
+    "sg_poisson_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int64, c_void_p]),
+    "sg_flow_plan_create": (c_int, [c_int, c_int, c_int, c_int, c_double, c_int, c_int, c_void_p, c_void_p,
+                                    c_void_p, c_int, c_int, POINTER(c_void_p)]),
+    "sg_flow_plan_destroy": (c_int, [c_void_p]),
+    "sg_flow_plan_bytes": (c_int64, [c_void_p]),
+    "sg_flow_set_timing_events": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),
+    "sg_flow_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, POINTER(StepScalars), c_void_p,
+                             c_void_p]),
+    "sg_max_abs_sum": (c_int, [c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p]),
+    "sg_flow_device_dt": (c_int, [c_void_p, c_void_p, c_double, c_double, c_double, c_double, POINTER(c_double),
+                                  POINTER(c_void_p), c_void_p]),
+    "sg_advection_eno3_step_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_diffusion_step_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_forcing_curl_update_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_outplane_curl_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_penalise_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "sg_curl_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_forcing_curl_update_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double,
+                                          c_void_p]),
+    "sg_cross_3d": (c_int, [c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_diffusion_step_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_divergence_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_penalise_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                               c_void_p]),
+    "sg_laplacian_filter_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                       c_void_p]),
+    "sg_ib_interaction": (c_int, [c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int, c_int, c_void_p,
+                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                  c_double, c_double, c_int, c_double, c_void_p, c_void_p, c_void_p]),
+    "sg_ib_spread": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                             c_int, c_void_p]),
+    "sg_ib_mismatch_step": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+}
+
+_lib = None
+
+
+class SophtGB300Error(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, name: str, status: int, message: str) -> None:
+        super().__init__(f"{name} failed with status {status}: {message}")
+        self.status = status
+
+
+def load(path: Path | str | None = None) -> ctypes.CDLL:
+    """Load the library (once) and attach the argument types of every entry point."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build it with `python -m sopht_gb300.build` (needs nvcc for sm_103a). "
+            "sopht_gb300 has no CPU fallback.")
+    lib = ctypes.CDLL(str(p))
+    for name, (restype, argtypes) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def call(name: str, *args) -> None:
+    """Call entry point ``name``; raise ValueError/RuntimeError on failure."""
+    lib = load()
+    status = getattr(lib, name)(*args)
+    if status != SG_OK:
+        msg = (lib.sg_last_error() or b"").decode(errors="replace")
+        if status in (SG_ERR_INVALID_ARG, SG_ERR_SHAPE, SG_ERR_UNSUPPORTED):
+            raise ValueError(f"{name}: {msg}")
+        raise SophtGB300Error(name, status, msg)
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGNATURES)

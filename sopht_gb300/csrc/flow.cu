@@ -1,0 +1,494 @@
+// Flow-step plan and the fused 2D/3D time step of the unbounded vorticity
+// Navier-Stokes simulators (navier_stokes_flow_simulators.py:171-209, 449-498).
+//
+// 2D step (5 kernels):  sweep (forcing curl + ENO3 + diffusion) -> Poisson load
+//   (penalise, write vorticity back, zero forcing, x R2C) -> column convolution
+//   -> x C2R -> curl + free stream + max|u|.
+// 3D step: forcing curl -> u x w curl update -> diffusion [-> filter] ->
+//   Poisson load (penalise, write back, zero forcing, x R2C, all 3 components)
+//   -> y FFT -> z FFT * G * IFFT -> y IFFT -> x C2R -> curl + free stream + max.
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+
+#include "flow_kernels.cuh"
+#include "poisson.cuh"
+
+namespace sg {
+int poisson_plan_create_impl(int, int, int, int, double, int, int, sg_poisson_plan_s**);
+void poisson_plan_free(sg_poisson_plan_s*);
+}  // namespace sg
+
+struct sg_flow_plan_s {
+    int dim = 2, nz = 1, ny = 0, nx = 0, dtype = SG_F32;
+    int width = 0, filter_type = 0, filter_order = 0;
+    double x_range = 1.0, dx = 0.0;
+    sg_poisson_plan_s* poisson = nullptr;
+    void* scratch_a = nullptr;  // vector field
+    void* scratch_b = nullptr;  // vector field (3D)
+    void* filt_a = nullptr;     // scalar field (3D filter)
+    void* filt_b = nullptr;
+    void* coef_x = nullptr;
+    void* coef_y = nullptr;
+    void* coef_z = nullptr;
+    // device block: [0, 64) sg_step_scalars, [64, 72) umax (field type), [72, 80) time
+    unsigned char* dev_block = nullptr;
+    int64_t bytes = 0;
+    // optional one-shot timing events recorded between the passes of the next step
+    int n_events = 0;
+    cudaEvent_t events[16] = {};
+    sg_step_scalars* dev_scalars() const { return reinterpret_cast<sg_step_scalars*>(dev_block); }
+    void* umax_slot() const { return dev_block + 64; }
+    double* time_slot() const { return reinterpret_cast<double*>(dev_block + 72); }
+    int64_t cells() const { return (int64_t)nz * ny * nx; }
+};
+
+namespace sg {
+
+// Record timing event `i` of the armed set (no-op when none is armed).
+static inline void mark(sg_flow_plan_s* p, int i, cudaStream_t stream) {
+    if (i < p->n_events && p->events[i]) cudaEventRecord(p->events[i], stream);
+}
+
+static void flow_plan_free(sg_flow_plan_s* p) {
+    if (!p) return;
+    poisson_plan_free(p->poisson);
+    cudaFree(p->scratch_a);
+    cudaFree(p->scratch_b);
+    cudaFree(p->filt_a);
+    cudaFree(p->filt_b);
+    cudaFree(p->coef_x);
+    cudaFree(p->coef_y);
+    cudaFree(p->coef_z);
+    cudaFree(p->dev_block);
+    delete p;
+}
+
+static int alloc_into(void** dst, size_t bytes, int64_t* total, const char* what) {
+    SG_TRY(cuda_status(cudaMalloc(dst, bytes), what));
+    *total += (int64_t)bytes;
+    return SG_OK;
+}
+
+static int upload_coef(void** dst, const void* host, int n, int esz, int64_t* total) {
+    if (!host) return SG_OK;
+    SG_TRY(alloc_into(dst, (size_t)n * esz, total, "penalisation table alloc"));
+    return cuda_status(cudaMemcpy(*dst, host, (size_t)n * esz, cudaMemcpyHostToDevice), "penalisation upload");
+}
+
+// ---------------------------------------------------------------- launchers
+template <typename T>
+int launch_sweep2d(const Sweep2DParams<T>& p, cudaStream_t stream) {
+    constexpr int TX = 32;
+    constexpr int TY = sizeof(T) == 4 ? 16 : 8;
+    dim3 grid(ceil_div(p.nx, TX), ceil_div(p.ny, TY));
+    sweep2d_kernel<T, TX, TY><<<grid, dim3(TX, 8), 0, stream>>>(p);
+    return launch_status("sweep2d");
+}
+
+template <typename T>
+int launch_flow_load(FlowLoadParams<T> p, cudaStream_t stream) {
+    const int esz = sizeof(cplx_t<T>);
+    const int rb = rows_per_block_for(p.st.n, esz);
+    const size_t smem = 2ull * rb * p.st.n * esz;
+    auto kern = flow_load_kernel<T>;
+    SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "flow_load smem attribute"));
+    kern<<<ceil_div(p.n_rows, rb), dim3(256 / rb, rb), smem, stream>>>(p);
+    return launch_status("flow_load");
+}
+
+template <typename T>
+int launch_curl2d(const Curl2DParams<T>& p, cudaStream_t stream) {
+    dim3 block(32, 8);
+    dim3 grid(ceil_div(p.nx, 32), ceil_div(p.ny, 8));
+    curl2d_kernel<T><<<grid, block, 0, stream>>>(p);
+    return launch_status("curl2d");
+}
+
+template <typename T>
+int launch_curl3d(const Curl3DParams<T>& p, int64_t n, cudaStream_t stream) {
+    curl3d_kernel<T><<<ceil_div(n, 256), 256, 0, stream>>>(p);
+    return launch_status("curl3d");
+}
+
+template <typename T>
+int filter3d(Grid3 G, T* field, int filter_type, int order, T* a, T* b, cudaStream_t stream) {
+    if (filter_type == 0 || order <= 0) return SG_OK;
+    const int64_t n = (int64_t)G.nz * G.ny * G.nx;
+    const unsigned blocks = ceil_div(n, 256);
+    for (int c = 0; c < 3; ++c) {
+        T* phi = field + c * n;
+        if (filter_type == 1) {
+            // multiplicative: (Lz Ly Lx)^order phi, subtracted once
+            const T* src = phi;
+            T* bufs[2] = {a, b};
+            int which = 0;
+            for (int it = 0; it < order; ++it) {
+                for (int axis = 0; axis < 3; ++axis) {
+                    T* dst = bufs[which];
+                    filter_pass3d_kernel<T><<<blocks, 256, 0, stream>>>(G, src, dst, axis);
+                    src = dst;
+                    which ^= 1;
+                }
+            }
+            subtract_kernel<T><<<blocks, 256, 0, stream>>>(n, phi, src);
+        } else {
+            // convolution: per axis, L_axis^order phi subtracted before the next axis
+            for (int axis = 0; axis < 3; ++axis) {
+                const T* src = phi;
+                T* bufs[2] = {a, b};
+                int which = 0;
+                for (int it = 0; it < order; ++it) {
+                    T* dst = bufs[which];
+                    filter_pass3d_kernel<T><<<blocks, 256, 0, stream>>>(G, src, dst, axis);
+                    src = dst;
+                    which ^= 1;
+                }
+                subtract_kernel<T><<<blocks, 256, 0, stream>>>(n, phi, src);
+            }
+        }
+    }
+    return launch_status("laplacian filter");
+}
+
+template int filter3d<float>(Grid3, float*, int, int, float*, float*, cudaStream_t);
+template int filter3d<double>(Grid3, double*, int, int, double*, double*, cudaStream_t);
+
+template <typename T>
+static FlowLoadParams<T> load_params(sg_flow_plan_s* p, const T* src, T* dst, T* forcing) {
+    sg_poisson_plan_s* pp = p->poisson;
+    FlowLoadParams<T> l{};
+    l.dim = p->dim;
+    l.nz = p->nz;
+    l.ny = p->ny;
+    l.nx = p->nx;
+    l.width = p->width;
+    l.src = src;
+    l.dst = dst;
+    l.forcing = forcing;
+    l.cx = (const T*)p->coef_x;
+    l.cy = (const T*)p->coef_y;
+    l.cz = (const T*)p->coef_z;
+    l.comp_stride = p->cells();
+    l.spec = reinterpret_cast<cplx_t<T>*>(pp->spec);
+    if (p->dim == 2) {
+        l.spec_map = row_map(p->ny, p->nx + 1, 1, 0, pp->spec_comp_elems);
+        l.n_rows = p->ny;
+    } else {
+        l.spec_map = row_map(p->ny, p->nx + 1, p->nz, (int64_t)2 * p->ny * (p->nx + 1), pp->spec_comp_elems);
+        l.n_rows = 3 * p->nz * p->ny;
+    }
+    l.st = pp->st_x;
+    l.tw_m = (const cplx_t<T>*)pp->tw_x;
+    l.tw_l = (const cplx_t<T>*)pp->tw_xl;
+    return l;
+}
+
+template <typename T>
+int flow_step_2d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& sc, bool free_stream,
+                 cudaStream_t stream) {
+    Sweep2DParams<T> s{};
+    s.ny = p->ny;
+    s.nx = p->nx;
+    s.w = w;
+    s.u = u;
+    s.f = f;
+    s.out = (T*)p->scratch_a;
+    s.sc = sc;
+    s.flags = SWEEP_ADVECT | SWEEP_DIFFUSE;
+    mark(p, 0, stream);
+    SG_TRY(launch_sweep2d<T>(s, stream));
+    mark(p, 1, stream);
+    FlowLoadParams<T> l = load_params<T>(p, (const T*)p->scratch_a, w, nullptr);
+    SG_TRY(launch_flow_load<T>(l, stream));
+    if (f) SG_TRY(cuda_status(cudaMemsetAsync(f, 0, 2 * sizeof(T) * p->cells(), stream), "forcing reset"));
+    mark(p, 2, stream);
+    SG_TRY(poisson_spectral_passes<T>(p->poisson, 1, stream));
+    mark(p, 3, stream);
+    SG_TRY(poisson_store_rows<T>(p->poisson, psi, 1, 0, stream));
+    mark(p, 4, stream);
+    SG_TRY(cuda_status(cudaMemsetAsync(p->umax_slot(), 0, 8, stream), "umax reset"));
+    Curl2DParams<T> c{};
+    c.ny = p->ny;
+    c.nx = p->nx;
+    c.psi = psi;
+    c.u = u;
+    c.prefactor = T(0.5) / (T)p->dx;
+    c.sc = sc;
+    c.add_free_stream = free_stream;
+    c.umax = (T*)p->umax_slot();
+    SG_TRY(launch_curl2d<T>(c, stream));
+    mark(p, 5, stream);
+    return SG_OK;
+}
+
+// The three spectral passes of the 3D solve with timing marks 5 and 6 between them.
+template <typename T>
+int poisson_spectral_passes_marked(sg_flow_plan_s* p, int ncomp, cudaStream_t stream) {
+    SG_TRY(poisson_spectral_pass3d<T>(p->poisson, ncomp, 0, stream));
+    mark(p, 5, stream);
+    SG_TRY(poisson_spectral_pass3d<T>(p->poisson, ncomp, 1, stream));
+    mark(p, 6, stream);
+    return poisson_spectral_pass3d<T>(p->poisson, ncomp, 2, stream);
+}
+
+template <typename T>
+int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& sc, bool free_stream,
+                 cudaStream_t stream) {
+    const int64_t n = p->cells();
+    const unsigned blocks = ceil_div(n, 256);
+    Grid3 G{p->nz, p->ny, p->nx};
+    T* A = (T*)p->scratch_a;
+    T* B = (T*)p->scratch_b;
+    const T* w1 = w;
+    mark(p, 0, stream);
+    if (f) {
+        Stencil3DParams<T> s{};
+        s.grid = G;
+        s.a = w;
+        s.b = f;
+        s.out = A;
+        s.sc = sc;
+        s.mode = 0;
+        forcing_curl3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
+        SG_TRY(launch_status("forcing_curl3d"));
+        w1 = A;
+    }
+    mark(p, 1, stream);
+    {
+        Stencil3DParams<T> s{};
+        s.grid = G;
+        s.a = w1;
+        s.b = u;
+        s.out = B;
+        s.sc = sc;
+        rotational_update3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
+        SG_TRY(launch_status("rotational_update3d"));
+    }
+    mark(p, 2, stream);
+    {
+        Stencil3DParams<T> s{};
+        s.grid = G;
+        s.a = B;
+        s.out = A;
+        s.sc = sc;
+        s.mode = 0;
+        diffusion3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
+        SG_TRY(launch_status("diffusion3d"));
+    }
+    SG_TRY(filter3d<T>(G, A, p->filter_type, p->filter_order, (T*)p->filt_a, (T*)p->filt_b, stream));
+    mark(p, 3, stream);
+    FlowLoadParams<T> l = load_params<T>(p, A, w, f);
+    SG_TRY(launch_flow_load<T>(l, stream));
+    mark(p, 4, stream);
+    SG_TRY(poisson_spectral_passes_marked<T>(p, 3, stream));
+    mark(p, 7, stream);
+    SG_TRY(poisson_store_rows<T>(p->poisson, psi, 3, n, stream));
+    mark(p, 8, stream);
+    SG_TRY(cuda_status(cudaMemsetAsync(p->umax_slot(), 0, 8, stream), "umax reset"));
+    Curl3DParams<T> c{};
+    c.grid = G;
+    c.psi = psi;
+    c.u = u;
+    c.prefactor = T(0.5) / (T)p->dx;
+    c.sc = sc;
+    c.add_free_stream = free_stream;
+    c.umax = (T*)p->umax_slot();
+    SG_TRY(launch_curl3d<T>(c, n, stream));
+    mark(p, 9, stream);
+    return SG_OK;
+}
+
+// max over cells of sum_d |v_d| into a field-typed slot (atomic, order free)
+template <typename T>
+__global__ void __launch_bounds__(256) max_abs_sum_kernel(int64_t n, int dim, const T* v, T* slot) {
+    T m = T(0);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T s = fabs(v[i]);
+        for (int d = 1; d < dim; ++d) s = s + fabs(v[d * n + i]);
+        m = fmax(m, s);
+    }
+    m = block_max(m);
+    if (threadIdx.x == 0) atomic_max_nonneg(slot, m);
+}
+
+template <typename T>
+int launch_max_abs_sum(int64_t n, int dim, const T* v, T* slot, cudaStream_t stream) {
+    SG_TRY(cuda_status(cudaMemsetAsync(slot, 0, sizeof(T), stream), "max slot reset"));
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 8);
+    max_abs_sum_kernel<T><<<blocks, 256, 0, stream>>>(n, dim, v, slot);
+    return launch_status("max_abs_sum");
+}
+
+template <typename T>
+__global__ void slot_to_double_kernel(const T* slot, double* out) {
+    *out = (double)*slot;
+}
+
+// compute_advection_diffusion_stable_timestep (passive_transport_flow_simulators.
+// py:139-155) evaluated in the field precision with numpy's promotion rules:
+// Python scalars take the field type, so every operation rounds to T.
+template <typename T>
+__global__ void device_dt_kernel(const T* umax_slot, sg_step_scalars* sc, double* time, int dim, T dx, double cfl,
+                                 double nu, double rho, double dt_prefac, double fs0, double fs1, double fs2) {
+    const T eps = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
+    const T tol = T(10) * eps;
+    const T umax = *umax_slot;
+    const T a = (T)cfl * dx / (umax + tol);
+    const T b = (T)0.9 * (dx * dx) / (T)(2 * dim) / (T)nu + tol;
+    T dt = b < a ? b : a;
+    dt = dt * (T)dt_prefac;
+    sc->dt = (double)dt;
+    T d2 = T(2) * dx;
+    d2 = d2 * (T)rho;
+    sc->forcing_prefac = (double)(dt / d2);
+    sc->advection_prefac = dim == 2 ? (double)(dt / dx) : (double)(dt / (T(2) * dx));
+    const T nudt = (T)nu * dt;
+    sc->diffusion_prefac = (double)(nudt / dx / dx);
+    sc->free_stream[0] = fs0;
+    sc->free_stream[1] = fs1;
+    sc->free_stream[2] = fs2;
+    *time += (double)dt;
+}
+
+template <typename T>
+int device_dt(sg_flow_plan_s* p, const void* velocity, double cfl, double nu, double rho, double prefac,
+              const double* fs, cudaStream_t stream) {
+    if (velocity)
+        SG_TRY(launch_max_abs_sum<T>(p->cells(), p->dim, (const T*)velocity, (T*)p->umax_slot(), stream));
+    device_dt_kernel<T><<<1, 1, 0, stream>>>((const T*)p->umax_slot(), p->dev_scalars(), p->time_slot(), p->dim,
+                                             (T)p->dx, cfl, nu, rho, prefac, fs ? fs[0] : 0.0, fs ? fs[1] : 0.0,
+                                             fs ? fs[2] : 0.0);
+    return launch_status("device_dt");
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sg_flow_plan_create(int dim, int nz, int ny, int nx, double x_range, int dtype, int width,
+                                   const void* cx, const void* cy, const void* cz, int filter_type,
+                                   int filter_order, sg_flow_plan* out) {
+    SG_REQUIRE(out != nullptr, SG_ERR_INVALID_ARG, "flow plan: null output pointer");
+    *out = nullptr;
+    SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "flow plan: dim must be 2 or 3");
+    SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, SG_ERR_INVALID_ARG, "flow plan: bad dtype");
+    if (dim == 2) nz = 1;
+    SG_REQUIRE(nx >= 6 && ny >= 6 && (dim == 2 || nz >= 6), SG_ERR_SHAPE,
+               "flow plan: each extent must be >= 6 (got %d, %d, %d)", nz, ny, nx);
+    SG_REQUIRE(width >= 0 && 2 * width <= nx && 2 * width <= ny && (dim == 2 || 2 * width <= nz), SG_ERR_SHAPE,
+               "flow plan: penalty width %d does not fit the grid", width);
+    SG_REQUIRE(width == 0 || (cx && cy && (dim == 2 || cz)), SG_ERR_INVALID_ARG,
+               "flow plan: penalisation tables required for width > 0");
+    SG_REQUIRE(filter_type >= 0 && filter_type <= 2 && filter_order >= 0, SG_ERR_INVALID_ARG,
+               "flow plan: bad filter setting");
+    SG_REQUIRE(dim == 3 || filter_type == 0, SG_ERR_INVALID_ARG, "flow plan: the filter is 3D only");
+    auto* p = new sg_flow_plan_s();
+    p->dim = dim;
+    p->nz = nz;
+    p->ny = ny;
+    p->nx = nx;
+    p->dtype = dtype;
+    p->width = width;
+    p->filter_type = filter_type;
+    p->filter_order = filter_order;
+    p->x_range = x_range;
+    p->dx = dtype == SG_F32 ? (double)(float)(x_range / nx) : x_range / nx;
+    const int esz = dtype_size(dtype);
+    const int64_t n = p->cells();
+    int st = SG_OK;
+    do {
+        if ((st = poisson_plan_create_impl(dim, nz, ny, nx, x_range, dtype, dim == 3 ? 3 : 1, &p->poisson))) break;
+        p->bytes += p->poisson->bytes;
+        if ((st = alloc_into(&p->scratch_a, (size_t)dim * n * esz, &p->bytes, "flow scratch alloc"))) break;
+        if (dim == 3 && (st = alloc_into(&p->scratch_b, (size_t)3 * n * esz, &p->bytes, "flow scratch alloc"))) break;
+        if (filter_type != 0) {
+            if ((st = alloc_into(&p->filt_a, (size_t)n * esz, &p->bytes, "filter scratch alloc"))) break;
+            if ((st = alloc_into(&p->filt_b, (size_t)n * esz, &p->bytes, "filter scratch alloc"))) break;
+        }
+        if (width > 0) {
+            if ((st = upload_coef(&p->coef_x, cx, nx, esz, &p->bytes))) break;
+            if ((st = upload_coef(&p->coef_y, cy, ny, esz, &p->bytes))) break;
+            if (dim == 3 && (st = upload_coef(&p->coef_z, cz, nz, esz, &p->bytes))) break;
+        }
+        if ((st = alloc_into((void**)&p->dev_block, 128, &p->bytes, "flow device block alloc"))) break;
+        if ((st = cuda_status(cudaMemset(p->dev_block, 0, 128), "flow device block init"))) break;
+        st = cuda_status(cudaDeviceSynchronize(), "flow plan create");
+    } while (0);
+    if (st != SG_OK) {
+        flow_plan_free(p);
+        return st;
+    }
+    *out = p;
+    return SG_OK;
+}
+
+extern "C" int sg_flow_set_timing_events(sg_flow_plan p, int n_events, void* const* events) {
+    SG_REQUIRE(p && n_events >= 0 && n_events <= 16 && (n_events == 0 || events), SG_ERR_INVALID_ARG,
+               "timing events: bad argument");
+    p->n_events = n_events;
+    for (int i = 0; i < 16; ++i) p->events[i] = i < n_events ? (cudaEvent_t)events[i] : nullptr;
+    return SG_OK;
+}
+
+extern "C" int sg_flow_plan_destroy(sg_flow_plan p) {
+    flow_plan_free(p);
+    return SG_OK;
+}
+
+extern "C" int64_t sg_flow_plan_bytes(sg_flow_plan p) { return p ? p->bytes : 0; }
+
+extern "C" int sg_flow_step(sg_flow_plan p, void* w, void* u, void* f, void* psi, const sg_step_scalars* scalars,
+                            const sg_step_scalars* dev_scalars, void* stream_) {
+    SG_REQUIRE(p && w && u && psi, SG_ERR_INVALID_ARG, "flow step: null argument");
+    SG_REQUIRE(scalars || dev_scalars, SG_ERR_INVALID_ARG, "flow step: no step scalars");
+    ScalarSrc sc{};
+    if (scalars) sc.host = *scalars;
+    sc.dev = dev_scalars;
+    const bool fs = dev_scalars != nullptr || (scalars && (scalars->free_stream[0] != 0.0 ||
+                                                          scalars->free_stream[1] != 0.0 ||
+                                                          scalars->free_stream[2] != 0.0));
+    auto stream = (cudaStream_t)stream_;
+    int st;
+    if (p->dtype == SG_F32) {
+        st = p->dim == 2 ? flow_step_2d<float>(p, (float*)w, (float*)u, (float*)f, (float*)psi, sc, fs, stream)
+                         : flow_step_3d<float>(p, (float*)w, (float*)u, (float*)f, (float*)psi, sc, fs, stream);
+    } else {
+        st = p->dim == 2 ? flow_step_2d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream)
+                         : flow_step_3d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream);
+    }
+    p->n_events = 0;  // timing events are armed for one step only
+    return st;
+}
+
+extern "C" int sg_max_abs_sum(int dtype, int dim, int64_t n, const void* v, double* out, void* stream_) {
+    SG_REQUIRE(v && out && n > 0 && dim >= 1 && dim <= 3, SG_ERR_INVALID_ARG, "max_abs_sum: bad argument");
+    auto stream = (cudaStream_t)stream_;
+    if (dtype == SG_F32) {
+        float* slot = reinterpret_cast<float*>(out);
+        SG_TRY(launch_max_abs_sum<float>(n, dim, (const float*)v, slot, stream));
+        slot_to_double_kernel<float><<<1, 1, 0, stream>>>(slot, out);
+        return launch_status("max_abs_sum finalize");
+    }
+    SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "max_abs_sum: bad dtype");
+    return launch_max_abs_sum<double>(n, dim, (const double*)v, reinterpret_cast<double*>(out), stream);
+}
+
+extern "C" int sg_flow_device_dt(sg_flow_plan p, const void* velocity, double cfl, double nu, double rho,
+                                 double dt_prefac, const double* free_stream, const sg_step_scalars** dev_out,
+                                 void* stream_) {
+    SG_REQUIRE(p, SG_ERR_INVALID_ARG, "device dt: null plan");
+    auto stream = (cudaStream_t)stream_;
+    int st = p->dtype == SG_F32 ? device_dt<float>(p, velocity, cfl, nu, rho, dt_prefac, free_stream, stream)
+                                : device_dt<double>(p, velocity, cfl, nu, rho, dt_prefac, free_stream, stream);
+    if (dev_out) *dev_out = p->dev_scalars();
+    return st;
+}
+
+namespace sg {
+template int launch_sweep2d<float>(const Sweep2DParams<float>&, cudaStream_t);
+template int launch_sweep2d<double>(const Sweep2DParams<double>&, cudaStream_t);
+template int launch_curl2d<float>(const Curl2DParams<float>&, cudaStream_t);
+template int launch_curl2d<double>(const Curl2DParams<double>&, cudaStream_t);
+}  // namespace sg

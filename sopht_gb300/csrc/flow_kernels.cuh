@@ -1,0 +1,500 @@
+// Stencil kernels of the unbounded vorticity Navier-Stokes step.
+//
+// Boundary conventions follow the reference's pystencils kernels, which
+// iterate the interior with as many ghost layers as the largest stencil offset
+// on every axis:
+//   forcing curl update   [1:-1]   ring unchanged  (update_vorticity_from_velocity_forcing_{2,3}d.py)
+//   ENO3 advection flux   [2:-2]   zero elsewhere  (advection_flux_2d.py)
+//   diffusion flux        [1:-1]   zero ring       (diffusion_flux_{2,3}d.py)
+//   curl                  [1:-1]   zero ring       (outplane_field_curl_2d.py, curl_3d.py)
+#pragma once
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace sg {
+
+// Step scalars: from the device struct when given, else the by-value copy.
+struct ScalarSrc {
+    sg_step_scalars host;
+    const sg_step_scalars* dev;
+    __device__ __forceinline__ double dt() const { return dev ? dev->dt : host.dt; }
+    __device__ __forceinline__ double forcing() const { return dev ? dev->forcing_prefac : host.forcing_prefac; }
+    __device__ __forceinline__ double advection() const { return dev ? dev->advection_prefac : host.advection_prefac; }
+    __device__ __forceinline__ double diffusion() const { return dev ? dev->diffusion_prefac : host.diffusion_prefac; }
+    __device__ __forceinline__ double free_stream(int c) const { return dev ? dev->free_stream[c] : host.free_stream[c]; }
+};
+
+// ---------------------------------------------------------------- 2D sweep
+// One fused pass: w1 = w + pf curl(f) ; w2 = w1 + ENO3 flux(w1, u) ;
+// w3 = w2 + k lap(w2).  Output w3 goes to a separate buffer (the caller's
+// vorticity is rewritten by the Poisson load pass) because neighbouring tiles
+// still read the input halo.
+enum { SWEEP_ADVECT = 1, SWEEP_DIFFUSE = 2 };
+
+template <typename T> struct Sweep2DParams {
+    int ny, nx;
+    const T* w;
+    const T* u;   // (2, ny, nx), may be null without SWEEP_ADVECT
+    const T* f;   // (2, ny, nx) or null
+    T* out;
+    ScalarSrc sc;
+    int flags;    // SWEEP_ADVECT | SWEEP_DIFFUSE
+};
+
+template <typename T>
+__device__ __forceinline__ T eno3_face(T qm1, T q0, T qp1, T qp2, T u0, T up1) {
+    const T third = T(1.0 / 3.0), five6 = T(5.0 / 6.0), sixth = T(1.0 / 6.0);
+    // advection_flux_2d.py:35-47: left-biased when u_0 > -u_{+1}
+    if (u0 > -up1) return third * qp1 + five6 * q0 - sixth * qm1;
+    return third * q0 + five6 * qp1 - sixth * qp2;
+}
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX * 8) sweep2d_kernel(Sweep2DParams<T> p) {
+    constexpr int HW = 3, HF = 4;
+    constexpr int WX = TX + 2 * HW, WY = TY + 2 * HW;
+    constexpr int FX = TX + 2 * HF, FY = TY + 2 * HF;
+    constexpr int W2X = TX + 2, W2Y = TY + 2;
+    __shared__ T s_fx[FY * FX];
+    __shared__ T s_fy[FY * FX];
+    __shared__ T s_w[WY * WX];
+    __shared__ T s_ux[WY * WX];
+    __shared__ T s_uy[WY * WX];
+    __shared__ T s_w1[WY * WX];
+    __shared__ T s_w2[W2Y * W2X];
+    const int nthr = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int ny = p.ny, nx = p.nx;
+    const int64_t plane = (int64_t)ny * nx;
+    const bool forcing = p.f != nullptr;
+    // load
+    for (int e = tid; e < WY * WX; e += nthr) {
+        const int gy = y0 - HW + e / WX, gx = x0 - HW + e % WX;
+        T w = T(0), ux = T(0), uy = T(0);
+        if (gy >= 0 && gy < ny && gx >= 0 && gx < nx) {
+            const int64_t g = (int64_t)gy * nx + gx;
+            w = p.w[g];
+            if (p.u) {
+                ux = p.u[g];
+                uy = p.u[plane + g];
+            }
+        }
+        s_w[e] = w;
+        s_ux[e] = ux;
+        s_uy[e] = uy;
+    }
+    if (forcing) {
+        for (int e = tid; e < FY * FX; e += nthr) {
+            const int gy = y0 - HF + e / FX, gx = x0 - HF + e % FX;
+            T fx = T(0), fy = T(0);
+            if (gy >= 0 && gy < ny && gx >= 0 && gx < nx) {
+                const int64_t g = (int64_t)gy * nx + gx;
+                fx = p.f[g];
+                fy = p.f[plane + g];
+            }
+            s_fx[e] = fx;
+            s_fy[e] = fy;
+        }
+    }
+    __syncthreads();
+    // w1 on the halo-3 region
+    const T pf = (T)p.sc.forcing();
+    for (int e = tid; e < WY * WX; e += nthr) {
+        const int ly = e / WX, lx = e % WX;
+        const int gy = y0 - HW + ly, gx = x0 - HW + lx;
+        T w1 = s_w[e];
+        if (forcing && gy >= 1 && gy <= ny - 2 && gx >= 1 && gx <= nx - 2) {
+            const int fe = (ly + 1) * FX + (lx + 1);
+            const T curl = s_fy[fe + 1] - s_fy[fe - 1] - s_fx[fe + FX] + s_fx[fe - FX];
+            w1 = w1 + curl * pf;
+        }
+        s_w1[e] = w1;
+    }
+    __syncthreads();
+    // w2 = w1 + ENO3 flux on the halo-1 region
+    const T inv_dx = -(T)p.sc.advection();
+    for (int e = tid; e < W2Y * W2X; e += nthr) {
+        const int ly = e / W2X + 2, lx = e % W2X + 2;  // coordinates in the halo-3 frame
+        const int gy = y0 - HW + ly, gx = x0 - HW + lx;
+        const int c = ly * WX + lx;
+        T w2 = s_w1[c];
+        if ((p.flags & SWEEP_ADVECT) && gy >= 2 && gy <= ny - 3 && gx >= 2 && gx <= nx - 3) {
+            auto qx = [&](int d) { return s_w1[c + d] * s_ux[c + d]; };
+            auto qy = [&](int d) { return s_w1[c + d * WX] * s_uy[c + d * WX]; };
+            const T east = eno3_face(qx(-1), qx(0), qx(1), qx(2), s_ux[c], s_ux[c + 1]);
+            const T west = eno3_face(qx(-2), qx(-1), qx(0), qx(1), s_ux[c - 1], s_ux[c]);
+            const T north = eno3_face(qy(-1), qy(0), qy(1), qy(2), s_uy[c], s_uy[c + WX]);
+            const T south = eno3_face(qy(-2), qy(-1), qy(0), qy(1), s_uy[c - WX], s_uy[c]);
+            T flux = inv_dx * east;
+            flux = flux - inv_dx * west;
+            flux = flux + inv_dx * north;
+            flux = flux - inv_dx * south;
+            w2 = w2 + flux;
+        }
+        s_w2[e] = w2;
+    }
+    __syncthreads();
+    // w3 = w2 + k lap(w2) on the tile
+    const T k = (T)p.sc.diffusion();
+    for (int e = tid; e < TY * TX; e += nthr) {
+        const int ly = e / TX, lx = e % TX;
+        const int gy = y0 + ly, gx = x0 + lx;
+        if (gy >= ny || gx >= nx) continue;
+        const int c = (ly + 1) * W2X + (lx + 1);
+        T w3 = s_w2[c];
+        if ((p.flags & SWEEP_DIFFUSE) && gy >= 1 && gy <= ny - 2 && gx >= 1 && gx <= nx - 2) {
+            const T lap = s_w2[c + W2X] + s_w2[c - W2X] + s_w2[c + 1] + s_w2[c - 1] - T(4) * s_w2[c];
+            w3 = w3 + k * lap;
+        }
+        p.out[(int64_t)gy * nx + gx] = w3;
+    }
+}
+
+// --------------------------------------------- fused Poisson load (x rows R2C)
+// Row q of component c (3D: q -> (c, z, y); 2D: q -> y).  Reads the swept
+// vorticity `src`, applies the boundary penalisation by index clamping and the
+// per-index sine factors (X pass, then Y, then Z, as penalise_field_boundary_
+// {2,3}d.py orders them), writes the result back to the caller's vorticity,
+// zeroes the forcing row, and emits the M+1 bins of the zero-padded row.
+template <typename T> struct FlowLoadParams {
+    int dim, nz, ny, nx;
+    int width;               // penalty zone width (0: none)
+    const T* src;            // swept vorticity, same layout as dst
+    T* dst;                  // caller's vorticity (penalised copy)
+    T* forcing;              // zeroed when not null
+    const T* cx;             // penalisation factors per index (null if width 0)
+    const T* cy;
+    const T* cz;
+    int64_t comp_stride;     // elements between components of src/dst/forcing
+    cplx_t<T>* spec;
+    RowMap spec_map;
+    int n_rows;
+    FFTStages st;
+    const cplx_t<T>* tw_m;
+    const cplx_t<T>* tw_l;
+};
+
+__device__ __forceinline__ int clamp_band(int i, int n, int w) {
+    if (w <= 0) return i;
+    return i < w - 1 ? w - 1 : (i > n - w ? n - w : i);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) flow_load_kernel(FlowLoadParams<T> p) {
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int M = p.st.n;
+    const int rb = blockDim.y;
+    C* buf0 = reinterpret_cast<C*>(smem_raw);
+    C* buf1 = buf0 + rb * M;
+    const int row0 = blockIdx.x * rb;
+    const int nthr = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nx = p.nx;
+    for (int e = tid; e < rb * M; e += nthr) {
+        const int r = e / M, n = e % M;
+        const int q = row0 + r;
+        C z = cmake<C>(T(0), T(0));
+        if (q < p.n_rows && 2 * n < nx) {
+            int y = q % p.ny, c, zi;
+            if (p.dim == 3) {
+                zi = (q / p.ny) % p.nz;
+                c = q / (p.ny * p.nz);
+            } else {
+                zi = 0;
+                c = q / p.ny;
+            }
+            const int sy = clamp_band(y, p.ny, p.width);
+            const int sz = p.dim == 3 ? clamp_band(zi, p.nz, p.width) : 0;
+            const int64_t src_row = (int64_t)c * p.comp_stride + ((int64_t)sz * p.ny + sy) * nx;
+            const int64_t dst_row = (int64_t)c * p.comp_stride + ((int64_t)zi * p.ny + y) * nx;
+            T v[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int x = 2 * n + h;
+                T val = T(0);
+                if (x < nx) {
+                    const int sx = clamp_band(x, nx, p.width);
+                    val = p.src[src_row + sx];
+                    if (p.width > 0) {
+                        val = val * p.cx[x];
+                        val = val * p.cy[y];
+                        if (p.dim == 3) val = val * p.cz[zi];
+                    }
+                    p.dst[dst_row + x] = val;
+                    if (p.forcing) p.forcing[dst_row + x] = T(0);
+                }
+                v[h] = val;
+            }
+            z = cmake<C>(v[0], v[1]);
+        }
+        buf0[r * M + n] = z;
+    }
+    __syncthreads();
+    C* Z = fft_smem<false, false>(buf0, buf1, p.st, rb, 1, M, p.tw_m);
+    for (int e = tid; e < rb * (M + 1); e += nthr) {
+        const int r = e / (M + 1), k = e % (M + 1);
+        const int q = row0 + r;
+        if (q >= p.n_rows) continue;
+        const C zk = Z[r * M + (k == M ? 0 : k)];
+        const C zc = cconj(Z[r * M + (k == 0 ? 0 : M - k)]);
+        const C w = p.tw_l[k];
+        const C s = cadd(zk, zc);
+        const C wd = cmul(w, csub(zk, zc));
+        p.spec[p.spec_map.offset(q) + k] = cmake<C>(T(0.5) * (s.x + wd.y), T(0.5) * (s.y - wd.x));
+    }
+}
+
+// ---------------------------------------- curl + free stream + max |u| (2D)
+template <typename T>
+__device__ __forceinline__ void atomic_max_nonneg(T* slot, T v);
+template <>
+__device__ __forceinline__ void atomic_max_nonneg<float>(float* slot, float v) {
+    atomicMax(reinterpret_cast<int*>(slot), __float_as_int(v));
+}
+template <>
+__device__ __forceinline__ void atomic_max_nonneg<double>(double* slot, double v) {
+    atomicMax(reinterpret_cast<unsigned long long*>(slot), (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__device__ __forceinline__ T block_max(T v) {
+    __shared__ T warp_max[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nw = (blockDim.x * blockDim.y + 31) / 32;
+    if ((tid & 31) == 0) warp_max[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+        v = tid < nw ? warp_max[tid] : T(0);
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;  // valid in thread 0
+}
+
+template <typename T> struct Curl2DParams {
+    int ny, nx;
+    const T* psi;
+    T* u;
+    T prefactor;
+    ScalarSrc sc;
+    int add_free_stream;
+    T* umax;   // may be null
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) curl2d_kernel(Curl2DParams<T> p) {
+    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int ny = p.ny, nx = p.nx;
+    T m = T(0);
+    if (gx < nx && gy < ny) {
+        const int64_t g = (int64_t)gy * nx + gx;
+        T ux = T(0), uy = T(0);
+        if (gy >= 1 && gy <= ny - 2 && gx >= 1 && gx <= nx - 2) {
+            ux = (p.psi[g + nx] - p.psi[g - nx]) * p.prefactor;
+            uy = (p.psi[g - 1] - p.psi[g + 1]) * p.prefactor;
+        }
+        if (p.add_free_stream) {
+            ux = ux + (T)p.sc.free_stream(0);
+            uy = uy + (T)p.sc.free_stream(1);
+        }
+        p.u[g] = ux;
+        p.u[(int64_t)ny * nx + g] = uy;
+        m = fabs(ux) + fabs(uy);
+    }
+    if (p.umax) {
+        m = block_max(m);
+        if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(p.umax, m);
+    }
+}
+
+// ------------------------------------------------------------ 3D kernels
+// Direct-load stencils; neighbour reuse is served by L1/L2.
+struct Grid3 {
+    int nz, ny, nx;
+    __device__ __forceinline__ int64_t n() const { return (int64_t)nz * ny * nx; }
+    __device__ __forceinline__ bool interior(int z, int y, int x) const {
+        return z >= 1 && z <= nz - 2 && y >= 1 && y <= ny - 2 && x >= 1 && x <= nx - 2;
+    }
+};
+
+// out = w + pf * curl_h(v) on [1:-1]^3 (w elsewhere)  — per component as
+// update_vorticity_from_velocity_forcing_3d.py:29-94 writes it.
+template <typename T>
+__device__ __forceinline__ void curl3_at(const T* v, int64_t g, int64_t n, int64_t sy, int64_t sz, T out[3]) {
+    const T* vx = v;
+    const T* vy = v + n;
+    const T* vz = v + 2 * n;
+    out[0] = vz[g + sy] - vz[g - sy] - vy[g + sz] + vy[g - sz];
+    out[1] = vx[g + sz] - vx[g - sz] - vz[g + 1] + vz[g - 1];
+    out[2] = vy[g + 1] - vy[g - 1] - vx[g + sy] + vx[g - sy];
+}
+
+template <typename T> struct Stencil3DParams {
+    Grid3 grid;
+    const T* a;      // primary input (vector)
+    const T* b;      // secondary input (vector) or null
+    T* out;          // output (vector)
+    ScalarSrc sc;
+    T prefactor;
+    int mode;
+};
+
+// w1 = w + pf curl(f)  (mode 0; f may be null -> copy)
+template <typename T>
+__global__ void __launch_bounds__(256) forcing_curl3d_kernel(Stencil3DParams<T> p) {
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
+    T w0 = p.a[g], w1 = p.a[n + g], w2 = p.a[2 * n + g];
+    if (p.b && G.interior(z, y, x)) {
+        const T pf = p.mode == 0 ? (T)p.sc.forcing() : p.prefactor;
+        T c[3];
+        curl3_at(p.b, g, n, sy, sz, c);
+        w0 = w0 + pf * c[0];
+        w1 = w1 + pf * c[1];
+        w2 = w2 + pf * c[2];
+    }
+    p.out[g] = w0;
+    p.out[n + g] = w1;
+    p.out[2 * n + g] = w2;
+}
+
+// w2 = w1 + pc curl(u x w1) on [1:-1]^3 (a = w1, b = u)
+template <typename T>
+__device__ __forceinline__ void cross_at(const T* u, const T* w, int64_t g, int64_t n, T c[3]) {
+    const T ux = u[g], uy = u[n + g], uz = u[2 * n + g];
+    const T wx = w[g], wy = w[n + g], wz = w[2 * n + g];
+    // elementwise_ops_3d.py:406-448: r_i = a_j b_k - b_j a_k
+    c[0] = uy * wz - wy * uz;
+    c[1] = uz * wx - wz * ux;
+    c[2] = ux * wy - wx * uy;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) rotational_update3d_kernel(Stencil3DParams<T> p) {
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
+    T w0 = p.a[g], w1 = p.a[n + g], w2 = p.a[2 * n + g];
+    if (G.interior(z, y, x)) {
+        const T pc = (T)p.sc.advection();
+        T cyp[3], cym[3], czp[3], czm[3], cxp[3], cxm[3];
+        cross_at(p.b, p.a, g + sy, n, cyp);
+        cross_at(p.b, p.a, g - sy, n, cym);
+        cross_at(p.b, p.a, g + sz, n, czp);
+        cross_at(p.b, p.a, g - sz, n, czm);
+        cross_at(p.b, p.a, g + 1, n, cxp);
+        cross_at(p.b, p.a, g - 1, n, cxm);
+        w0 = w0 + pc * (cyp[2] - cym[2] - czp[1] + czm[1]);
+        w1 = w1 + pc * (czp[0] - czm[0] - cxp[2] + cxm[2]);
+        w2 = w2 + pc * (cxp[1] - cxm[1] - cyp[0] + cym[0]);
+    }
+    p.out[g] = w0;
+    p.out[n + g] = w1;
+    p.out[2 * n + g] = w2;
+}
+
+// w3 = w2 + k lap(w2) on [1:-1]^3 per component (diffusion_timestep_3d.py)
+template <typename T>
+__global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) {
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
+    const T k = p.mode == 0 ? (T)p.sc.diffusion() : p.prefactor;
+    const bool in = G.interior(z, y, x);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const T* f = p.a + c * n;
+        T v = f[g];
+        if (in) {
+            // diffusion_flux_3d.py:34-43 term order: z+1, z-1, y+1, y-1, x+1, x-1
+            const T lap = f[g + sz] + f[g - sz] + f[g + sy] + f[g - sy] + f[g + 1] + f[g - 1] - T(6) * f[g];
+            v = v + k * lap;
+        }
+        p.out[c * n + g] = v;
+    }
+}
+
+// One 1D Laplacian filter pass g = 0.25 (2 f - f[+s] - f[-s]) on [1:-1]^3,
+// zero ring (laplacian_filter_3d.py:55-73), scalar field.
+template <typename T>
+__global__ void __launch_bounds__(256) filter_pass3d_kernel(Grid3 G, const T* in, T* out, int axis) {
+    const int64_t n = G.n();
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    const int64_t s = axis == 0 ? 1 : (axis == 1 ? (int64_t)G.nx : (int64_t)G.nx * G.ny);
+    T v = T(0);
+    if (G.interior(z, y, x)) v = T(0.25) * (-in[g + s] - in[g - s] + T(2) * in[g]);
+    out[g] = v;
+}
+
+// f -= g (elementwise) over n cells
+template <typename T>
+__global__ void __launch_bounds__(256) subtract_kernel(int64_t n, T* f, const T* g) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) f[i] = f[i] - g[i];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) copy_kernel(int64_t n, T* dst, const T* src) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+// u = 0.5/dx curl(psi) on [1:-1]^3 (zero ring) + U_inf, with the max of
+// sum |u_d| (curl_3d.py:13-132, elementwise_ops_3d.py add_fixed_val)
+template <typename T> struct Curl3DParams {
+    Grid3 grid;
+    const T* psi;
+    T* u;
+    T prefactor;
+    ScalarSrc sc;
+    int add_free_stream;
+    T* umax;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) curl3d_kernel(Curl3DParams<T> p) {
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    T m = T(0);
+    if (g < n) {
+        const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+        T c[3] = {T(0), T(0), T(0)};
+        if (G.interior(z, y, x)) {
+            curl3_at(p.psi, g, n, (int64_t)G.nx, (int64_t)G.nx * G.ny, c);
+            c[0] = p.prefactor * c[0];
+            c[1] = p.prefactor * c[1];
+            c[2] = p.prefactor * c[2];
+        }
+        if (p.add_free_stream) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) c[d] = c[d] + (T)p.sc.free_stream(d);
+        }
+        p.u[g] = c[0];
+        p.u[n + g] = c[1];
+        p.u[2 * n + g] = c[2];
+        m = fabs(c[0]) + fabs(c[1]) + fabs(c[2]);
+    }
+    if (p.umax) {
+        m = block_max(m);
+        if (threadIdx.x == 0) atomic_max_nonneg(p.umax, m);
+    }
+}
+
+}  // namespace sg

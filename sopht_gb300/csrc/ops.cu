@@ -1,0 +1,265 @@
+// Single-operator entry points: the reference's individual stencil kernels,
+// exposed one by one for the lower-level kernel-factory API and for per-operator
+// parity tests.  The fused flow step does not go through these.
+#include "flow_kernels.cuh"
+
+namespace sg {
+
+template <typename T>
+int launch_sweep2d(const Sweep2DParams<T>& p, cudaStream_t stream);
+template <typename T>
+int launch_curl2d(const Curl2DParams<T>& p, cudaStream_t stream);
+template <typename T>
+int filter3d(Grid3 G, T* field, int filter_type, int order, T* a, T* b, cudaStream_t stream);
+
+template <typename T>
+__global__ void __launch_bounds__(256) penalise_kernel(int dim, int nz, int ny, int nx, int width, const T* in,
+                                                        T* out, const T* cx, const T* cy, const T* cz, int ncomp) {
+    const int64_t n = (int64_t)nz * ny * nx;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * ncomp) return;
+    const int64_t g = t % n;
+    const int c = (int)(t / n);
+    const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = (int)(g / ((int64_t)nx * ny));
+    const int sx = clamp_band(x, nx, width), sy = clamp_band(y, ny, width);
+    const int sz = dim == 3 ? clamp_band(z, nz, width) : 0;
+    T v = in[c * n + ((int64_t)sz * ny + sy) * nx + sx];
+    if (width > 0) {
+        v = v * cx[x];
+        v = v * cy[y];
+        if (dim == 3) v = v * cz[z];
+    }
+    out[c * n + g] = v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) cross3d_kernel(int64_t n, const T* a, const T* b, T* out) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    T c[3];
+    cross_at(a, b, g, n, c);
+    out[g] = c[0];
+    out[n + g] = c[1];
+    out[2 * n + g] = c[2];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) divergence3d_kernel(Grid3 G, const T* f, T* div, T inv_dx) {
+    const int64_t n = G.n();
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
+    T v = T(0);
+    if (G.interior(z, y, x)) {
+        // divergence_3d.py: (dfx/dx + dfy/dy + dfz/dz) * 0.5 * inv_dx
+        v = (f[g + 1] - f[g - 1] + f[n + g + sy] - f[n + g - sy] + f[2 * n + g + sz] - f[2 * n + g - sz]) *
+            T(0.5) * inv_dx;
+    }
+    div[g] = v;
+}
+
+template <typename T>
+static int sweep_op(int ny, int nx, const void* in, void* out, const void* u, const void* f, double pf, double adv,
+                    double diff, int flags, cudaStream_t stream) {
+    Sweep2DParams<T> s{};
+    s.ny = ny;
+    s.nx = nx;
+    s.w = (const T*)in;
+    s.u = (const T*)u;
+    s.f = (const T*)f;
+    s.out = (T*)out;
+    s.sc.host.forcing_prefac = pf;
+    s.sc.host.advection_prefac = adv;
+    s.sc.host.diffusion_prefac = diff;
+    s.flags = flags;
+    return launch_sweep2d<T>(s, stream);
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+#define SG_DTYPE_DISPATCH(dtype, CALL_F, CALL_D)                                     \
+    do {                                                                              \
+        if ((dtype) == SG_F32) return CALL_F;                                         \
+        SG_REQUIRE((dtype) == SG_F64, SG_ERR_INVALID_ARG, "bad dtype %d", (int)(dtype)); \
+        return CALL_D;                                                                \
+    } while (0)
+
+static int check2d(int ny, int nx, const void* a, const void* b) {
+    SG_REQUIRE(a && b, SG_ERR_INVALID_ARG, "null field pointer");
+    SG_REQUIRE(ny >= 1 && nx >= 1, SG_ERR_SHAPE, "bad 2D extent (%d, %d)", ny, nx);
+    SG_REQUIRE(a != b, SG_ERR_INVALID_ARG, "input and output must not alias (stencil halo)");
+    return SG_OK;
+}
+
+extern "C" int sg_advection_eno3_step_2d(int dtype, int ny, int nx, const void* in, void* out, const void* velocity,
+                                         double dt_by_dx, void* stream) {
+    SG_TRY(check2d(ny, nx, in, out));
+    SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, sweep_op<float>(ny, nx, in, out, velocity, nullptr, 0, dt_by_dx, 0, SWEEP_ADVECT, s),
+                      sweep_op<double>(ny, nx, in, out, velocity, nullptr, 0, dt_by_dx, 0, SWEEP_ADVECT, s));
+}
+
+extern "C" int sg_diffusion_step_2d(int dtype, int ny, int nx, const void* in, void* out, double k, void* stream) {
+    SG_TRY(check2d(ny, nx, in, out));
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, sweep_op<float>(ny, nx, in, out, nullptr, nullptr, 0, 0, k, SWEEP_DIFFUSE, s),
+                      sweep_op<double>(ny, nx, in, out, nullptr, nullptr, 0, 0, k, SWEEP_DIFFUSE, s));
+}
+
+extern "C" int sg_forcing_curl_update_2d(int dtype, int ny, int nx, const void* in, void* out, const void* forcing,
+                                         double prefactor, void* stream) {
+    SG_TRY(check2d(ny, nx, in, out));
+    SG_REQUIRE(forcing, SG_ERR_INVALID_ARG, "null forcing");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, sweep_op<float>(ny, nx, in, out, nullptr, forcing, prefactor, 0, 0, 0, s),
+                      sweep_op<double>(ny, nx, in, out, nullptr, forcing, prefactor, 0, 0, 0, s));
+}
+
+template <typename T>
+static int curl2d_op(int ny, int nx, const void* psi, void* curl, double pref, cudaStream_t s) {
+    Curl2DParams<T> c{};
+    c.ny = ny;
+    c.nx = nx;
+    c.psi = (const T*)psi;
+    c.u = (T*)curl;
+    c.prefactor = (T)pref;
+    c.add_free_stream = 0;
+    c.umax = nullptr;
+    return launch_curl2d<T>(c, s);
+}
+
+extern "C" int sg_outplane_curl_2d(int dtype, int ny, int nx, const void* psi, void* curl, double prefactor,
+                                   void* stream) {
+    SG_TRY(check2d(ny, nx, psi, curl));
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, curl2d_op<float>(ny, nx, psi, curl, prefactor, s),
+                      curl2d_op<double>(ny, nx, psi, curl, prefactor, s));
+}
+
+template <typename T>
+static int penalise_op(int dim, int nz, int ny, int nx, const void* in, void* out, int width, const void* cx,
+                       const void* cy, const void* cz, int ncomp, cudaStream_t s) {
+    const int64_t n = (int64_t)nz * ny * nx * ncomp;
+    penalise_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(dim, nz, ny, nx, width, (const T*)in, (T*)out,
+                                                        (const T*)cx, (const T*)cy, (const T*)cz, ncomp);
+    return launch_status("penalise");
+}
+
+extern "C" int sg_penalise_2d(int dtype, int ny, int nx, const void* in, void* out, int width, const void* cx,
+                              const void* cy, void* stream) {
+    SG_TRY(check2d(ny, nx, in, out));
+    SG_REQUIRE(width >= 0 && 2 * width <= nx && 2 * width <= ny, SG_ERR_SHAPE, "penalty width does not fit");
+    SG_REQUIRE(width == 0 || (cx && cy), SG_ERR_INVALID_ARG, "null penalisation table");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, penalise_op<float>(2, 1, ny, nx, in, out, width, cx, cy, nullptr, 1, s),
+                      penalise_op<double>(2, 1, ny, nx, in, out, width, cx, cy, nullptr, 1, s));
+}
+
+static int check3d(int nz, int ny, int nx, const void* a, const void* b) {
+    SG_REQUIRE(a && b, SG_ERR_INVALID_ARG, "null field pointer");
+    SG_REQUIRE(nz >= 1 && ny >= 1 && nx >= 1, SG_ERR_SHAPE, "bad 3D extent");
+    SG_REQUIRE(a != b, SG_ERR_INVALID_ARG, "input and output must not alias (stencil halo)");
+    return SG_OK;
+}
+
+template <typename T>
+static int stencil3d_op(int which, int nz, int ny, int nx, const void* a, const void* b, void* out, double pref,
+                        cudaStream_t s) {
+    Stencil3DParams<T> p{};
+    p.grid = Grid3{nz, ny, nx};
+    p.a = (const T*)a;
+    p.b = (const T*)b;
+    p.out = (T*)out;
+    p.prefactor = (T)pref;
+    p.mode = 1;
+    const int64_t n = (int64_t)nz * ny * nx;
+    const unsigned blocks = ceil_div(n, 256);
+    if (which == 0) forcing_curl3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+    else if (which == 1) diffusion3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+    else {
+        Curl3DParams<T> c{};
+        c.grid = p.grid;
+        c.psi = (const T*)a;
+        c.u = (T*)out;
+        c.prefactor = (T)pref;
+        curl3d_kernel<T><<<blocks, 256, 0, s>>>(c);
+    }
+    return launch_status("stencil3d op");
+}
+
+extern "C" int sg_curl_3d(int dtype, int nz, int ny, int nx, const void* field, void* curl, double prefactor,
+                          void* stream) {
+    SG_TRY(check3d(nz, ny, nx, field, curl));
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, stencil3d_op<float>(2, nz, ny, nx, field, nullptr, curl, prefactor, s),
+                      stencil3d_op<double>(2, nz, ny, nx, field, nullptr, curl, prefactor, s));
+}
+
+extern "C" int sg_forcing_curl_update_3d(int dtype, int nz, int ny, int nx, const void* in, void* out,
+                                         const void* forcing, double prefactor, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, in, out));
+    SG_REQUIRE(forcing, SG_ERR_INVALID_ARG, "null forcing");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, stencil3d_op<float>(0, nz, ny, nx, in, forcing, out, prefactor, s),
+                      stencil3d_op<double>(0, nz, ny, nx, in, forcing, out, prefactor, s));
+}
+
+extern "C" int sg_diffusion_step_3d(int dtype, int nz, int ny, int nx, const void* in, void* out, double k,
+                                    void* stream) {
+    SG_TRY(check3d(nz, ny, nx, in, out));
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, stencil3d_op<float>(1, nz, ny, nx, in, nullptr, out, k, s),
+                      stencil3d_op<double>(1, nz, ny, nx, in, nullptr, out, k, s));
+}
+
+template <typename T>
+static int cross_op(int64_t n, const void* a, const void* b, void* out, cudaStream_t s) {
+    cross3d_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(n, (const T*)a, (const T*)b, (T*)out);
+    return launch_status("cross3d");
+}
+
+extern "C" int sg_cross_3d(int dtype, int64_t n, const void* a, const void* b, void* out, void* stream) {
+    SG_REQUIRE(a && b && out && n >= 1, SG_ERR_INVALID_ARG, "cross: bad argument");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, cross_op<float>(n, a, b, out, s), cross_op<double>(n, a, b, out, s));
+}
+
+template <typename T>
+static int div_op(int nz, int ny, int nx, const void* f, void* div, double inv_dx, cudaStream_t s) {
+    Grid3 G{nz, ny, nx};
+    divergence3d_kernel<T><<<ceil_div((int64_t)nz * ny * nx, 256), 256, 0, s>>>(G, (const T*)f, (T*)div, (T)inv_dx);
+    return launch_status("divergence3d");
+}
+
+extern "C" int sg_divergence_3d(int dtype, int nz, int ny, int nx, const void* field, void* div, double inv_dx,
+                                void* stream) {
+    SG_TRY(check3d(nz, ny, nx, field, div));
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, div_op<float>(nz, ny, nx, field, div, inv_dx, s),
+                      div_op<double>(nz, ny, nx, field, div, inv_dx, s));
+}
+
+extern "C" int sg_penalise_3d(int dtype, int nz, int ny, int nx, const void* in, void* out, int width,
+                              const void* cx, const void* cy, const void* cz, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, in, out));
+    SG_REQUIRE(width >= 0 && 2 * width <= nx && 2 * width <= ny && 2 * width <= nz, SG_ERR_SHAPE,
+               "penalty width does not fit");
+    SG_REQUIRE(width == 0 || (cx && cy && cz), SG_ERR_INVALID_ARG, "null penalisation table");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, penalise_op<float>(3, nz, ny, nx, in, out, width, cx, cy, cz, 3, s),
+                      penalise_op<double>(3, nz, ny, nx, in, out, width, cx, cy, cz, 3, s));
+}
+
+extern "C" int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* field, int filter_type,
+                                      int filter_order, void* a, void* b, void* stream) {
+    SG_REQUIRE(field && a && b, SG_ERR_INVALID_ARG, "filter: null pointer");
+    SG_REQUIRE(filter_type >= 0 && filter_type <= 2 && filter_order >= 0, SG_ERR_INVALID_ARG, "filter: bad setting");
+    auto s = (cudaStream_t)stream;
+    Grid3 G{nz, ny, nx};
+    SG_DTYPE_DISPATCH(dtype, filter3d<float>(G, (float*)field, filter_type, filter_order, (float*)a, (float*)b, s),
+                      filter3d<double>(G, (double*)field, filter_type, filter_order, (double*)a, (double*)b, s));
+}

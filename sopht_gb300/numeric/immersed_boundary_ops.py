@@ -1,0 +1,153 @@
+"""Virtual-boundary forcing on CUDA tensors (mirrors sopht/numeric/immersed_boundary_ops).
+
+``VirtualBoundaryForcing`` keeps the reference's constructor, buffers and
+methods (immersed_boundary_ops/VirtualBoundaryForcing.py:20-283).  The
+Lagrangian buffers live on the GPU in ``real_t``; marker positions and body
+velocities are float64 (host numpy arrays are staged through pinned memory).
+Support, weights, interpolation, mismatch and force are one warp-per-marker
+kernel; spreading is a deterministic owner-ordered kernel without atomics.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..utils import default_device, normalize_real_t, ptr, sg_dtype, stream_ptr, torch_dtype
+
+KERNEL_TYPES = {"cosine": 0, "peskin": 1}
+
+
+class _PinnedStage:
+    """Pinned host staging of a float64 (dim, n) array, reused across calls.
+
+    Before the buffer is overwritten, the event recorded after the previous
+    copy is waited on, so an in-flight upload never sees new data."""
+
+    def __init__(self, shape, device):
+        self.host = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+        self.dev = torch.empty(shape, dtype=torch.float64, device=device)
+        self.event = torch.cuda.Event()
+        self.pending = False
+
+    def upload(self, arr) -> torch.Tensor:
+        if isinstance(arr, torch.Tensor) and arr.is_cuda:
+            if arr.dtype == torch.float64 and arr.is_contiguous():
+                return arr
+            self.dev.copy_(arr)
+            return self.dev
+        if self.pending:
+            self.event.synchronize()
+        self.host.numpy()[...] = np.asarray(arr if not isinstance(arr, torch.Tensor) else arr.numpy())
+        self.dev.copy_(self.host, non_blocking=True)
+        self.event.record()
+        self.pending = True
+        return self.dev
+
+
+class VirtualBoundaryForcing:
+    """Feedback F = K xi + C dU between a Lagrangian body and the Eulerian flow."""
+
+    def __init__(self, virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, grid_dim, dx,
+                 num_lag_nodes, real_t, eul_grid_coord_shift=None, interp_kernel_width=None,
+                 enable_eul_grid_forcing_reset=True, num_threads=False, start_time=0.0,
+                 interp_kernel_type="cosine", device=None):
+        if grid_dim not in (2, 3):
+            raise ValueError("Invalid grid dimensions, must be either 2 or 3")
+        real_t = normalize_real_t(real_t)
+        if interp_kernel_width is None:
+            interp_kernel_width = 2
+        if interp_kernel_width != 2:
+            raise ValueError("Interpolation kernel inconsistent with interpolation kernel width!")
+        if interp_kernel_type not in KERNEL_TYPES:
+            raise ValueError("Invalid interpolation kernel type. Current supported types are'cosine' and 'peskin'.")
+        self.grid_dim = grid_dim
+        self.virtual_boundary_stiffness_coeff = virtual_boundary_stiffness_coeff
+        self.virtual_boundary_damping_coeff = virtual_boundary_damping_coeff
+        self.time = start_time
+        self.real_t = real_t
+        self.dx = dx
+        self.eul_grid_coord_shift = real_t(dx / 2) if eul_grid_coord_shift is None else eul_grid_coord_shift
+        self.interp_kernel_width = interp_kernel_width
+        self.interp_kernel_type = interp_kernel_type
+        self.num_lag_nodes = num_lag_nodes
+        self.device = default_device(device)
+        dev, tdt = self.device, torch_dtype(real_t)
+        n = num_lag_nodes
+        self.nearest_eul_grid_index_to_lag_grid = torch.zeros((grid_dim, n), dtype=torch.int32, device=dev)
+        self.interp_weights = torch.zeros(((2 * interp_kernel_width) ** grid_dim, n), dtype=tdt, device=dev)
+        self.lag_grid_flow_velocity_field = torch.zeros((grid_dim, n), dtype=tdt, device=dev)
+        self.lag_grid_position_mismatch_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
+        self.lag_grid_velocity_mismatch_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
+        self.lag_grid_forcing_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._pos_stage = _PinnedStage((grid_dim, n), dev)
+        self._vel_stage = _PinnedStage((grid_dim, n), dev)
+        self.enable_eul_grid_forcing_reset = enable_eul_grid_forcing_reset
+        if enable_eul_grid_forcing_reset:
+            self.compute_interaction_forcing = (
+                self.compute_interaction_force_on_eul_and_lag_grid_with_eul_grid_forcing_reset)
+        else:
+            self.compute_interaction_forcing = self.compute_interaction_force_on_eul_and_lag_grid
+
+    # -- grid extent of a field (component first)
+    def _extent(self, field):
+        if self.grid_dim == 2:
+            _, ny, nx = field.shape
+            return 1, ny, nx
+        _, nz, ny, nx = field.shape
+        return nz, ny, nx
+
+    def _interaction(self, eul_velocity, position, body_velocity, xi_step=False, xi_dt=0.0, dev_scalars=None):
+        if eul_velocity.dtype != torch_dtype(self.real_t):
+            raise ValueError("Eulerian velocity dtype does not match real_t")
+        pos = self._pos_stage.upload(position)
+        vel = self._vel_stage.upload(body_velocity)
+        nz, ny, nx = self._extent(eul_velocity)
+        _lib.call("sg_ib_interaction", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, float(self.dx),
+                  float(self.eul_grid_coord_shift), self.num_lag_nodes, KERNEL_TYPES[self.interp_kernel_type],
+                  ptr(pos), ptr(vel), ptr(eul_velocity), ptr(self.nearest_eul_grid_index_to_lag_grid),
+                  ptr(self.interp_weights), ptr(self.lag_grid_flow_velocity_field),
+                  ptr(self.lag_grid_velocity_mismatch_field), ptr(self.lag_grid_position_mismatch_field),
+                  ptr(self.lag_grid_forcing_field), float(self.virtual_boundary_stiffness_coeff),
+                  float(self.virtual_boundary_damping_coeff), int(xi_step), float(xi_dt), dev_scalars,
+                  ptr(self._status), stream_ptr(self.device))
+
+    def _spread(self, eul_forcing, reset: bool):
+        nz, ny, nx = self._extent(eul_forcing)
+        _lib.call("sg_ib_spread", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, self.num_lag_nodes,
+                  ptr(self.nearest_eul_grid_index_to_lag_grid), ptr(self.interp_weights),
+                  ptr(self.lag_grid_forcing_field), ptr(eul_forcing), int(reset), stream_ptr(self.device))
+
+    def check_markers_in_domain(self) -> None:
+        """Raise if any marker's interpolation support left the grid (synchronises)."""
+        status = int(self._status.item())
+        if status != 0:
+            self._status.zero_()
+            raise ValueError("an immersed-boundary marker's support lies outside the Eulerian grid")
+
+    def compute_interaction_force_on_lag_grid(self, eul_grid_velocity_field, lag_grid_position_field,
+                                              lag_grid_velocity_field):
+        """VirtualBoundaryForcing.py:187-230."""
+        self._interaction(eul_grid_velocity_field, lag_grid_position_field, lag_grid_velocity_field)
+
+    def compute_interaction_force_on_eul_and_lag_grid(self, eul_grid_forcing_field, eul_grid_velocity_field,
+                                                      lag_grid_position_field, lag_grid_velocity_field):
+        """VirtualBoundaryForcing.py:232-253."""
+        self._interaction(eul_grid_velocity_field, lag_grid_position_field, lag_grid_velocity_field)
+        self._spread(eul_grid_forcing_field, reset=False)
+
+    def compute_interaction_force_on_eul_and_lag_grid_with_eul_grid_forcing_reset(
+            self, eul_grid_forcing_field, eul_grid_velocity_field, lag_grid_position_field,
+            lag_grid_velocity_field):
+        """VirtualBoundaryForcing.py:255-274."""
+        self._interaction(eul_grid_velocity_field, lag_grid_position_field, lag_grid_velocity_field)
+        self._spread(eul_grid_forcing_field, reset=True)
+
+    def time_step(self, dt):
+        """VirtualBoundaryForcing.py:276-283: xi += dt * dU."""
+        _lib.call("sg_ib_mismatch_step", sg_dtype(self.real_t), self.grid_dim * self.num_lag_nodes,
+                  ptr(self.lag_grid_position_mismatch_field), ptr(self.lag_grid_velocity_mismatch_field),
+                  float(self.real_t(dt)), stream_ptr(self.device))
+        self.time += dt

@@ -1,0 +1,39 @@
+"""Flow simulators and immersed-body coupling (sopht.simulator counterparts)."""
+
+from .flow import (
+    FlowSimulator,
+    UnboundedNavierStokesFlowSimulator2D,
+    UnboundedNavierStokesFlowSimulator3D,
+    create_unbounded_flow_simulator_2d,
+    create_unbounded_flow_simulator_3d,
+)
+from .immersed_body import (
+    CircularCylinderForcingGrid,
+    CosseratRodElementCentricForcingGrid,
+    CosseratRodFlowInteraction,
+    CosseratRodNodalForcingGrid,
+    Cylinder,
+    FlowForces,
+    ImmersedBodyFlowInteraction,
+    ImmersedBodyForcingGrid,
+    RigidBodyFlowInteraction,
+    TwoDimensionalCylinderForcingGrid,
+)
+
+__all__ = [
+    "CircularCylinderForcingGrid",
+    "CosseratRodElementCentricForcingGrid",
+    "CosseratRodFlowInteraction",
+    "CosseratRodNodalForcingGrid",
+    "Cylinder",
+    "FlowForces",
+    "FlowSimulator",
+    "ImmersedBodyFlowInteraction",
+    "ImmersedBodyForcingGrid",
+    "RigidBodyFlowInteraction",
+    "TwoDimensionalCylinderForcingGrid",
+    "UnboundedNavierStokesFlowSimulator2D",
+    "UnboundedNavierStokesFlowSimulator3D",
+    "create_unbounded_flow_simulator_2d",
+    "create_unbounded_flow_simulator_3d",
+]

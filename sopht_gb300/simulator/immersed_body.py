@@ -1,0 +1,326 @@
+"""Immersed body - flow interaction (mirrors sopht/simulator/immersed_body).
+
+The forcing grids stay on the host in float64 numpy, exactly as the reference
+keeps them (they are pyelastica geometry); every interaction call uploads the
+marker positions and velocities through pinned memory and runs the
+GPU virtual-boundary forcing.  Body forces and torques come back to the host
+for pyelastica (``compute_flow_forces_and_torques``).
+
+``Cylinder`` and ``CosseratRodState`` are small stand-ins carrying the
+attributes the forcing grids read, for users without pyelastica; a real
+``elastica.Cylinder`` / ``elastica.CosseratRod`` works unchanged.
+"""
+
+from __future__ import annotations
+
+import logging
+from abc import abstractmethod
+
+import numpy as np
+import torch
+
+from ..numeric.immersed_boundary_ops import VirtualBoundaryForcing
+
+logger = logging.getLogger(__name__)
+
+
+# ------------------------------------------------------------ forcing grids
+
+
+class ImmersedBodyForcingGrid:
+    """immersed_body_forcing_grid.py:9-54."""
+
+    def __init__(self, grid_dim: int, num_lag_nodes: int) -> None:
+        self.grid_dim = grid_dim
+        self.num_lag_nodes = num_lag_nodes
+        self.position_field = np.zeros((self.grid_dim, self.num_lag_nodes))
+        self.velocity_field = np.zeros_like(self.position_field)
+        if grid_dim == 2:
+            logger.warning("2D body forcing grid generated, this assumes the body moves in XY plane!")
+
+    @abstractmethod
+    def compute_lag_grid_position_field(self) -> None: ...
+
+    @abstractmethod
+    def compute_lag_grid_velocity_field(self) -> None: ...
+
+    @abstractmethod
+    def transfer_forcing_from_grid_to_body(self, body_flow_forces, body_flow_torques, lag_grid_forcing_field): ...
+
+    @abstractmethod
+    def get_maximum_lagrangian_grid_spacing(self) -> float: ...
+
+
+class Cylinder:
+    """Rigid cylinder with the attributes the forcing grids read (pyelastica layout).
+
+    Stand-in for ``elastica.Cylinder`` when pyelastica is absent: position
+    (3, 1), directors (3, 3, 1) with rows d1, d2, d3, velocity (3, 1), angular
+    velocity in the local frame (3, 1) and radius.  ``direction`` is d3 and
+    ``normal`` is d1, as pyelastica defines them.
+    """
+
+    def __init__(self, start, direction=(0.0, 0.0, 1.0), normal=(1.0, 0.0, 0.0), base_length=1.0,
+                 base_radius=0.1, density=1.0):
+        d3 = np.asarray(direction, dtype=np.float64)
+        d1 = np.asarray(normal, dtype=np.float64)
+        d2 = np.cross(d3, d1)
+        self.position_collection = np.asarray(start, dtype=np.float64).reshape(3, 1).copy()
+        self.director_collection = np.stack([d1, d2, d3]).reshape(3, 3, 1)
+        self.velocity_collection = np.zeros((3, 1))
+        self.omega_collection = np.zeros((3, 1))
+        self.radius = base_radius
+        self.length = base_length
+        self.density = density
+
+
+class TwoDimensionalCylinderForcingGrid(ImmersedBodyForcingGrid):
+    """rigid_body_forcing_grids.py:11-79: markers on a cylinder in the XY plane."""
+
+    def __init__(self, grid_dim: int, num_lag_nodes: int, rigid_body) -> None:
+        if grid_dim != 2:
+            raise ValueError("Invalid grid dimensions. 2D cylinder forcing grid is only defined for grid_dim=2")
+        self.cylinder = rigid_body
+        super().__init__(grid_dim, num_lag_nodes)
+        self.local_frame_relative_position_field = np.zeros_like(self.position_field)
+        self.global_frame_relative_position_field = np.zeros_like(self.position_field)
+
+    def compute_lag_grid_position_field(self) -> None:
+        q = self.cylinder.director_collection[: self.grid_dim, : self.grid_dim, 0]
+        self.global_frame_relative_position_field[...] = q.T @ self.local_frame_relative_position_field
+        self.position_field[...] = (self.cylinder.position_collection[: self.grid_dim]
+                                    + self.global_frame_relative_position_field)
+
+    def compute_lag_grid_velocity_field(self) -> None:
+        # the angular velocity lies along d3 (global Z): v = V + omega_z e_z x r
+        omega_z = (self.cylinder.director_collection[self.grid_dim, self.grid_dim, 0]
+                   * self.cylinder.omega_collection[self.grid_dim, 0])
+        rel = self.global_frame_relative_position_field
+        self.velocity_field[0] = self.cylinder.velocity_collection[0] - omega_z * rel[1]
+        self.velocity_field[1] = self.cylinder.velocity_collection[1] + omega_z * rel[0]
+
+    def transfer_forcing_from_grid_to_body(self, body_flow_forces, body_flow_torques, lag_grid_forcing_field):
+        f = np.asarray(lag_grid_forcing_field, dtype=np.float64)
+        body_flow_forces[: self.grid_dim] = -np.sum(f, axis=1).reshape(-1, 1)
+        rel = self.global_frame_relative_position_field
+        body_flow_torques[self.grid_dim] = self.cylinder.director_collection[self.grid_dim, self.grid_dim, 0] * np.sum(
+            -rel[0] * f[1] + rel[1] * f[0])
+
+    def get_maximum_lagrangian_grid_spacing(self) -> float:
+        raise NotImplementedError
+
+
+class CircularCylinderForcingGrid(TwoDimensionalCylinderForcingGrid):
+    """rigid_body_forcing_grids.py:82-105: markers at theta_k = (k + 1/2) 2 pi / N."""
+
+    def __init__(self, grid_dim: int, rigid_body, num_forcing_points: int) -> None:
+        super().__init__(grid_dim=grid_dim, num_lag_nodes=num_forcing_points, rigid_body=rigid_body)
+        dtheta = 2.0 * np.pi / self.num_lag_nodes
+        theta = np.linspace(dtheta / 2.0, 2.0 * np.pi - dtheta / 2.0, self.num_lag_nodes)
+        self.local_frame_relative_position_field[0, :] = self.cylinder.radius * np.cos(theta)
+        self.local_frame_relative_position_field[1, :] = self.cylinder.radius * np.sin(theta)
+        self.compute_lag_grid_position_field()
+        self.compute_lag_grid_velocity_field()
+
+    def get_maximum_lagrangian_grid_spacing(self) -> float:
+        return self.cylinder.radius * (2.0 * np.pi / self.num_lag_nodes)
+
+
+def _node_to_element_velocity(mass, node_velocity):
+    """Element velocity as the mass-weighted mean of its two nodes (pyelastica)."""
+    return (mass[1:] * node_velocity[:, 1:] + mass[:-1] * node_velocity[:, :-1]) / (mass[1:] + mass[:-1])
+
+
+class CosseratRodNodalForcingGrid(ImmersedBodyForcingGrid):
+    """cosserat_rod_forcing_grids.py:10-79: markers at the rod nodes."""
+
+    def __init__(self, grid_dim: int, cosserat_rod) -> None:
+        super().__init__(grid_dim, cosserat_rod.n_elems + 1)
+        self.cosserat_rod = cosserat_rod
+        self.moment_arm = np.zeros((3, cosserat_rod.n_elems))
+        self.compute_lag_grid_position_field()
+        self.compute_lag_grid_velocity_field()
+
+    def compute_lag_grid_position_field(self) -> None:
+        self.position_field[...] = self.cosserat_rod.position_collection[: self.grid_dim]
+
+    def compute_lag_grid_velocity_field(self) -> None:
+        self.velocity_field[...] = self.cosserat_rod.velocity_collection[: self.grid_dim]
+
+    def transfer_forcing_from_grid_to_body(self, body_flow_forces, body_flow_torques, lag_grid_forcing_field):
+        body_flow_forces[: self.grid_dim] = -np.asarray(lag_grid_forcing_field, dtype=np.float64)
+        pos = self.cosserat_rod.position_collection
+        self.moment_arm[...] = (pos[..., 1:] - pos[..., :-1]) / 2.0
+        body_flow_torques[...] = np.cross(self.moment_arm, (body_flow_forces[..., 1:] - body_flow_forces[..., :-1])
+                                          / 2.0, axis=0)
+        body_flow_torques[..., -1] += np.cross(self.moment_arm[..., -1], body_flow_forces[..., -1]) / 2.0
+        body_flow_torques[..., 0] -= np.cross(self.moment_arm[..., 0], body_flow_forces[..., 0]) / 2.0
+        body_flow_torques[...] = np.einsum("ijk,jk->ik", self.cosserat_rod.director_collection, body_flow_torques)
+
+    def get_maximum_lagrangian_grid_spacing(self) -> float:
+        return np.amax(self.cosserat_rod.lengths)
+
+
+class CosseratRodElementCentricForcingGrid(ImmersedBodyForcingGrid):
+    """cosserat_rod_forcing_grids.py:82-130: markers at element centres."""
+
+    def __init__(self, grid_dim: int, cosserat_rod) -> None:
+        super().__init__(grid_dim, cosserat_rod.n_elems)
+        self.cosserat_rod = cosserat_rod
+        self.compute_lag_grid_position_field()
+        self.compute_lag_grid_velocity_field()
+
+    def compute_lag_grid_position_field(self) -> None:
+        p = self.cosserat_rod.position_collection
+        self.position_field[...] = (p[: self.grid_dim, 1:] + p[: self.grid_dim, :-1]) / 2.0
+
+    def compute_lag_grid_velocity_field(self) -> None:
+        self.velocity_field[...] = _node_to_element_velocity(self.cosserat_rod.mass,
+                                                             self.cosserat_rod.velocity_collection)[: self.grid_dim]
+
+    def transfer_forcing_from_grid_to_body(self, body_flow_forces, body_flow_torques, lag_grid_forcing_field):
+        f = np.asarray(lag_grid_forcing_field, dtype=np.float64)
+        body_flow_forces[...] = 0.0
+        body_flow_forces[: self.grid_dim, 1:] -= 0.5 * f
+        body_flow_forces[: self.grid_dim, :-1] -= 0.5 * f
+
+    def get_maximum_lagrangian_grid_spacing(self) -> float:
+        return np.amax(self.cosserat_rod.lengths)
+
+
+# ----------------------------------------------------------------- interaction
+
+
+class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
+    """immersed_body_flow_interaction.py:15-141."""
+
+    def __init__(self, eul_grid_forcing_field, eul_grid_velocity_field, body_flow_forces, body_flow_torques,
+                 forcing_grid_cls, virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, dx, grid_dim,
+                 real_t=np.float64, eul_grid_coord_shift=None, interp_kernel_width=None,
+                 enable_eul_grid_forcing_reset=False, num_threads=False, start_time=0.0, **forcing_grid_kwargs):
+        self.body_flow_forces = body_flow_forces
+        self.body_flow_torques = body_flow_torques
+        interp_kernel_type = forcing_grid_kwargs.pop("interp_kernel_type", "cosine")
+        self.forcing_grid = forcing_grid_cls(grid_dim=grid_dim, **forcing_grid_kwargs)
+        if not isinstance(eul_grid_forcing_field, torch.Tensor) or not eul_grid_forcing_field.is_cuda:
+            raise ValueError("eul_grid_forcing_field must be the simulator's CUDA tensor")
+        self.eul_grid_forcing_field = eul_grid_forcing_field
+        self.eul_grid_velocity_field = eul_grid_velocity_field
+        max_lag_grid_dx = self.forcing_grid.get_maximum_lagrangian_grid_spacing()
+        grid_type = type(self.forcing_grid).__name__
+        if max_lag_grid_dx > 2 * dx:
+            logger.warning("For %s: max Lagrangian grid spacing %s > 2 * dx (%s); the Lagrangian grid is too "
+                           "coarse relative to the Eulerian grid.", grid_type, max_lag_grid_dx, dx)
+        elif max_lag_grid_dx < 0.5 * dx:
+            logger.warning("For %s: max Lagrangian grid spacing %s < 0.5 * dx (%s); redundant forcing points.",
+                           grid_type, max_lag_grid_dx, dx)
+        else:
+            logger.info("For %s: Lagrangian grid is resolved almost the same as the Eulerian grid (dx = %s).",
+                        grid_type, dx)
+        # immersed_body_flow_interaction.py:83-86
+        virtual_boundary_stiffness_coeff *= max_lag_grid_dx ** (grid_dim - 1)
+        virtual_boundary_damping_coeff *= max_lag_grid_dx ** (grid_dim - 1)
+        super().__init__(virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, grid_dim, dx,
+                         self.forcing_grid.num_lag_nodes, real_t, eul_grid_coord_shift, interp_kernel_width,
+                         enable_eul_grid_forcing_reset, num_threads, start_time,
+                         interp_kernel_type=interp_kernel_type, device=eul_grid_forcing_field.device)
+        self._host_forcing = torch.empty(self.lag_grid_forcing_field.shape, dtype=self.lag_grid_forcing_field.dtype,
+                                         pin_memory=True)
+
+    def compute_interaction_on_lag_grid(self) -> None:
+        self.forcing_grid.compute_lag_grid_position_field()
+        self.forcing_grid.compute_lag_grid_velocity_field()
+        self.compute_interaction_force_on_lag_grid(self.eul_grid_velocity_field, self.forcing_grid.position_field,
+                                                   self.forcing_grid.velocity_field)
+
+    def __call__(self) -> None:
+        self.forcing_grid.compute_lag_grid_position_field()
+        self.forcing_grid.compute_lag_grid_velocity_field()
+        self.compute_interaction_forcing(eul_grid_forcing_field=self.eul_grid_forcing_field,
+                                         eul_grid_velocity_field=self.eul_grid_velocity_field,
+                                         lag_grid_position_field=self.forcing_grid.position_field,
+                                         lag_grid_velocity_field=self.forcing_grid.velocity_field)
+
+    def device_call(self, dev_scalars: int) -> None:
+        """``time_step(dt)`` then ``__call__()`` with dt read on the GPU (one kernel pair).
+
+        For captured time loops: the marker kinematics are taken from the
+        device copies already uploaded (static bodies or bodies whose
+        kinematics the caller refreshes with ``upload_kinematics``)."""
+        self._interaction(self.eul_grid_velocity_field, self._pos_stage.dev, self._vel_stage.dev, xi_step=True,
+                          dev_scalars=dev_scalars)
+        self._spread(self.eul_grid_forcing_field, reset=self.enable_eul_grid_forcing_reset)
+
+    def upload_kinematics(self) -> None:
+        """Refresh the device copies of the marker positions and velocities."""
+        self.forcing_grid.compute_lag_grid_position_field()
+        self.forcing_grid.compute_lag_grid_velocity_field()
+        self._pos_stage.upload(self.forcing_grid.position_field)
+        self._vel_stage.upload(self.forcing_grid.velocity_field)
+
+    def lag_grid_forcing_host(self) -> np.ndarray:
+        """The Lagrangian forcing on the host (synchronises)."""
+        self._host_forcing.copy_(self.lag_grid_forcing_field)
+        return self._host_forcing.numpy()
+
+    def compute_flow_forces_and_torques(self) -> None:
+        """immersed_body_flow_interaction.py:124-131 (one device->host read)."""
+        self.compute_interaction_on_lag_grid()
+        self.forcing_grid.transfer_forcing_from_grid_to_body(
+            body_flow_forces=self.body_flow_forces, body_flow_torques=self.body_flow_torques,
+            lag_grid_forcing_field=self.lag_grid_forcing_host())
+
+    def get_grid_deviation_error_l2_norm(self) -> float:
+        """immersed_body_flow_interaction.py:133-141."""
+        xi = self.lag_grid_position_mismatch_field.double()
+        return float(torch.linalg.vector_norm(xi).item()) / np.sqrt(self.forcing_grid.num_lag_nodes)
+
+
+class RigidBodyFlowInteraction(ImmersedBodyFlowInteraction):
+    """rigid_body/rigid_body_flow_interaction.py:9-54."""
+
+    def __init__(self, rigid_body, eul_grid_forcing_field, eul_grid_velocity_field,
+                 virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, dx, grid_dim, forcing_grid_cls,
+                 real_t=np.float64, eul_grid_coord_shift=None, interp_kernel_width=None,
+                 enable_eul_grid_forcing_reset=False, num_threads=False, start_time=0.0, **forcing_grid_kwargs):
+        forcing_grid_kwargs["rigid_body"] = rigid_body
+        super().__init__(eul_grid_forcing_field, eul_grid_velocity_field, np.zeros((3, 1)), np.zeros((3, 1)),
+                         forcing_grid_cls, virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, dx,
+                         grid_dim, real_t, eul_grid_coord_shift, interp_kernel_width, enable_eul_grid_forcing_reset,
+                         num_threads, start_time, **forcing_grid_kwargs)
+
+
+class CosseratRodFlowInteraction(ImmersedBodyFlowInteraction):
+    """cosserat_rod/cosserat_rod_flow_interaction.py:9-58."""
+
+    def __init__(self, cosserat_rod, eul_grid_forcing_field, eul_grid_velocity_field,
+                 virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, dx, grid_dim, forcing_grid_cls,
+                 real_t=np.float64, eul_grid_coord_shift=None, interp_kernel_width=None,
+                 enable_eul_grid_forcing_reset=False, num_threads=False, start_time=0.0, **forcing_grid_kwargs):
+        forcing_grid_kwargs["cosserat_rod"] = cosserat_rod
+        super().__init__(eul_grid_forcing_field, eul_grid_velocity_field, np.zeros((3, cosserat_rod.n_elems + 1)),
+                         np.zeros((3, cosserat_rod.n_elems)), forcing_grid_cls, virtual_boundary_stiffness_coeff,
+                         virtual_boundary_damping_coeff, dx, grid_dim, real_t, eul_grid_coord_shift,
+                         interp_kernel_width, enable_eul_grid_forcing_reset, num_threads, start_time,
+                         **forcing_grid_kwargs)
+
+
+try:  # FlowForces plugs into pyelastica's forcing interface when it is installed
+    from elastica import NoForces as _NoForces  # type: ignore
+except Exception:  # pragma: no cover - pyelastica absent
+    class _NoForces:  # minimal stand-in of elastica.NoForces
+        def __init__(self) -> None:
+            pass
+
+
+class FlowForces(_NoForces):
+    """flow_forces.py:12-25: adds the flow forces/torques to a pyelastica system."""
+
+    def __init__(self, body_flow_interactor) -> None:
+        super().__init__()
+        self.body_flow_interactor = body_flow_interactor
+
+    def apply_forces(self, system, time: float = 0.0) -> None:
+        self.body_flow_interactor.compute_flow_forces_and_torques()
+        system.external_forces += self.body_flow_interactor.body_flow_forces
+        system.external_torques += self.body_flow_interactor.body_flow_torques

@@ -1,0 +1,153 @@
+"""CPU checks of the C ABI and of the host-side reformulations (no GPU needed).
+
+* the library loads, and exports exactly the entry points ``include/*.h``
+  declares (and the ctypes binding knows each of them);
+* argument validation fails with the documented status before any CUDA call;
+* the GPU path's reformulations, restated in numpy, agree with the oracle:
+  penalisation as one clamped gather times per-index factors, and the
+  domain-doubled Poisson solve as row R2C -> column convolution -> row C2R
+  without materialising the doubled box.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+from conftest import load_golden, real_t_of, ref_tol
+
+from oracle import stencils as st
+from oracle.poisson import UnboundedPoisson2D, UnboundedPoisson3D, greens_function_2d, greens_function_3d
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sopht_gb300 import _lib
+    from sopht_gb300.build import LIB, build
+    if not LIB.exists():
+        build()
+    return _lib.load()
+
+
+def _header_symbols():
+    syms = set()
+    for h in (REPO / "include").glob("*.h"):
+        text = h.read_text()
+        syms |= set(re.findall(r"\b(sg_[a-z0-9_]+)\s*\(", text))
+    return syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from sopht_gb300 import _lib
+    declared = _header_symbols()
+    assert len(declared) >= 25
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+    assert declared == set(_lib.declared_symbols()), "ctypes binding out of sync with the header"
+    assert lib.sg_version() >= 100
+
+
+def test_argument_validation_without_gpu(lib):
+    plan = ctypes.c_void_p()
+    assert lib.sg_poisson_plan_create(4, 8, 8, 8, 1.0, 0, 1, ctypes.byref(plan)) == 1
+    assert b"dim" in lib.sg_last_error()
+    assert lib.sg_poisson_plan_create(2, 1, 8, 7, 1.0, 0, 1, ctypes.byref(plan)) == 2  # odd nx
+    assert lib.sg_poisson_plan_create(2, 1, 8, 8, 1.0, 7, 1, ctypes.byref(plan)) == 1  # bad dtype
+    assert lib.sg_poisson_plan_create(2, 1, 10, 22, 1.0, 0, 1, ctypes.byref(plan)) == 4  # nx = 2*11
+    assert lib.sg_flow_plan_create(2, 1, 4, 4, 1.0, 0, 2, None, None, None, 0, 0, ctypes.byref(plan)) == 2
+    assert lib.sg_ib_spread(0, 5, 1, 8, 8, 3, None, None, None, None, 0, None) == 1
+
+
+def _clamped_penalise(field, width, cx, cy, cz=None):
+    """Penalisation as the fused kernels do it: gather from the clamped index, times factors."""
+    def clamp(i, n):
+        return np.clip(i, width - 1, n - width) if width > 0 else i
+
+    if field.ndim == 2:
+        ny, nx = field.shape
+        yy, xx = np.meshgrid(clamp(np.arange(ny), ny), clamp(np.arange(nx), nx), indexing="ij")
+        out = field[yy, xx] * cx[None, :]
+        return out * cy[:, None]
+    nz, ny, nx = field.shape
+    zz, yy, xx = np.meshgrid(clamp(np.arange(nz), nz), clamp(np.arange(ny), ny), clamp(np.arange(nx), nx),
+                             indexing="ij")
+    out = field[zz, yy, xx] * cx[None, None, :]
+    out = out * cy[None, :, None]
+    return out * cz[:, None, None]
+
+
+@pytest.mark.parametrize("width", [0, 2, 3, 4])
+def test_penalise_as_clamped_gather(precision, width):
+    from sopht_gb300.numeric.eulerian_grid_ops import penalisation_factors
+    g = load_golden("stencils2d", precision)
+    rt = real_t_of(precision)
+    for tag in ("sq", "rect"):
+        f = g[f"{tag}/field"]
+        pos = g[f"{tag}/position"]
+        dx = rt(1.0 / f.shape[1])
+        ref = f.copy()
+        st.penalise_2d(ref, width, dx, pos[0], pos[1])
+        cx = penalisation_factors(width, dx, pos[0][0, :], rt)
+        cy = penalisation_factors(width, dx, pos[1][:, 0], rt)
+        np.testing.assert_array_equal(_clamped_penalise(f, width, cx, cy), ref)
+    g3 = load_golden("stencils3d", precision)
+    f = g3["rect/field"][0]
+    pos = g3["rect/position"]
+    dx = rt(1.0 / f.shape[2])
+    ref = f.copy()
+    st.penalise_3d(ref, width, dx, pos[0], pos[1], pos[2])
+    cx = penalisation_factors(width, dx, pos[0][0, 0, :], rt)
+    cy = penalisation_factors(width, dx, pos[1][0, :, 0], rt)
+    cz = penalisation_factors(width, dx, pos[2][:, 0, 0], rt)
+    np.testing.assert_array_equal(_clamped_penalise(f, width, cx, cy, cz), ref)
+
+
+def _split_solve_2d(rhs, ny, nx, x_range):
+    """Row R2C (implicit zero pad) -> column FFT * G_sym * IFFT, crop -> row C2R, crop."""
+    g, dx = greens_function_2d(ny, nx, x_range, np.float64)
+    ghat = np.fft.rfft2(g).real[: ny + 1, :] * dx**2 / (4 * ny * nx)
+    a = np.fft.rfft(rhs, n=2 * nx, axis=1)                     # (ny, nx+1)
+    b = np.fft.fft(a, n=2 * ny, axis=0)                        # (2ny, nx+1)
+    ks = np.minimum(np.arange(2 * ny), 2 * ny - np.arange(2 * ny))
+    b = b * ghat[ks, :]
+    c = np.fft.ifft(b, axis=0)[:ny] * (2 * ny)                 # unnormalised inverse, crop
+    return np.fft.irfft(c, n=2 * nx, axis=1)[:, :nx] * (2 * nx)
+
+
+def _split_solve_3d(rhs, nz, ny, nx, x_range):
+    g, dx = greens_function_3d(nz, ny, nx, x_range, np.float64)
+    ghat = np.fft.rfftn(g).real[: nz + 1, : ny + 1, :] * dx**3 / (8 * nz * ny * nx)
+    a = np.fft.rfft(rhs, n=2 * nx, axis=2)
+    a = np.fft.fft(a, n=2 * ny, axis=1)
+    a = np.fft.fft(a, n=2 * nz, axis=0)
+    kz = np.minimum(np.arange(2 * nz), 2 * nz - np.arange(2 * nz))
+    ky = np.minimum(np.arange(2 * ny), 2 * ny - np.arange(2 * ny))
+    a = a * ghat[kz][:, ky, :]
+    a = np.fft.ifft(a, axis=0)[:nz] * (2 * nz)
+    a = np.fft.ifft(a, axis=1)[:, :ny] * (2 * ny)
+    return np.fft.irfft(a, n=2 * nx, axis=2)[..., :nx] * (2 * nx)
+
+
+def test_split_poisson_matches_doubled_box():
+    rng = np.random.default_rng(5)
+    for ny, nx, xr in ((12, 24, 1.0), (16, 16, 2.0), (6, 12, 1.0)):
+        rhs = rng.standard_normal((ny, nx))
+        ref = UnboundedPoisson2D(ny, nx, xr, np.float64).solve(rhs)
+        np.testing.assert_allclose(_split_solve_2d(rhs, ny, nx, xr), ref, rtol=0, atol=1e-13)
+    for nz, ny, nx in ((6, 8, 12), (8, 8, 8)):
+        rhs = rng.standard_normal((nz, ny, nx))
+        ref = UnboundedPoisson3D(nz, ny, nx, 1.0, np.float64).solve(rhs)
+        np.testing.assert_allclose(_split_solve_3d(rhs, nz, ny, nx, 1.0), ref, rtol=0, atol=1e-13)
+
+
+def test_ghat_is_real_and_symmetric():
+    """The even-reflected Green's function has a real, even transform (table storage)."""
+    g, _ = greens_function_3d(6, 8, 10, 1.0, np.float64)
+    gh = np.fft.rfftn(g)
+    assert np.abs(gh.imag).max() < 1e-12 * np.abs(gh.real).max()
+    np.testing.assert_allclose(gh.real[1:6], gh.real[-1:-6:-1], rtol=1e-12, atol=1e-14)
