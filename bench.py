@@ -238,7 +238,8 @@ def run_gpu(args, rank, world):
     kernels = {}
     for name, vals in per_pass.items():
         ms = float(np.mean(vals))
-        kernels[name] = {"ms": round(ms, 5), "GB_s": round(PASS_BYTES[name] * cells / (ms * 1e-3) / 1e9, 1)}
+        kernels[name] = {"ms": round(ms, 5), "GB_s": round(PASS_BYTES[name] * cells / (ms * 1e-3) / 1e9, 1),
+                         "launches_timed": len(vals)}
     value = world * steps / (elapsed_ms * 1e-3)
 
     # end to end through the public API: host dt, H2D marker kinematics, D2H forcing

@@ -46,8 +46,10 @@ struct sg_flow_plan_s {
 namespace sg {
 
 // Record timing event `i` of the armed set (no-op when none is armed).
+// The external flag makes the record a node of a graph being captured (a plain
+// record during capture only orders streams); outside capture it is a normal record.
 static inline void mark(sg_flow_plan_s* p, int i, cudaStream_t stream) {
-    if (i < p->n_events && p->events[i]) cudaEventRecord(p->events[i], stream);
+    if (i < p->n_events && p->events[i]) cudaEventRecordWithFlags(p->events[i], stream, cudaEventRecordExternal);
 }
 
 static void flow_plan_free(sg_flow_plan_s* p) {
