@@ -40,7 +40,7 @@ inline bool fft_factor(int n, FFTStages& st) {
     st.nstages = 0;
     if (n < 1) return false;
     int m = n;
-    while (m % 8 == 0 && m > 8) { st.radix[st.nstages++] = 8; m /= 8; }
+    while (m % 8 == 0) { st.radix[st.nstages++] = 8; m /= 8; }
     while (m % 4 == 0) { st.radix[st.nstages++] = 4; m /= 4; }
     while (m % 2 == 0) { st.radix[st.nstages++] = 2; m /= 2; }
     while (m % 3 == 0) { st.radix[st.nstages++] = 3; m /= 3; }
@@ -441,7 +441,7 @@ inline int lines_per_block_for(int N, int elem_bytes) {
 }
 
 template <typename T>
-int launch_rows_r2c(RowsR2CParams<T> p, cudaStream_t stream) {
+int launch_rows_r2c_generic(RowsR2CParams<T> p, cudaStream_t stream) {
     const int esz = sizeof(cplx_t<T>);
     const int rb = rows_per_block_for(p.st.n, esz);
     const size_t smem = 2ull * rb * p.st.n * esz;
@@ -454,7 +454,7 @@ int launch_rows_r2c(RowsR2CParams<T> p, cudaStream_t stream) {
 }
 
 template <typename T>
-int launch_rows_c2r(RowsC2RParams<T> p, cudaStream_t stream) {
+int launch_rows_c2r_generic(RowsC2RParams<T> p, cudaStream_t stream) {
     const int esz = sizeof(cplx_t<T>);
     const int rb = rows_per_block_for(p.st.n, esz);
     const size_t smem = 2ull * rb * p.st.n * esz;
@@ -467,7 +467,7 @@ int launch_rows_c2r(RowsC2RParams<T> p, cudaStream_t stream) {
 }
 
 template <typename T, int MODE>
-int launch_lines(LinesParams<T> p, cudaStream_t stream) {
+int launch_lines_generic(LinesParams<T> p, cudaStream_t stream) {
     const int esz = sizeof(cplx_t<T>);
     if (p.W <= 0) p.W = lines_per_block_for(p.st.n, esz);
     const size_t smem = 2ull * p.W * p.st.n * esz;

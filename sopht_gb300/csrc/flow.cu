@@ -88,8 +88,21 @@ int launch_sweep2d(const Sweep2DParams<T>& p, cudaStream_t stream) {
     return launch_status("sweep2d");
 }
 
+template <typename T, int N>
+int launch_fast_flow_load(const FlowLoadParams<T>& p, cudaStream_t stream) {
+    const size_t smem = fast_smem_bytes<N>(sizeof(cplx_t<T>));
+    auto kern = fast_flow_load_kernel<T, N>;
+    SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "fast flow_load smem attribute"));
+    kern<<<ceil_div(p.n_rows, FastShape<N>::W), FastShape<N>::NT, smem, stream>>>(p);
+    return launch_status("fast flow_load");
+}
+
 template <typename T>
 int launch_flow_load(FlowLoadParams<T> p, cudaStream_t stream) {
+#define SG_CALL(NN) launch_fast_flow_load<T, NN>(p, stream)
+    SG_FAST_SWITCH(p.st.n, SG_CALL)
+#undef SG_CALL
     const int esz = sizeof(cplx_t<T>);
     const int rb = rows_per_block_for(p.st.n, esz);
     const size_t smem = 2ull * rb * p.st.n * esz;
@@ -169,6 +182,7 @@ static FlowLoadParams<T> load_params(sg_flow_plan_s* p, const T* src, T* dst, T*
     l.src = src;
     l.dst = dst;
     l.forcing = forcing;
+    l.zero_ncomp = 1;
     l.cx = (const T*)p->coef_x;
     l.cy = (const T*)p->coef_y;
     l.cz = (const T*)p->coef_z;
@@ -202,9 +216,9 @@ int flow_step_2d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
     mark(p, 0, stream);
     SG_TRY(launch_sweep2d<T>(s, stream));
     mark(p, 1, stream);
-    FlowLoadParams<T> l = load_params<T>(p, (const T*)p->scratch_a, w, nullptr);
+    FlowLoadParams<T> l = load_params<T>(p, (const T*)p->scratch_a, w, f);
+    l.zero_ncomp = 2;  // one vorticity row zeroes the row of both forcing components
     SG_TRY(launch_flow_load<T>(l, stream));
-    if (f) SG_TRY(cuda_status(cudaMemsetAsync(f, 0, 2 * sizeof(T) * p->cells(), stream), "forcing reset"));
     mark(p, 2, stream);
     SG_TRY(poisson_spectral_passes<T>(p->poisson, 1, stream));
     mark(p, 3, stream);

@@ -10,7 +10,7 @@
 #pragma once
 
 #include "common.cuh"
-#include "fft.cuh"
+#include "fft_fast.cuh"
 
 namespace sg {
 
@@ -164,6 +164,7 @@ template <typename T> struct FlowLoadParams {
     const T* src;            // swept vorticity, same layout as dst
     T* dst;                  // caller's vorticity (penalised copy)
     T* forcing;              // zeroed when not null
+    int zero_ncomp;          // forcing rows zeroed per row: the row's component and the next ones
     const T* cx;             // penalisation factors per index (null if width 0)
     const T* cy;
     const T* cz;
@@ -224,7 +225,8 @@ __global__ void __launch_bounds__(256) flow_load_kernel(FlowLoadParams<T> p) {
                         if (p.dim == 3) val = val * p.cz[zi];
                     }
                     p.dst[dst_row + x] = val;
-                    if (p.forcing) p.forcing[dst_row + x] = T(0);
+                    if (p.forcing)
+                        for (int zc = 0; zc < p.zero_ncomp; ++zc) p.forcing[dst_row + zc * p.comp_stride + x] = T(0);
                 }
                 v[h] = val;
             }
@@ -245,6 +247,69 @@ __global__ void __launch_bounds__(256) flow_load_kernel(FlowLoadParams<T> p) {
         const C wd = cmul(w, csub(zk, zc));
         p.spec[p.spec_map.offset(q) + k] = cmake<C>(T(0.5) * (s.x + wd.y), T(0.5) * (s.y - wd.x));
     }
+}
+
+// Size-specialised variant of flow_load_kernel (M = nx in FastShape set).
+template <typename T, int M>
+__global__ void __launch_bounds__(FastShape<M>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
+    using C = cplx_t<T>;
+    using S = FastShape<M>;
+    constexpr int W = S::W, LS = S::LS, NT = S::NT, PER = M * W / NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* buf = reinterpret_cast<C*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int row0 = blockIdx.x * W;
+    const int nx = p.nx;  // == M
+#pragma unroll
+    for (int b = 0; b < PER; ++b) {
+        const int e = tid + b * NT;
+        const int r = e / M, n = e % M;
+        const int q = row0 + r;
+        C z = cmake<C>(T(0), T(0));
+        if (q < p.n_rows && 2 * n < nx) {
+            const int y = q % p.ny;
+            int c, zi;
+            if (p.dim == 3) {
+                zi = (q / p.ny) % p.nz;
+                c = q / (p.ny * p.nz);
+            } else {
+                zi = 0;
+                c = q / p.ny;
+            }
+            const int sy = clamp_band(y, p.ny, p.width);
+            const int sz = p.dim == 3 ? clamp_band(zi, p.nz, p.width) : 0;
+            const int64_t src_row = (int64_t)c * p.comp_stride + ((int64_t)sz * p.ny + sy) * nx;
+            const int64_t dst_row = (int64_t)c * p.comp_stride + ((int64_t)zi * p.ny + y) * nx;
+            const int x0 = 2 * n;
+            const int s0 = clamp_band(x0, nx, p.width), s1 = clamp_band(x0 + 1, nx, p.width);
+            if (s0 == x0 && s1 == x0 + 1) {
+                z = *reinterpret_cast<const C*>(p.src + src_row + x0);
+            } else {
+                z.x = p.src[src_row + s0];
+                z.y = p.src[src_row + s1];
+            }
+            if (p.width > 0) {
+                z.x = z.x * p.cx[x0];
+                z.y = z.y * p.cx[x0 + 1];
+                const T fy = p.cy[y];
+                z.x = z.x * fy;
+                z.y = z.y * fy;
+                if (p.dim == 3) {
+                    const T fz = p.cz[zi];
+                    z.x = z.x * fz;
+                    z.y = z.y * fz;
+                }
+            }
+            *reinterpret_cast<C*>(p.dst + dst_row + x0) = z;
+            if (p.forcing)
+                for (int zc = 0; zc < p.zero_ncomp; ++zc)
+                    *reinterpret_cast<C*>(p.forcing + dst_row + zc * p.comp_stride + x0) = cmake<C>(T(0), T(0));
+        }
+        buf[n * LS + r] = z;
+    }
+    __syncthreads();
+    fast_fft<M, false>(buf, p.tw_m, tid);
+    r2c_post_store<T, M>(buf, p.tw_l, p.spec, p.spec_map, row0, p.n_rows, tid);
 }
 
 // ---------------------------------------- curl + free stream + max |u| (2D)

@@ -1,7 +1,7 @@
 // Internal definition of the unbounded Poisson plan, shared with the flow step.
 #pragma once
 
-#include "fft.cuh"
+#include "fft_fast.cuh"
 
 struct sg_poisson_plan_s {
     int dim = 2;

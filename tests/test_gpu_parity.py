@@ -74,9 +74,13 @@ def test_poisson_3d_vs_reference(precision, tag):
     assert rel_l2(out, g[f"{tag}/solution"]) < RTOL_L2[precision]
 
 
-@pytest.mark.parametrize("shape", [(64, 128), (96, 192), (48, 96), (128, 64), (81, 162), (50, 100), (35, 70)])
+@pytest.mark.parametrize("shape", [(64, 128), (96, 192), (48, 96), (128, 64), (81, 162), (50, 100), (35, 70),
+                                   (32, 64), (128, 256), (192, 384), (256, 512), (384, 768), (512, 1024)])
 def test_poisson_2d_vs_oracle_sizes(precision, shape):
-    """Radix 2, 3, 5, 7 lengths (2*96 = 3*64, 2*81 = 2*3^4, 100, 70) against the oracle."""
+    """Generic (radix 2, 3, 5, 7) and size-specialised FFT lengths against the FP64 oracle.
+
+    Size-specialised lengths: 64, 128, 192, 256, 384, 512, 768, 1024 (rows use
+    M = nx, columns 2 ny); the others take the generic kernels."""
     from oracle.poisson import UnboundedPoisson2D
     from sopht_gb300.numeric import UnboundedPoissonSolver2D as GPUPoisson
     ny, nx = shape
@@ -89,7 +93,8 @@ def test_poisson_2d_vs_oracle_sizes(precision, shape):
     assert rel_l2(host(sol), ref) < (2e-6 if rt == np.float32 else 1e-13)
 
 
-@pytest.mark.parametrize("shape", [(32, 48, 64), (24, 24, 24), (16, 32, 48)])
+@pytest.mark.parametrize("shape", [(32, 48, 64), (24, 24, 24), (16, 32, 48), (64, 64, 64), (32, 64, 128),
+                                   (128, 128, 128)])
 def test_poisson_3d_vs_oracle_sizes(precision, shape):
     from oracle.poisson import UnboundedPoisson3D
     from sopht_gb300.numeric import UnboundedPoissonSolver3D as GPUPoisson
@@ -241,14 +246,13 @@ def test_ns_step_3d_vs_reference(precision, tag):
     assert torch.count_nonzero(sim.eul_grid_forcing_field).item() == 0
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-def test_multi_step_vs_oracle_and_determinism(precision, dim):
+@pytest.mark.parametrize("dim,grid", [(2, (64, 128)), (2, (96, 192)), (3, (24, 30, 40)), (3, (32, 32, 64))])
+def test_multi_step_vs_oracle_and_determinism(precision, dim, grid):
     """Ten forced steps on a larger grid against the oracle; two runs bitwise equal."""
     import sopht_gb300.simulator as sps
     from oracle.flow import NavierStokes2DOracle, NavierStokes3DOracle
     rt = real_t_of(precision)
     rng = np.random.default_rng(3)
-    grid = (64, 128) if dim == 2 else (24, 30, 40)
     kw = dict(grid_size=grid, x_range=1.0, kinematic_viscosity=2e-3, real_t=rt, with_forcing=True,
               with_free_stream_flow=True)
     w0 = rng.standard_normal((grid if dim == 2 else (3, *grid))).astype(rt)
