@@ -82,6 +82,22 @@ int64_t sg_poisson_plan_bytes(sg_poisson_plan plan);
 int sg_poisson_solve(sg_poisson_plan plan, const void* rhs, void* sol, int ncomp,
                      int64_t comp_stride, void* stream);
 
+/* Allocation-free variant of the 2D solve (no counterpart in the reference).
+ * For callers that cannot allocate device memory: code running inside CUDA
+ * graph capture, hosts whose device memory is owned by another framework's
+ * pool, and embeddings that forbid allocation after start-up.  It solves the
+ * same problem as sg_poisson_solve with ncomp = 1, fp32 only, using a fixed
+ * ~10 MB file-scope device array instead of a plan (every GPU that loads the
+ * library holds it until the process exits).  Limit: ny <= 256, even
+ * nx <= 512; larger grids return SG_ERR_SHAPE.  The first call on a device
+ * (and a call with a new ny, nx or x_range) looks up the array's address and
+ * rebuilds the Green's table into it, so make that first call before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps
+ * (other streams, other host threads) race and must be serialised by the
+ * caller. */
+int sg_poisson2d_solve_noalloc(int ny, int nx, double x_range, const float* rhs, float* sol,
+                               void* stream);
+
 /* --------------------------------------------------------- flow step plan */
 /* Replaces the kernel compilation of UnboundedNavierStokesFlowSimulator2D/3D
  * (navier_stokes_flow_simulators.py:89-162, 327-440).  pen_coef_{x,y,z} are

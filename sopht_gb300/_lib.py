@@ -42,6 +42,7 @@ _SIGNATURES = {
     "sg_poisson_plan_destroy": (c_int, [c_void_p]),
     "sg_poisson_plan_bytes": (c_int64, [c_void_p]),
     "sg_poisson_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int64, c_void_p]),
+    "sg_poisson2d_solve_noalloc": (c_int, [c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]),
     "sg_flow_plan_create": (c_int, [c_int, c_int, c_int, c_int, c_double, c_int, c_int, c_void_p, c_void_p,
                                     c_void_p, c_int, c_int, POINTER(c_void_p)]),
     "sg_flow_plan_destroy": (c_int, [c_void_p]),

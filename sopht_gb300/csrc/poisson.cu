@@ -404,3 +404,153 @@ extern "C" int sg_poisson_solve(sg_poisson_plan p, const void* rhs, void* sol, i
     SG_TRY(sg::poisson_spectral_passes<double>(p, ncomp, stream));
     return sg::poisson_store_rows<double>(p, (double*)sol, ncomp, comp_stride, stream);
 }
+
+// ===========================================================================
+// Allocation-free 2D solve.
+//
+// Some callers cannot call cudaMalloc at all: code that runs while a CUDA
+// graph is being captured, a host application whose memory pools are owned by
+// another framework and must not grow, or an embedding that forbids device
+// allocation after start-up.  For them sg_poisson2d_solve_noalloc solves the
+// same unbounded 2D Poisson problem as sg_poisson_solve without any allocation:
+// its FFT workspace, Green's table and twiddles, and the FP64 buffers used to
+// build the table, live in one file-scope __device__ array of fixed size,
+// which every GPU that loads this library holds until the process exits.
+//
+// Limits: fp32 only, ny <= 256 and nx <= 512 (nx even; nx, 2 ny with prime
+// factors 2, 3, 5, 7 only).  Larger grids are rejected with SG_ERR_SHAPE.
+// ===========================================================================
+namespace sg {
+
+constexpr int kNoAllocMaxNy = 256;
+constexpr int kNoAllocMaxNx = 512;
+
+// byte offsets inside the static scratch (each region 256-byte aligned)
+constexpr size_t na_align(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t kNaGreens64 = 0;  // double G, (2 ny) x (2 nx)
+constexpr size_t kNaSpec64 = na_align(kNaGreens64 + sizeof(double) * 2 * kNoAllocMaxNy * 2 * kNoAllocMaxNx);
+constexpr size_t kNaTw64 = na_align(kNaSpec64 + sizeof(double2) * 2 * kNoAllocMaxNy * (kNoAllocMaxNx + 1));
+// double twiddles: nx, nx + 1, 2 ny entries
+constexpr size_t kNaTable = na_align(kNaTw64 + sizeof(double2) * (2 * kNoAllocMaxNx + 1 + 2 * kNoAllocMaxNy));
+constexpr size_t kNaSpec = na_align(kNaTable + sizeof(float) * (kNoAllocMaxNy + 1) * (kNoAllocMaxNx + 1));
+constexpr size_t kNaTw = na_align(kNaSpec + sizeof(float2) * kNoAllocMaxNy * (kNoAllocMaxNx + 1));
+constexpr size_t kNaBytes = na_align(kNaTw + sizeof(float2) * (2 * kNoAllocMaxNx + 1 + 2 * kNoAllocMaxNy));
+
+// The scratch.  Host code must not use this name as an address: it is a host
+// stand-in; the device address comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NoAllocState {
+    unsigned char* base = nullptr;  // device address of g_noalloc_scratch
+    bool table_ready = false;
+    int ny = 0, nx = 0;
+    double x_range = 0.0;
+};
+constexpr int kNoAllocMaxDevices = 64;
+static NoAllocState g_noalloc_state[kNoAllocMaxDevices];
+
+static int noalloc_build(NoAllocState& st, sg_poisson_plan_s& p, cudaStream_t stream) {
+    unsigned char* b = st.base;
+    const int nx = p.nx, ny = p.ny;
+    double* g = reinterpret_cast<double*>(b + kNaGreens64);
+    double2* spec64 = reinterpret_cast<double2*>(b + kNaSpec64);
+    double2* tw64x = reinterpret_cast<double2*>(b + kNaTw64);
+    double2* tw64xl = tw64x + nx;
+    double2* tw64y = tw64xl + (nx + 1);
+    float2* twx = reinterpret_cast<float2*>(b + kNaTw);
+    float2* twxl = twx + nx;
+    float2* twy = twxl + (nx + 1);
+    twiddle_kernel<double><<<ceil_div(nx, 256), 256, 0, stream>>>(tw64x, nx, nx);
+    twiddle_kernel<double><<<ceil_div(nx + 1, 256), 256, 0, stream>>>(tw64xl, nx + 1, 2 * nx);
+    twiddle_kernel<double><<<ceil_div(2 * ny, 256), 256, 0, stream>>>(tw64y, 2 * ny, 2 * ny);
+    twiddle_kernel<float><<<ceil_div(nx, 256), 256, 0, stream>>>(twx, nx, nx);
+    twiddle_kernel<float><<<ceil_div(nx + 1, 256), 256, 0, stream>>>(twxl, nx + 1, 2 * nx);
+    twiddle_kernel<float><<<ceil_div(2 * ny, 256), 256, 0, stream>>>(twy, 2 * ny, 2 * ny);
+    SG_TRY(launch_status("noalloc twiddles"));
+    const int64_t nreal = (int64_t)2 * ny * 2 * nx;
+    const double y_range = p.x_range * ((double)ny / nx);
+    greens_2d_kernel<<<ceil_div(nreal, 256), 256, 0, stream>>>(g, 2 * ny, 2 * nx, p.x_range, y_range, p.dx);
+    SG_TRY(launch_status("noalloc greens"));
+    RowsR2CParams<double> r{};
+    r.in = g;
+    r.in_map = row_map(2 * ny, 2 * nx);
+    r.n_in = 2 * nx;
+    r.out = spec64;
+    r.out_map = row_map(2 * ny, nx + 1);
+    r.n_rows = 2 * ny;
+    r.st = p.st_x;
+    r.tw_m = tw64x;
+    r.tw_l = tw64xl;
+    SG_TRY(launch_rows_r2c<double>(r, stream));
+    LinesParams<double> ly{};
+    ly.in = spec64;
+    ly.out = spec64;
+    ly.n_in = 2 * ny;
+    ly.n_out = 2 * ny;
+    ly.inner = nx + 1;
+    ly.line_stride = nx + 1;
+    ly.outer_stride = 0;
+    ly.n_outer = 1;
+    ly.st = p.st_y;
+    ly.tw = tw64y;
+    SG_TRY((launch_lines<double, LINE_FWD>(ly, stream)));
+    const int64_t table_elems = (int64_t)(ny + 1) * (nx + 1);
+    greens_extract_kernel<float><<<ceil_div(table_elems, 256), 256, 0, stream>>>(
+        reinterpret_cast<float*>(b + kNaTable), spec64, 0, ny, nx + 1, 0, nx + 1, p.dx * p.dx / (4.0 * ny * nx));
+    return launch_status("noalloc greens extract");
+}
+
+}  // namespace sg
+
+extern "C" int sg_poisson2d_solve_noalloc(int ny, int nx, double x_range, const float* rhs, float* sol,
+                                          void* stream_) {
+    using namespace sg;
+    SG_REQUIRE(rhs && sol, SG_ERR_INVALID_ARG, "poisson2d noalloc: null field pointer");
+    SG_REQUIRE(ny >= 2 && nx >= 2 && nx % 2 == 0 && ny <= kNoAllocMaxNy && nx <= kNoAllocMaxNx, SG_ERR_SHAPE,
+               "poisson2d noalloc: grid (%d, %d) outside the static scratch limit (ny <= %d, even nx <= %d)", ny,
+               nx, kNoAllocMaxNy, kNoAllocMaxNx);
+    SG_REQUIRE(x_range > 0, SG_ERR_INVALID_ARG, "poisson2d noalloc: x_range must be positive");
+    sg_poisson_plan_s p;
+    p.dim = 2;
+    p.nz = 1;
+    p.ny = ny;
+    p.nx = nx;
+    p.dtype = SG_F32;
+    p.max_comp = 1;
+    p.x_range = x_range;
+    p.dx = (double)(float)(x_range / nx);
+    if (!(fft_factor(nx, p.st_x) && fft_factor(2 * ny, p.st_y))) {
+        set_last_error("poisson2d noalloc: nx=%d and 2ny=%d must factor into 2, 3, 5 and 7", nx, 2 * ny);
+        return SG_ERR_UNSUPPORTED;
+    }
+    int dev = 0;
+    SG_TRY(cuda_status(cudaGetDevice(&dev), "poisson2d noalloc: cudaGetDevice"));
+    SG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, SG_ERR_INVALID_ARG, "poisson2d noalloc: device %d", dev);
+    NoAllocState& st = g_noalloc_state[dev];
+    if (st.base == nullptr) {
+        // once per device, with that device current
+        void* addr = nullptr;
+        SG_TRY(cuda_status(cudaGetSymbolAddress(&addr, g_noalloc_scratch), "poisson2d noalloc: symbol address"));
+        st.base = static_cast<unsigned char*>(addr);
+    }
+    auto stream = (cudaStream_t)stream_;
+    if (!st.table_ready || st.ny != ny || st.nx != nx || st.x_range != x_range) {
+        st.table_ready = false;
+        SG_TRY(noalloc_build(st, p, stream));
+        st.table_ready = true;
+        st.ny = ny;
+        st.nx = nx;
+        st.x_range = x_range;
+    }
+    unsigned char* b = st.base;
+    float2* twx = reinterpret_cast<float2*>(b + kNaTw);
+    p.tw_x = twx;
+    p.tw_xl = twx + nx;
+    p.tw_y = twx + nx + (nx + 1);
+    p.greens = b + kNaTable;
+    p.spec = b + kNaSpec;
+    p.spec_comp_elems = (int64_t)ny * (nx + 1);
+    SG_TRY(poisson_load_rows<float>(&p, rhs, 1, 0, stream));
+    SG_TRY(poisson_spectral_passes<float>(&p, 1, stream));
+    return poisson_store_rows<float>(&p, sol, 1, 0, stream);
+}
