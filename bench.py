@@ -1,16 +1,24 @@
-"""Benchmark: the coupled 3D rod-in-flow step on GB300 (flow steps/s).
+"""Benchmark: coupled flow steps/s of the SophT flow-step hot path on GB300.
 
-Workload (one GPU): unbounded vorticity Navier-Stokes on a 128^3 grid, fp32,
-cubic domain of side 1 (Poisson by domain doubling to a 256^3 FFT), one
-clamped rod of 64 elements (length 0.3, radius 0.01) at the domain centre with
-an element-centric forcing grid and cosine-delta virtual-boundary coupling
-(K = -2e4, C = -1e2), uniform inflow U = 1, Re = 100 on the rod length
-(nu = 3e-3), dt from the stable-timestep rule at CFL 0.1.  One step is: stable
-dt, interactor time_step + interaction + spreading, flow time step.
+Workloads (``--workload``, one GPU each; the default is the headline one):
 
-The rod stays on the host (pyelastica's role); here it is held rigid and
-clamped (its markers do not move), which is the configuration's initial
-state; the rod dynamics integrator is not part of the timed path in either arm.
+  rod128     3D unbounded vorticity Navier-Stokes on 128^3, fp32, cubic domain of
+             side 1 (Poisson by domain doubling, 256^3 FFT), one clamped rod of 64
+             elements (length 0.3, radius 0.01) at the domain centre with an
+             element-centric forcing grid and cosine-delta virtual-boundary
+             coupling (K = -2e4, C = -1e2), inflow U = 1, Re = 100 on the rod
+             length, dt from the stable-timestep rule at CFL 0.1.
+  cylinder2d 2D 256(y) x 512(x), fp32, x-domain 1, cylinder of diameter 0.1 at
+             (0.25, 0.25) with 96 markers, K = -5e4, C = -20, U = 1,
+             Re = 200 on the diameter, CFL 0.1.
+  carpet256  3D 256^3, fp32, a 4 x 4 carpet of 16 clamped rods (100 elements,
+             length 0.2, radius 0.005) standing on the plane z0 = 6 dx, one
+             interactor per rod, U = 1 along x, Re = 500 on the rod length.
+
+One step is: stable dt, every interactor's time_step + interaction +
+spreading, then the flow time step.  Rods and the cylinder stay on the host
+(pyelastica's role); they are held at their initial, clamped pose, so the body
+integrator is not part of the timed path in either arm.
 
 Arms
   default            this repository's GPU path.
@@ -18,7 +26,7 @@ Arms
                (device dt + IB interaction + spread + flow step) replayed K times.
       e2e    : the same steps through the public Python API, per step uploading
                the marker kinematics from pinned host memory and reading the
-               Lagrangian forcing back (what a host rod integrator needs).
+               Lagrangian forcing back (what a host body integrator needs).
   --impl reference   the reference algorithm's CPU implementation (the numpy/
                scipy oracle of this repository, since the reference's own JIT
                dependencies are not installable), all host cores, bounded sample.
@@ -29,11 +37,13 @@ Prints one JSON line on rank 0.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
 import sys
 import time
+from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
@@ -41,45 +51,91 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-GRID = (128, 128, 128)
-X_RANGE = 1.0
-U_INF = np.array([1.0, 0.0, 0.0])
-ROD_LENGTH, ROD_RADIUS, N_ELEM = 0.3, 0.01, 64
-NU = 1.0 * ROD_LENGTH / 100.0
-K_STIFF, C_DAMP = -2e4, -1e2
-CFL = 0.1
 METRIC = "flow steps/s & Gcell-updates/s vs plain GPU path at stated FP64-oracle L2 error"
-WORKLOAD = ("3D unbounded vorticity NS 128^3 fp32 (256^3 doubled FFT), one clamped rod (64 elements, "
-            "element-centric cosine-delta forcing), U=1 inflow, Re=100 on rod length, CFL 0.1")
 
-# algorithmic bytes per cell per pass of the fused fp32 3D step (3 components)
-PASS_NAMES = ["forcing_curl", "uxw_update", "diffusion", "poisson_load", "y_fft", "z_conv", "y_ifft",
-              "x_c2r", "curl"]
-PASS_BYTES = {  # per cell, fp32, read + write
-    "forcing_curl": 36, "uxw_update": 36, "diffusion": 24, "poisson_load": 60, "y_fft": 72, "z_conv": 108,
-    "y_ifft": 72, "x_c2r": 36, "curl": 24}
+# algorithmic bytes per cell per pass of the fp32 step (read + write)
+PASSES_3D = {"forcing_curl": 36, "uxw_update": 36, "diffusion": 24, "poisson_load": 60, "y_fft": 72,
+             "z_conv": 108, "y_ifft": 72, "x_c2r": 36, "curl": 24}
+PASSES_2D = {"sweep": 24, "poisson_load": 32, "y_conv": 20, "x_c2r": 12, "curl": 12}
 
 
 class RodState:
-    """A straight clamped rod with the attributes the forcing grids read."""
+    """A straight rod along z with the attributes the forcing grids read."""
 
-    def __init__(self):
-        n = N_ELEM
-        base = np.array([0.5, 0.5, 0.5 - ROD_LENGTH / 2])
-        s = np.linspace(0.0, ROD_LENGTH, n + 1)
-        self.n_elems = n
-        self.position_collection = base[:, None] + np.outer([0.0, 0.0, 1.0], s)
-        self.velocity_collection = np.zeros((3, n + 1))
-        area = np.pi * ROD_RADIUS**2
-        self.mass = np.full(n + 1, area * ROD_LENGTH / n)
+    def __init__(self, base, length, radius, n_elem):
+        s = np.linspace(0.0, length, n_elem + 1)
+        self.n_elems = n_elem
+        self.position_collection = np.asarray(base, dtype=np.float64)[:, None] + np.outer([0.0, 0.0, 1.0], s)
+        self.velocity_collection = np.zeros((3, n_elem + 1))
+        area = np.pi * radius**2
+        self.mass = np.full(n_elem + 1, area * length / n_elem)
         self.mass[[0, -1]] *= 0.5
-        self.lengths = np.full(n, ROD_LENGTH / n)
-        self.director_collection = np.repeat(np.eye(3)[:, :, None], n, axis=2)
+        self.lengths = np.full(n_elem, length / n_elem)
+        self.director_collection = np.repeat(np.eye(3)[:, :, None], n_elem, axis=2)
 
 
-def initial_vorticity(real_t):
-    rng = np.random.default_rng(42)
-    return (1e-3 * rng.standard_normal((3, *GRID))).astype(real_t)
+@dataclass
+class Workload:
+    name: str
+    description: str
+    grid: tuple
+    nu: float
+    u_inf: np.ndarray
+    kind: str                      # "rods" or "cylinder"
+    bodies: list = field(default_factory=list)
+    K: float = 0.0
+    C: float = 0.0
+    x_range: float = 1.0
+    cfl: float = 0.1
+    n_markers: int = 96
+
+    @property
+    def dim(self):
+        return len(self.grid)
+
+    @property
+    def passes(self):
+        return PASSES_3D if self.dim == 3 else PASSES_2D
+
+    @property
+    def cells(self):
+        return int(np.prod(self.grid))
+
+    def initial_vorticity(self, real_t):
+        rng = np.random.default_rng(42)
+        shape = self.grid if self.dim == 2 else (3, *self.grid)
+        return (1e-3 * rng.standard_normal(shape)).astype(real_t)
+
+
+def make_workload(name: str) -> Workload:
+    if name == "rod128":
+        length = 0.3
+        return Workload(
+            name, "3D unbounded vorticity NS 128^3 fp32 (256^3 doubled FFT), one clamped rod (64 elements, "
+                  "element-centric cosine-delta forcing), U=1 inflow, Re=100 on rod length, CFL 0.1",
+            (128, 128, 128), 1.0 * length / 100.0, np.array([1.0, 0.0, 0.0]), "rods",
+            bodies=[dict(base=(0.5, 0.5, 0.5 - length / 2), length=length, radius=0.01, n_elem=64)],
+            K=-2e4, C=-1e2)
+    if name == "cylinder2d":
+        return Workload(
+            name, "2D unbounded vorticity NS 256x512 fp32, cylinder D=0.1 at (0.25, 0.25), 96 markers, "
+                  "U=1, Re=200 on the diameter, CFL 0.1",
+            (256, 512), 1.0 * 0.1 / 200.0, np.array([1.0, 0.0]), "cylinder",
+            bodies=[dict(centre=(0.25, 0.25, 0.0), radius=0.05)], K=-5e4, C=-20.0, n_markers=96)
+    if name == "carpet256":
+        n = 256
+        dx = 1.0 / n
+        length = 0.2
+        bodies = []
+        for i in range(4):
+            for j in range(4):
+                bodies.append(dict(base=(0.3 + 0.13 * i, 0.3 + 0.13 * j, 6 * dx), length=length,
+                                   radius=0.005, n_elem=100))
+        return Workload(
+            name, "3D unbounded vorticity NS 256^3 fp32 (512^3 doubled FFT), 4x4 carpet of 16 clamped rods "
+                  "(100 elements each, one interactor per rod), U=1 along x, Re=500 on rod length, CFL 0.1",
+            (n, n, n), 1.0 * length / 500.0, np.array([1.0, 0.0, 0.0]), "rods", bodies=bodies, K=-2e4, C=-1e2)
+    raise ValueError(f"unknown workload {name}")
 
 
 # ------------------------------------------------------------------ clocks
@@ -133,45 +189,57 @@ class ClockSampler:
 # ---------------------------------------------------------------- GPU arm
 
 
-def make_gpu_case(real_t, device):
+def make_gpu_case(wl: Workload, real_t, device):
     import torch
 
     import sopht_gb300.simulator as sps
 
-    sim = sps.UnboundedNavierStokesFlowSimulator3D(
-        grid_size=GRID, x_range=X_RANGE, kinematic_viscosity=NU, cfl=CFL, real_t=real_t, with_forcing=True,
-        with_free_stream_flow=True, device=device)
-    sim.vorticity_field.copy_(torch.from_numpy(initial_vorticity(real_t)).to(device))
-    rod = RodState()
-    inter = sps.CosseratRodFlowInteraction(
-        cosserat_rod=rod, eul_grid_forcing_field=sim.eul_grid_forcing_field,
-        eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=K_STIFF,
-        virtual_boundary_damping_coeff=C_DAMP, dx=sim.dx, grid_dim=3, real_t=real_t,
-        forcing_grid_cls=sps.CosseratRodElementCentricForcingGrid)
-    return sim, inter
+    Sim = sps.UnboundedNavierStokesFlowSimulator2D if wl.dim == 2 else sps.UnboundedNavierStokesFlowSimulator3D
+    sim = Sim(grid_size=wl.grid, x_range=wl.x_range, kinematic_viscosity=wl.nu, cfl=wl.cfl, real_t=real_t,
+              with_forcing=True, with_free_stream_flow=True, device=device)
+    sim.vorticity_field.copy_(torch.from_numpy(wl.initial_vorticity(real_t)).to(device))
+    inters = []
+    for b in wl.bodies:
+        if wl.kind == "cylinder":
+            cyl = sps.Cylinder(b["centre"], base_radius=b["radius"])
+            inters.append(sps.RigidBodyFlowInteraction(
+                rigid_body=cyl, eul_grid_forcing_field=sim.eul_grid_forcing_field,
+                eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=wl.K,
+                virtual_boundary_damping_coeff=wl.C, dx=sim.dx, grid_dim=2, real_t=real_t,
+                forcing_grid_cls=sps.CircularCylinderForcingGrid, num_forcing_points=wl.n_markers))
+        else:
+            rod = RodState(b["base"], b["length"], b["radius"], b["n_elem"])
+            inters.append(sps.CosseratRodFlowInteraction(
+                cosserat_rod=rod, eul_grid_forcing_field=sim.eul_grid_forcing_field,
+                eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=wl.K,
+                virtual_boundary_damping_coeff=wl.C, dx=sim.dx, grid_dim=3, real_t=real_t,
+                forcing_grid_cls=sps.CosseratRodElementCentricForcingGrid))
+    return sim, inters
 
 
-def public_api_step(sim, inter):
-    """One coupled step through the drop-in API (flow_past_rod_case.py:231-250 order)."""
+def public_api_step(wl, sim, inters):
+    """One coupled step through the drop-in API (the reference example loops' order)."""
     dt = sim.compute_stable_timestep()
-    inter.time_step(dt=dt)
-    inter()
-    sim.time_step(dt=dt, free_stream_velocity=U_INF)
-    return inter.lag_grid_forcing_host()
+    for inter in inters:
+        inter.time_step(dt=dt)
+        inter()
+    sim.time_step(dt=dt, free_stream_velocity=wl.u_inf)
+    return [inter.lag_grid_forcing_host() for inter in inters]
 
 
-def device_step(sim, inter, events=None):
+def device_step(wl, sim, inters, events=None):
     """The same step with dt on the device (capturable)."""
     from sopht_gb300 import _lib
-    dsc = sim.device_stable_timestep(free_stream_velocity=U_INF, recompute_max=False)
-    inter.device_call(dsc)
+    dsc = sim.device_stable_timestep(free_stream_velocity=wl.u_inf, recompute_max=False)
+    for inter in inters:
+        inter.device_call(dsc)
     if events is not None:
-        arr = (__import__("ctypes").c_void_p * len(events))(*[e.cuda_event for e in events])
+        arr = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
         _lib.call("sg_flow_set_timing_events", sim._plan, len(events), arr)
     sim.time_step_device(dsc)
 
 
-def run_gpu(args, rank, world):
+def run_gpu(args, wl: Workload, rank, world):
     import torch
 
     from sopht_gb300.build import build
@@ -181,21 +249,21 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     rt = np.float32
-    sim, inter = make_gpu_case(rt, device)
-    inter.upload_kinematics()
-    # initial max |u| for the first device dt
-    sim.device_stable_timestep(free_stream_velocity=U_INF, recompute_max=True)
+    sim, inters = make_gpu_case(wl, rt, device)
+    for inter in inters:
+        inter.upload_kinematics()
+    sim.device_stable_timestep(free_stream_velocity=wl.u_inf, recompute_max=True)
     stream = torch.cuda.Stream(device)
     torch.cuda.synchronize()
-    # warm-up (also compiles nothing: kernels are AOT) and graph capture of S steps
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            device_step(sim, inter)
+            device_step(wl, sim, inters)
     torch.cuda.synchronize()
     seg = min(args.steps, 25)
     n_seg = max(1, args.steps // seg)
     steps = seg * n_seg
-    n_ev = len(PASS_NAMES) + 1
+    pass_names = list(wl.passes)
+    n_ev = len(pass_names) + 1
     events = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ev)] for _ in range(seg)]
     with torch.cuda.stream(stream):
         for ev_list in events:  # torch creates the CUDA events lazily, on first record
@@ -207,7 +275,7 @@ def run_gpu(args, rank, world):
         stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.graph(graph, stream=stream):
             for k in range(seg):
-                device_step(sim, inter, events[k])
+                device_step(wl, sim, inters, events[k])
     torch.cuda.synchronize()
     graph.replay()  # one untimed replay after capture
     torch.cuda.synchronize()
@@ -229,80 +297,78 @@ def run_gpu(args, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed_ms = float(t.item())
         torch.distributed.barrier()
-    # per-pass durations from the last replay
-    per_pass = {name: [] for name in PASS_NAMES}
-    for k in range(seg):
-        for i, name in enumerate(PASS_NAMES):
-            per_pass[name].append(events[k][i].elapsed_time(events[k][i + 1]))
-    cells = int(np.prod(GRID))
+    cells = wl.cells
     kernels = {}
-    for name, vals in per_pass.items():
+    for i, name in enumerate(pass_names):
+        vals = [events[k][i].elapsed_time(events[k][i + 1]) for k in range(seg)]
         ms = float(np.mean(vals))
-        kernels[name] = {"ms": round(ms, 5), "GB_s": round(PASS_BYTES[name] * cells / (ms * 1e-3) / 1e9, 1),
+        kernels[name] = {"ms": round(ms, 5), "GB_s": round(wl.passes[name] * cells / (ms * 1e-3) / 1e9, 1),
                          "launches_timed": len(vals)}
     value = world * steps / (elapsed_ms * 1e-3)
+    graph.reset()
+    del graph
 
     # end to end through the public API: host dt, H2D marker kinematics, D2H forcing
-    sim_e, inter_e = make_gpu_case(rt, device)
+    sim_e, inters_e = make_gpu_case(wl, rt, device)
     for _ in range(args.warmup):
-        public_api_step(sim_e, inter_e)
+        public_api_step(wl, sim_e, inters_e)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    e2e_steps = steps
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        public_api_step(sim_e, inter_e)
+    for _ in range(steps):
+        public_api_step(wl, sim_e, inters_e)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], device=device)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
-    n_lag = inter_e.num_lag_nodes
-    h2d = 2 * 3 * n_lag * 8
-    d2h = 3 * n_lag * 4 + 8
+    n_lag = sum(inter.num_lag_nodes for inter in inters_e)
+    h2d = 2 * wl.dim * n_lag * 8
+    d2h = wl.dim * n_lag * 4 + 8
+    del sim_e, inters_e
 
     accuracy = None
     if rank == 0 and not args.skip_accuracy:
-        accuracy = accuracy_vs_fp64(args, device, min(steps, args.accuracy_steps))
+        accuracy = accuracy_vs_fp64(wl, device, min(steps, args.accuracy_steps))
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = run_cpu_sample(args.cpu_seconds)
+        cpu = run_cpu_sample(wl, args.cpu_seconds)
     if rank != 0:
         return
     top = max(kernels, key=lambda k: kernels[k]["ms"])
-    peaks = load_peaks()
-    hbm = peaks.get("hbm_gbs")
-    algo = PASS_BYTES[top] * cells
+    hbm = load_peaks().get("hbm_gbs")
+    peak = hbm or 6800.0
+    algo = wl.passes[top] * cells
     achieved = algo / (kernels[top]["ms"] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 3) if hbm else None,
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 3),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "fallback 6800 GB/s",
-                "traffic": traffic_from_profiles(top), "algorithmic_bytes_per_launch": algo}
-    if not hbm:
-        roofline["peak"] = 6800.0
-        roofline["frac"] = round(achieved / 6800.0, 3)
+                "traffic": traffic_from_profiles(wl.name, top), "algorithmic_bytes_per_launch": algo}
     step_ms = elapsed_ms / steps
-    step_bytes = sum(PASS_BYTES.values()) * cells
+    step_bytes = sum(wl.passes.values()) * cells
+    launches_per_step = 1 + 2 * len(inters) + (9 if wl.dim == 3 else 5)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "flow steps/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "gcell_updates_per_s": round(world * cells * steps / (elapsed_ms * 1e-3) / 1e9, 3),
-        "config": {"workload": WORKLOAD, "grid": list(GRID), "dt_rule": "compute_stable_timestep, CFL 0.1",
-                   "rod": "rigid clamped stand-in, host-side; rod integrator not timed", "parallelism":
-                   "replicas only" if world > 1 else "single GPU",
-                   "l2": "no flush: step working set ~250 MB > 126 MB L2"},
+        "config": {"workload": wl.description, "name": wl.name, "grid": list(wl.grid),
+                   "dt_rule": "compute_stable_timestep, CFL 0.1", "bodies": len(wl.bodies),
+                   "body_kinematics": "clamped/fixed pose on the host; body integrator not timed",
+                   "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "l2": "no flush: the step working set exceeds the 126 MB L2" if cells * 4 * 20 > 126e6 else
+                         "working set fits in L2 (launch-latency-bound size)"},
         "roofline": roofline,
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
                           "achieved_GB_s": round(step_bytes / (step_ms * 1e-3) / 1e9, 1),
-                          "frac": round(step_bytes / (step_ms * 1e-3) / 1e9 / (hbm or 6800.0), 3)},
+                          "frac": round(step_bytes / (step_ms * 1e-3) / 1e9 / peak, 3)},
         "kernels": kernels,
-        "e2e": {"value": round(world * e2e_steps / e2e_s, 2), "unit": "flow steps/s",
+        "e2e": {"value": round(world * steps / e2e_s, 2), "unit": "flow steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "public API per step: host dt (sync), H2D marker positions+velocities, D2H lag forcing"},
-        "gpu_launches": 12 * steps,
+        "gpu_launches": launches_per_step * steps,
         "clocks": clock_info,
         "accuracy": accuracy,
         "cpu_baseline": cpu,
@@ -310,21 +376,22 @@ def run_gpu(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def accuracy_vs_fp64(args, device, steps):
+def accuracy_vs_fp64(wl, device, steps):
     """Relative L2 of the fp32 GPU path against the same path in fp64 after `steps` steps."""
     import torch
-    res = {}
     fields = {}
     for rt in (np.float32, np.float64):
-        sim, inter = make_gpu_case(rt, device)
+        sim, inters = make_gpu_case(wl, rt, device)
         for _ in range(steps):
             dt = sim.compute_stable_timestep()
-            inter.time_step(dt=dt)
-            inter()
-            sim.time_step(dt=dt, free_stream_velocity=U_INF)
+            for inter in inters:
+                inter.time_step(dt=dt)
+                inter()
+            sim.time_step(dt=dt, free_stream_velocity=wl.u_inf)
         torch.cuda.synchronize()
         fields[rt] = (sim.vorticity_field.double().cpu().numpy(), sim.velocity_field.double().cpu().numpy())
-        del sim, inter
+        del sim, inters
+    res = {}
     for i, name in enumerate(("vorticity", "velocity")):
         a, b = fields[np.float32][i], fields[np.float64][i]
         res[f"{name}_rel_l2_vs_fp64"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
@@ -343,12 +410,12 @@ def load_peaks():
     return {}
 
 
-def traffic_from_profiles(kernel):
+def traffic_from_profiles(workload, kernel):
     """DRAM bytes per launch recorded by the committed ncu summary, if any."""
     p = ROOT / "profiles" / "traffic.json"
     if p.exists():
         try:
-            return json.loads(p.read_text()).get(kernel)
+            return json.loads(p.read_text()).get(workload, {}).get(kernel)
         except Exception:
             return None
     return None
@@ -357,54 +424,68 @@ def traffic_from_profiles(kernel):
 # ------------------------------------------------------------ CPU (oracle)
 
 
-def make_cpu_case():
-    from oracle.flow import ImmersedBodyInteractionOracle, NavierStokes3DOracle, RodElementCentricGridOracle
+def make_cpu_case(wl: Workload):
+    from oracle.flow import (
+        CircularCylinderOracle,
+        ImmersedBodyInteractionOracle,
+        NavierStokes2DOracle,
+        NavierStokes3DOracle,
+        RodElementCentricGridOracle,
+    )
     rt = np.float32
-    sim = NavierStokes3DOracle(GRID, X_RANGE, NU, cfl=CFL, real_t=rt, with_forcing=True,
-                               with_free_stream_flow=True)
-    sim.vorticity_field[...] = initial_vorticity(rt)
-    rod = RodState()
-    grid = RodElementCentricGridOracle(rod)
-    inter = ImmersedBodyInteractionOracle(sim.eul_grid_forcing_field, sim.velocity_field,
-                                          np.zeros((3, N_ELEM + 1)), np.zeros((3, N_ELEM)), grid, K_STIFF,
-                                          C_DAMP, sim.dx, 3, real_t=rt)
-    return sim, inter
+    Sim = NavierStokes2DOracle if wl.dim == 2 else NavierStokes3DOracle
+    sim = Sim(wl.grid, wl.x_range, wl.nu, cfl=wl.cfl, real_t=rt, with_forcing=True, with_free_stream_flow=True)
+    sim.vorticity_field[...] = wl.initial_vorticity(rt)
+    inters = []
+    for b in wl.bodies:
+        if wl.kind == "cylinder":
+            grid = CircularCylinderOracle(b["centre"], b["radius"], wl.n_markers)
+            forces, torques = np.zeros((3, 1)), np.zeros((3, 1))
+        else:
+            rod = RodState(b["base"], b["length"], b["radius"], b["n_elem"])
+            grid = RodElementCentricGridOracle(rod)
+            forces, torques = np.zeros((3, rod.n_elems + 1)), np.zeros((3, rod.n_elems))
+        inters.append(ImmersedBodyInteractionOracle(sim.eul_grid_forcing_field, sim.velocity_field, forces,
+                                                    torques, grid, wl.K, wl.C, sim.dx, wl.dim, real_t=rt))
+    return sim, inters
 
 
-def cpu_step(sim, inter):
+def cpu_step(wl, sim, inters):
     dt = sim.compute_stable_timestep()
-    inter.time_step(dt)
-    inter()
-    sim.time_step(dt, U_INF)
+    for inter in inters:
+        inter.time_step(dt)
+        inter()
+    sim.time_step(dt, wl.u_inf)
 
 
-def run_cpu_sample(seconds, max_steps=None):
-    sim, inter = make_cpu_case()
-    cpu_step(sim, inter)  # warm-up (plans, caches)
+def run_cpu_sample(wl, seconds, max_steps=None):
+    sim, inters = make_cpu_case(wl)
+    cpu_step(wl, sim, inters)  # warm-up (plans, caches)
     n = 0
     t0 = time.perf_counter()
     while True:
-        cpu_step(sim, inter)
+        cpu_step(wl, sim, inters)
         n += 1
         el = time.perf_counter() - t0
         if el >= seconds or (max_steps and n >= max_steps):
             break
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     return {"value": round(n / el, 4), "unit": "flow steps/s", "cores": cores, "kind": "port",
-            "sample": f"{n} coupled steps of the same 128^3 workload after 1 warm-up step ({el:.1f} s), "
+            "sample": f"{n} coupled steps of the same workload ({wl.name}) after 1 warm-up step ({el:.1f} s), "
                       "numpy + scipy.fft with workers = all cores, fp32"}
 
 
-def run_reference(args, rank, world):
+def run_reference(args, wl, rank, world):
     if rank != 0:
         return
     budget = max(10.0, min(180.0, float(args.cpu_seconds) * 4))
-    cpu = run_cpu_sample(budget, max_steps=args.steps)
+    cpu = run_cpu_sample(wl, budget, max_steps=args.steps)
     out = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "flow steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "ms_per_step": round(1e3 / cpu["value"], 2),
-           "config": {"workload": WORKLOAD, "grid": list(GRID), "dt_rule": "compute_stable_timestep, CFL 0.1"},
+           "config": {"workload": wl.description, "name": wl.name, "grid": list(wl.grid),
+                      "dt_rule": "compute_stable_timestep, CFL 0.1"},
            "cpu_baseline": cpu,
            "e2e": {"value": cpu["value"], "unit": "flow steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "the reference's pystencils/pyfftw/numba stack is not installable offline; its algorithm runs "
@@ -418,12 +499,14 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="rod128", choices=["rod128", "cylinder2d", "carpet256"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    wl = make_workload(args.workload)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
@@ -432,9 +515,9 @@ def main():
         torch.distributed.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     try:
         if args.impl == "reference":
-            run_reference(args, rank, world)
+            run_reference(args, wl, rank, world)
         else:
-            run_gpu(args, rank, world)
+            run_gpu(args, wl, rank, world)
     finally:
         if world > 1:
             import torch
