@@ -1,14 +1,21 @@
-// Size-specialised FFT kernels (compile-time length N) for the common extents.
+// Size-specialised FFT kernels (compile-time length N and lines per block W).
 //
-// Same passes and parameter structs as fft.cuh, but every transform length,
-// radix schedule, stride and butterfly count is a compile-time constant, so
-// index arithmetic folds away and all loops unroll.  Layout in shared memory
-// is point-major / line-minor with an odd line pitch LS = W + 1 (in complex
-// elements): consecutive threads of a stage touch consecutive lines, and the
-// row kernels' coalesced loads (consecutive points of one row) hit distinct
-// banks.  Each stage is in place: a thread reads its E = N W / NT elements into
-// registers, the block synchronises, and the thread writes its butterfly
-// outputs back -- one buffer, so twice the resident blocks of a ping-pong.
+// Same passes and parameter structs as fft.cuh, but the transform length, the
+// radix schedule, strides and butterfly counts are compile-time constants, so
+// index arithmetic folds away and all loops unroll.
+//  * Shared layout: point-major / line-minor with an odd line pitch LS = W + 1
+//    (in complex elements).  Consecutive threads of a stage touch consecutive
+//    lines, and the row kernels' coalesced loads (consecutive points of one
+//    row) hit distinct banks.
+//  * Stages are in place: a thread reads its E = N W / NT elements into
+//    registers, the block synchronises, and the thread writes its butterfly
+//    outputs back (one buffer instead of a ping-pong pair).
+//  * Twiddles are staged into shared memory once per block.
+//  * Per-row metadata of the row kernels (global offsets, boundary factors) is
+//    computed once per block, not per element.
+//  * Each length has a wide shape (16 lines, 128-byte runs for the strided
+//    passes) and a narrow one (1-8 lines) chosen when the wide shape would not
+//    give every SM at least two blocks.
 #pragma once
 
 #include "fft.cuh"
@@ -32,37 +39,35 @@ __host__ __device__ constexpr int sched_radix(int n, int s) {
     while (n % 3 == 0) { if (c++ == s) return 3; n /= 3; }
     return 1;
 }
-__host__ __device__ constexpr int sched_ns(int n, int s) {
-    int p = 1;
-    for (int i = 0; i < s; ++i) p *= sched_radix(n, i);
-    return p;
-}
 
-// Per-length launch shape: W lines per block, NT threads, E elements per thread.
-template <int N> struct FastShape;
-#define SG_FAST_SHAPE(NN, WW, NTT)                                          \
-    template <> struct FastShape<NN> {                                     \
-        static constexpr int W = WW, NT = NTT, E = NN * WW / NTT, LS = WW + 1; \
-    };
-SG_FAST_SHAPE(64, 32, 128)
-SG_FAST_SHAPE(128, 16, 128)
-SG_FAST_SHAPE(256, 16, 256)
-SG_FAST_SHAPE(512, 16, 512)
-SG_FAST_SHAPE(1024, 8, 512)
-SG_FAST_SHAPE(192, 16, 128)
-SG_FAST_SHAPE(384, 16, 256)
-SG_FAST_SHAPE(768, 8, 256)
-#undef SG_FAST_SHAPE
+// E complex elements per thread: a multiple of every radix of the schedule
+template <int N> struct FastElems {
+    static constexpr int E = (N % 3 == 0) ? 24 : 16;
+};
 
-inline bool fast_length(int n) {
-    switch (n) {
-        case 64: case 128: case 256: case 512: case 1024: case 192: case 384: case 768: return true;
-        default: return false;
-    }
-}
+template <int N, int W> struct FastShape {
+    static constexpr int E = FastElems<N>::E;
+    static constexpr int NT = N * W / E;
+    static constexpr int LS = W + 1;
+    static_assert(NT >= 32 && NT <= 1024 && NT % 32 == 0, "block size must be whole warps");
+};
+
+// wide / narrow line counts per length
+template <int N> struct FastWidth;
+#define SG_FAST_WIDTH(NN, WIDE, NARROW) \
+    template <> struct FastWidth<NN> { static constexpr int wide = WIDE, narrow = NARROW; };
+SG_FAST_WIDTH(64, 32, 8)
+SG_FAST_WIDTH(128, 16, 4)
+SG_FAST_WIDTH(256, 16, 2)
+SG_FAST_WIDTH(512, 16, 2)
+SG_FAST_WIDTH(1024, 8, 1)
+SG_FAST_WIDTH(192, 16, 4)
+SG_FAST_WIDTH(384, 16, 2)
+SG_FAST_WIDTH(768, 8, 1)
+#undef SG_FAST_WIDTH
 
 template <int N, int S, int NS, bool INV, int W, int LS, int NT, typename C>
-__device__ __forceinline__ void fast_stage(C* buf, const C* __restrict__ tw, int tid) {
+__device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid) {
     constexpr int R = sched_radix(N, S);
     constexpr int NB = N / R;
     constexpr int TOT = NB * W;
@@ -100,7 +105,7 @@ __device__ __forceinline__ void fast_stage(C* buf, const C* __restrict__ tw, int
 }
 
 template <int N, int S, int NS, bool INV, int W, int LS, int NT, typename C>
-__device__ __forceinline__ void fast_stages(C* buf, const C* __restrict__ tw, int tid) {
+__device__ __forceinline__ void fast_stages(C* buf, const C* tw, int tid) {
     if constexpr (S < sched_count(N)) {
         fast_stage<N, S, NS, INV, W, LS, NT>(buf, tw, tid);
         fast_stages<N, S + 1, NS * sched_radix(N, S), INV, W, LS, NT>(buf, tw, tid);
@@ -108,27 +113,33 @@ __device__ __forceinline__ void fast_stages(C* buf, const C* __restrict__ tw, in
 }
 
 // Whole in-place transform of the W lines in `buf` (ends synchronised).
-template <int N, bool INV, typename C>
-__device__ __forceinline__ void fast_fft(C* buf, const C* __restrict__ tw, int tid) {
-    using S = FastShape<N>;
-    fast_stages<N, 0, 1, INV, S::W, S::LS, S::NT>(buf, tw, tid);
+template <int N, int W, bool INV, typename C>
+__device__ __forceinline__ void fast_fft(C* buf, const C* tw, int tid) {
+    using S = FastShape<N, W>;
+    fast_stages<N, 0, 1, INV, W, S::LS, S::NT>(buf, tw, tid);
+}
+
+template <typename C>
+__device__ __forceinline__ void stage_table(C* dst, const C* __restrict__ src, int n, int tid, int nt) {
+    for (int i = tid; i < n; i += nt) dst[i] = src[i];
 }
 
 // ----------------------------------------------------------- strided lines
-template <typename T, int N, int MODE>
-__global__ void __launch_bounds__(FastShape<N>::NT) fast_lines_kernel(LinesParams<T> p) {
+template <typename T, int N, int W, int MODE>
+__global__ void __launch_bounds__(FastShape<N, W>::NT) fast_lines_kernel(LinesParams<T> p) {
     using C = cplx_t<T>;
-    using S = FastShape<N>;
-    constexpr int W = S::W, LS = S::LS, NT = S::NT;
+    using S = FastShape<N, W>;
+    constexpr int LS = S::LS, NT = S::NT, PER = N * W / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
+    C* tw = buf + N * LS;
     const int tid = threadIdx.x;
     const int chunks = (p.inner + W - 1) / W;
     const int outer = blockIdx.x / chunks;
     const int c0 = (blockIdx.x % chunks) * W;
     const int wcount = min(W, p.inner - c0);
+    stage_table(tw, p.tw, N, tid, NT);
     const C* src = p.in + (int64_t)outer * p.outer_stride + c0;
-    constexpr int PER = N * W / NT;
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int e = tid + b * NT;
@@ -139,20 +150,31 @@ __global__ void __launch_bounds__(FastShape<N>::NT) fast_lines_kernel(LinesParam
     }
     __syncthreads();
     if (MODE == LINE_INV) {
-        fast_fft<N, true>(buf, p.tw, tid);
+        fast_fft<N, W, true>(buf, tw, tid);
     } else {
-        fast_fft<N, false>(buf, p.tw, tid);
+        fast_fft<N, W, false>(buf, tw, tid);
         if (MODE == LINE_CONV) {
+            // every element a thread touches has the same line w, so the table
+            // row of that line is computed once
+            const int w = tid % W;
+            const int k0 = tid / W;
+            int64_t gbase = 0;
+            if (w < wcount) {
+                const int inner = c0 + w;
+                const int m = inner / p.g.inner_div;
+                const int kx = inner - m * p.g.inner_div;
+                const int ms = p.g.m_mod > 0 ? min(m, p.g.m_mod - m) : 0;
+                gbase = (int64_t)ms * p.g.m_stride + kx;
+            }
 #pragma unroll
             for (int b = 0; b < PER; ++b) {
-                const int e = tid + b * NT;
-                const int k = e / W, w = e % W;
+                const int k = k0 + b * (NT / W);
                 const int ks = min(k, N - k);
-                const T gv = (w < wcount) ? p.g.at(ks, c0 + w) : T(0);
+                const T gv = (w < wcount) ? p.g.table[(int64_t)ks * p.g.k_stride + gbase] : T(0);
                 buf[k * LS + w] = cscale(buf[k * LS + w], gv);
             }
             __syncthreads();
-            fast_fft<N, true>(buf, p.tw, tid);
+            fast_fft<N, W, true>(buf, tw, tid);
         }
     }
     C* dst = p.out + (int64_t)outer * p.outer_stride + c0;
@@ -166,77 +188,105 @@ __global__ void __launch_bounds__(FastShape<N>::NT) fast_lines_kernel(LinesParam
 
 // -------------------------------------------------------------- row kernels
 // Rows of the x axis: W rows per block, element (row r, point n) at buf[n*LS + r].
+// Shared: buf [M][LS], twiddles tw_m [M] and tw_l [M + 1], row offsets [2 W].
 
-template <typename T, int M>
-__device__ __forceinline__ void r2c_post_store(const cplx_t<T>* buf, const cplx_t<T>* __restrict__ tw_l,
-                                               cplx_t<T>* out, const RowMap& map, int row0, int n_rows,
-                                               int tid) {
+template <int M, int W> struct RowSmem {
+    static constexpr int LS = W + 1;
+    template <typename C> static constexpr size_t bytes() {
+        return sizeof(C) * ((size_t)M * LS + M + (M + 1)) + sizeof(int64_t) * 2 * W + 16;
+    }
+};
+
+template <typename T, int M, int W>
+__device__ __forceinline__ void r2c_post_store(const cplx_t<T>* buf, const cplx_t<T>* tw_l, cplx_t<T>* out,
+                                               const int64_t* out_off, int row0, int n_rows, int tid) {
     using C = cplx_t<T>;
-    using S = FastShape<M>;
-    constexpr int W = S::W, LS = S::LS, NT = S::NT;
+    using S = FastShape<M, W>;
+    constexpr int LS = S::LS, NT = S::NT;
     // each row emits M + 1 bins; threads walk bins of one row (coalesced store)
     for (int e = tid; e < W * (M + 1); e += NT) {
-        const int r = e / (M + 1), k = e % (M + 1);
-        const int q = row0 + r;
-        if (q >= n_rows) continue;
+        const int r = e / (M + 1), k = e - r * (M + 1);
+        if (row0 + r >= n_rows) continue;
         const C zk = buf[(k == M ? 0 : k) * LS + r];
         const C zc = cconj(buf[(k == 0 ? 0 : M - k) * LS + r]);
         const C w = tw_l[k];
         const C s = cadd(zk, zc);
         const C wd = cmul(w, csub(zk, zc));
-        out[map.offset(q) + k] = cmake<C>(T(0.5) * (s.x + wd.y), T(0.5) * (s.y - wd.x));
+        out[out_off[r] + k] = cmake<C>(T(0.5) * (s.x + wd.y), T(0.5) * (s.y - wd.x));
     }
 }
 
-template <typename T, int M>
-__global__ void __launch_bounds__(FastShape<M>::NT) fast_rows_r2c_kernel(RowsR2CParams<T> p) {
+template <typename T, int M, int W>
+__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_r2c_kernel(RowsR2CParams<T> p) {
     using C = cplx_t<T>;
-    using S = FastShape<M>;
-    constexpr int W = S::W, LS = S::LS, NT = S::NT, PER = M * W / NT;
+    using S = FastShape<M, W>;
+    constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
+    C* tw_m = buf + M * LS;
+    C* tw_l = tw_m + M;
+    int64_t* in_off = reinterpret_cast<int64_t*>(
+        (reinterpret_cast<uintptr_t>(tw_l + M + 1) + 15) & ~uintptr_t(15));
+    int64_t* out_off = in_off + W;
     const int tid = threadIdx.x;
     const int row0 = blockIdx.x * W;
+    if (tid < W) {
+        in_off[tid] = p.in_map.offset(row0 + tid);
+        out_off[tid] = p.out_map.offset(row0 + tid);
+    }
+    stage_table(tw_m, p.tw_m, M, tid, NT);
+    stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    __syncthreads();
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int e = tid + b * NT;
         const int r = e / M, n = e % M;
-        const int q = row0 + r;
         C z = cmake<C>(T(0), T(0));
-        if (q < p.n_rows) {
-            const T* src = p.in + p.in_map.offset(q);
+        if (row0 + r < p.n_rows) {
+            const T* src = p.in + in_off[r];
             if (2 * n + 1 < p.n_in) z = *reinterpret_cast<const C*>(src + 2 * n);
             else if (2 * n < p.n_in) z.x = src[2 * n];
         }
         buf[n * LS + r] = z;
     }
     __syncthreads();
-    fast_fft<M, false>(buf, p.tw_m, tid);
-    r2c_post_store<T, M>(buf, p.tw_l, p.out, p.out_map, row0, p.n_rows, tid);
+    fast_fft<M, W, false>(buf, tw_m, tid);
+    r2c_post_store<T, M, W>(buf, tw_l, p.out, out_off, row0, p.n_rows, tid);
 }
 
-template <typename T, int M>
-__global__ void __launch_bounds__(FastShape<M>::NT) fast_rows_c2r_kernel(RowsC2RParams<T> p) {
+template <typename T, int M, int W>
+__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_c2r_kernel(RowsC2RParams<T> p) {
     using C = cplx_t<T>;
-    using S = FastShape<M>;
-    constexpr int W = S::W, LS = S::LS, NT = S::NT, PER = M * W / NT;
+    using S = FastShape<M, W>;
+    constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
+    C* tw_m = buf + M * LS;
+    C* tw_l = tw_m + M;
+    int64_t* in_off = reinterpret_cast<int64_t*>(
+        (reinterpret_cast<uintptr_t>(tw_l + M + 1) + 15) & ~uintptr_t(15));
+    int64_t* out_off = in_off + W;
     const int tid = threadIdx.x;
     const int row0 = blockIdx.x * W;
+    if (tid < W) {
+        in_off[tid] = p.in_map.offset(row0 + tid);
+        out_off[tid] = p.out_map.offset(row0 + tid);
+    }
+    stage_table(tw_m, p.tw_m, M, tid, NT);
+    stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    __syncthreads();
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int e = tid + b * NT;
         const int r = e / M, k = e % M;
-        const int q = row0 + r;
         C Zk = cmake<C>(T(0), T(0));
-        if (q < p.n_rows) {
-            const C* src = p.in + p.in_map.offset(q);
+        if (row0 + r < p.n_rows) {
+            const C* src = p.in + in_off[r];
             C xk = src[k];
             C xm = src[M - k];
             if (k == 0) { xk.y = T(0); xm.y = T(0); }
             const C xc = cconj(xm);
-            C w = p.tw_l[k];
+            C w = tw_l[k];
             w.y = -w.y;
             const C s = cadd(xk, xc);
             const C wd = cmul(w, csub(xk, xc));
@@ -245,70 +295,74 @@ __global__ void __launch_bounds__(FastShape<M>::NT) fast_rows_c2r_kernel(RowsC2R
         buf[k * LS + r] = Zk;
     }
     __syncthreads();
-    fast_fft<M, true>(buf, p.tw_m, tid);
+    fast_fft<M, W, true>(buf, tw_m, tid);
     // n_out real points = n_out/2 complex values per row (n_out even)
     const int half = p.n_out >> 1;
     for (int e = tid; e < W * half; e += NT) {
-        const int r = e / half, n = e % half;
-        const int q = row0 + r;
-        if (q >= p.n_rows) continue;
-        *reinterpret_cast<C*>(p.out + p.out_map.offset(q) + 2 * n) = buf[n * LS + r];
+        const int r = e / half, n = e - r * half;
+        if (row0 + r >= p.n_rows) continue;
+        *reinterpret_cast<C*>(p.out + out_off[r] + 2 * n) = buf[n * LS + r];
     }
 }
 
 // ------------------------------------------------------------- dispatch
-template <int N> inline size_t fast_smem_bytes(int esz) { return (size_t)N * FastShape<N>::LS * esz; }
+inline int fast_pick_width(long long units, int wide, int narrow) {
+    // the wide shape when it still gives every SM two blocks, else the narrow one
+    return (units + wide - 1) / wide >= 2 * 152 ? wide : narrow;
+}
 
-template <typename T, int N>
+template <typename T, int N, int W>
 int launch_fast_rows_r2c(const RowsR2CParams<T>& p, cudaStream_t stream) {
-    const size_t smem = fast_smem_bytes<N>(sizeof(cplx_t<T>));
-    auto kern = fast_rows_r2c_kernel<T, N>;
+    const size_t smem = RowSmem<N, W>::template bytes<cplx_t<T>>();
+    auto kern = fast_rows_r2c_kernel<T, N, W>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast rows_r2c smem attribute"));
-    kern<<<ceil_div(p.n_rows, FastShape<N>::W), FastShape<N>::NT, smem, stream>>>(p);
+    kern<<<ceil_div(p.n_rows, W), FastShape<N, W>::NT, smem, stream>>>(p);
     return launch_status("fast rows_r2c");
 }
 
-template <typename T, int N>
+template <typename T, int N, int W>
 int launch_fast_rows_c2r(const RowsC2RParams<T>& p, cudaStream_t stream) {
-    const size_t smem = fast_smem_bytes<N>(sizeof(cplx_t<T>));
-    auto kern = fast_rows_c2r_kernel<T, N>;
+    const size_t smem = RowSmem<N, W>::template bytes<cplx_t<T>>();
+    auto kern = fast_rows_c2r_kernel<T, N, W>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast rows_c2r smem attribute"));
-    kern<<<ceil_div(p.n_rows, FastShape<N>::W), FastShape<N>::NT, smem, stream>>>(p);
+    kern<<<ceil_div(p.n_rows, W), FastShape<N, W>::NT, smem, stream>>>(p);
     return launch_status("fast rows_c2r");
 }
 
-template <typename T, int N, int MODE>
+template <typename T, int N, int W, int MODE>
 int launch_fast_lines(LinesParams<T> p, cudaStream_t stream) {
-    const size_t smem = fast_smem_bytes<N>(sizeof(cplx_t<T>));
-    auto kern = fast_lines_kernel<T, N, MODE>;
+    const size_t smem = sizeof(cplx_t<T>) * ((size_t)N * FastShape<N, W>::LS + N);
+    auto kern = fast_lines_kernel<T, N, W, MODE>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast lines smem attribute"));
-    p.W = FastShape<N>::W;
-    const long long blocks = (long long)p.n_outer * ((p.inner + p.W - 1) / p.W);
+    p.W = W;
+    const long long blocks = (long long)p.n_outer * ((p.inner + W - 1) / W);
     SG_REQUIRE(blocks < (1LL << 31), SG_ERR_SHAPE, "lines: too many blocks (%lld)", blocks);
-    kern<<<(unsigned)blocks, FastShape<N>::NT, smem, stream>>>(p);
+    kern<<<(unsigned)blocks, FastShape<N, W>::NT, smem, stream>>>(p);
     return launch_status("fast lines");
 }
 
-#define SG_FAST_SWITCH(N_, CALL)                                                  \
-    switch (N_) {                                                                 \
-        case 64: return CALL(64);                                                 \
-        case 128: return CALL(128);                                               \
-        case 256: return CALL(256);                                               \
-        case 512: return CALL(512);                                               \
-        case 1024: return CALL(1024);                                             \
-        case 192: return CALL(192);                                               \
-        case 384: return CALL(384);                                               \
-        case 768: return CALL(768);                                               \
-        default: break;                                                           \
+// Calls CALL(N, W) with compile-time N from the runtime length and the wide or
+// narrow width for `units` independent lines/rows; falls through otherwise.
+#define SG_FAST_DISPATCH(N_, UNITS, CALL)                                                          \
+    switch (N_) {                                                                                  \
+        case 64: return fast_pick_width(UNITS, 32, 8) == 32 ? CALL(64, 32) : CALL(64, 8);          \
+        case 128: return fast_pick_width(UNITS, 16, 4) == 16 ? CALL(128, 16) : CALL(128, 4);       \
+        case 256: return fast_pick_width(UNITS, 16, 2) == 16 ? CALL(256, 16) : CALL(256, 2);       \
+        case 512: return fast_pick_width(UNITS, 16, 2) == 16 ? CALL(512, 16) : CALL(512, 2);       \
+        case 1024: return fast_pick_width(UNITS, 8, 1) == 8 ? CALL(1024, 8) : CALL(1024, 1);       \
+        case 192: return fast_pick_width(UNITS, 16, 4) == 16 ? CALL(192, 16) : CALL(192, 4);       \
+        case 384: return fast_pick_width(UNITS, 16, 2) == 16 ? CALL(384, 16) : CALL(384, 2);       \
+        case 768: return fast_pick_width(UNITS, 8, 1) == 8 ? CALL(768, 8) : CALL(768, 1);          \
+        default: break;                                                                            \
     }
 
 template <typename T>
 int launch_rows_r2c(RowsR2CParams<T> p, cudaStream_t stream) {
-#define SG_CALL(NN) launch_fast_rows_r2c<T, NN>(p, stream)
-    SG_FAST_SWITCH(p.st.n, SG_CALL)
+#define SG_CALL(NN, WW) launch_fast_rows_r2c<T, NN, WW>(p, stream)
+    SG_FAST_DISPATCH(p.st.n, p.n_rows, SG_CALL)
 #undef SG_CALL
     return launch_rows_r2c_generic<T>(p, stream);
 }
@@ -316,8 +370,8 @@ int launch_rows_r2c(RowsR2CParams<T> p, cudaStream_t stream) {
 template <typename T>
 int launch_rows_c2r(RowsC2RParams<T> p, cudaStream_t stream) {
     if (p.n_out % 2 == 0) {
-#define SG_CALL(NN) launch_fast_rows_c2r<T, NN>(p, stream)
-        SG_FAST_SWITCH(p.st.n, SG_CALL)
+#define SG_CALL(NN, WW) launch_fast_rows_c2r<T, NN, WW>(p, stream)
+        SG_FAST_DISPATCH(p.st.n, p.n_rows, SG_CALL)
 #undef SG_CALL
     }
     return launch_rows_c2r_generic<T>(p, stream);
@@ -325,8 +379,9 @@ int launch_rows_c2r(RowsC2RParams<T> p, cudaStream_t stream) {
 
 template <typename T, int MODE>
 int launch_lines(LinesParams<T> p, cudaStream_t stream) {
-#define SG_CALL(NN) launch_fast_lines<T, NN, MODE>(p, stream)
-    SG_FAST_SWITCH(p.st.n, SG_CALL)
+    const long long units = (long long)p.n_outer * p.inner;
+#define SG_CALL(NN, WW) launch_fast_lines<T, NN, WW, MODE>(p, stream)
+    SG_FAST_DISPATCH(p.st.n, units, SG_CALL)
 #undef SG_CALL
     return launch_lines_generic<T, MODE>(p, stream);
 }

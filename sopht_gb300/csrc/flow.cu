@@ -88,20 +88,20 @@ int launch_sweep2d(const Sweep2DParams<T>& p, cudaStream_t stream) {
     return launch_status("sweep2d");
 }
 
-template <typename T, int N>
+template <typename T, int N, int W>
 int launch_fast_flow_load(const FlowLoadParams<T>& p, cudaStream_t stream) {
-    const size_t smem = fast_smem_bytes<N>(sizeof(cplx_t<T>));
-    auto kern = fast_flow_load_kernel<T, N>;
+    const size_t smem = FlowLoadSmem<N, W>::template bytes<T>();
+    auto kern = fast_flow_load_kernel<T, N, W>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast flow_load smem attribute"));
-    kern<<<ceil_div(p.n_rows, FastShape<N>::W), FastShape<N>::NT, smem, stream>>>(p);
+    kern<<<ceil_div(p.n_rows, W), FastShape<N, W>::NT, smem, stream>>>(p);
     return launch_status("fast flow_load");
 }
 
 template <typename T>
 int launch_flow_load(FlowLoadParams<T> p, cudaStream_t stream) {
-#define SG_CALL(NN) launch_fast_flow_load<T, NN>(p, stream)
-    SG_FAST_SWITCH(p.st.n, SG_CALL)
+#define SG_CALL(NN, WW) launch_fast_flow_load<T, NN, WW>(p, stream)
+    SG_FAST_DISPATCH(p.st.n, p.n_rows, SG_CALL)
 #undef SG_CALL
     const int esz = sizeof(cplx_t<T>);
     const int rb = rows_per_block_for(p.st.n, esz);

@@ -249,67 +249,93 @@ __global__ void __launch_bounds__(256) flow_load_kernel(FlowLoadParams<T> p) {
     }
 }
 
-// Size-specialised variant of flow_load_kernel (M = nx in FastShape set).
-template <typename T, int M>
-__global__ void __launch_bounds__(FastShape<M>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
+// Size-specialised variant of flow_load_kernel (M = nx in the fast set).  Per
+// block, the W rows' source/destination offsets and y/z boundary factors are
+// computed once into shared memory; each element then costs a clamp on x only.
+template <int M, int W> struct FlowLoadSmem {
+    template <typename T> static constexpr size_t bytes() {
+        using C = cplx_t<T>;
+        return sizeof(C) * ((size_t)M * (W + 1) + M + (M + 1)) + sizeof(int64_t) * 3 * W + sizeof(T) * 2 * W + 32;
+    }
+};
+
+template <typename T, int M, int W>
+__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
     using C = cplx_t<T>;
-    using S = FastShape<M>;
-    constexpr int W = S::W, LS = S::LS, NT = S::NT, PER = M * W / NT;
+    using S = FastShape<M, W>;
+    constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
+    C* tw_m = buf + M * LS;
+    C* tw_l = tw_m + M;
+    int64_t* src_off = reinterpret_cast<int64_t*>(
+        (reinterpret_cast<uintptr_t>(tw_l + M + 1) + 15) & ~uintptr_t(15));
+    int64_t* dst_off = src_off + W;
+    int64_t* spec_off = dst_off + W;
+    T* fy = reinterpret_cast<T*>(spec_off + W);
+    T* fz = fy + W;
     const int tid = threadIdx.x;
     const int row0 = blockIdx.x * W;
     const int nx = p.nx;  // == M
+    if (tid < W) {
+        const int q = row0 + tid;
+        const int y = q % p.ny;
+        int c, zi;
+        if (p.dim == 3) {
+            zi = (q / p.ny) % p.nz;
+            c = q / (p.ny * p.nz);
+        } else {
+            zi = 0;
+            c = q / p.ny;
+        }
+        const int sy = clamp_band(y, p.ny, p.width);
+        const int sz = p.dim == 3 ? clamp_band(zi, p.nz, p.width) : 0;
+        src_off[tid] = (int64_t)c * p.comp_stride + ((int64_t)sz * p.ny + sy) * nx;
+        dst_off[tid] = (int64_t)c * p.comp_stride + ((int64_t)zi * p.ny + y) * nx;
+        spec_off[tid] = p.spec_map.offset(q);
+        fy[tid] = p.width > 0 ? p.cy[y] : T(1);
+        fz[tid] = (p.width > 0 && p.dim == 3) ? p.cz[zi] : T(1);
+    }
+    stage_table(tw_m, p.tw_m, M, tid, NT);
+    stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    __syncthreads();
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int e = tid + b * NT;
         const int r = e / M, n = e % M;
-        const int q = row0 + r;
         C z = cmake<C>(T(0), T(0));
-        if (q < p.n_rows && 2 * n < nx) {
-            const int y = q % p.ny;
-            int c, zi;
-            if (p.dim == 3) {
-                zi = (q / p.ny) % p.nz;
-                c = q / (p.ny * p.nz);
-            } else {
-                zi = 0;
-                c = q / p.ny;
-            }
-            const int sy = clamp_band(y, p.ny, p.width);
-            const int sz = p.dim == 3 ? clamp_band(zi, p.nz, p.width) : 0;
-            const int64_t src_row = (int64_t)c * p.comp_stride + ((int64_t)sz * p.ny + sy) * nx;
-            const int64_t dst_row = (int64_t)c * p.comp_stride + ((int64_t)zi * p.ny + y) * nx;
+        if (row0 + r < p.n_rows && 2 * n < nx) {
             const int x0 = 2 * n;
             const int s0 = clamp_band(x0, nx, p.width), s1 = clamp_band(x0 + 1, nx, p.width);
+            const T* src = p.src + src_off[r];
             if (s0 == x0 && s1 == x0 + 1) {
-                z = *reinterpret_cast<const C*>(p.src + src_row + x0);
+                z = *reinterpret_cast<const C*>(src + x0);
             } else {
-                z.x = p.src[src_row + s0];
-                z.y = p.src[src_row + s1];
+                z.x = src[s0];
+                z.y = src[s1];
             }
             if (p.width > 0) {
+                // penalise_field_boundary_{2,3}d.py order: X factor, then Y, then Z
                 z.x = z.x * p.cx[x0];
                 z.y = z.y * p.cx[x0 + 1];
-                const T fy = p.cy[y];
-                z.x = z.x * fy;
-                z.y = z.y * fy;
+                z.x = z.x * fy[r];
+                z.y = z.y * fy[r];
                 if (p.dim == 3) {
-                    const T fz = p.cz[zi];
-                    z.x = z.x * fz;
-                    z.y = z.y * fz;
+                    z.x = z.x * fz[r];
+                    z.y = z.y * fz[r];
                 }
             }
-            *reinterpret_cast<C*>(p.dst + dst_row + x0) = z;
+            const int64_t d = dst_off[r] + x0;
+            *reinterpret_cast<C*>(p.dst + d) = z;
             if (p.forcing)
                 for (int zc = 0; zc < p.zero_ncomp; ++zc)
-                    *reinterpret_cast<C*>(p.forcing + dst_row + zc * p.comp_stride + x0) = cmake<C>(T(0), T(0));
+                    *reinterpret_cast<C*>(p.forcing + d + zc * p.comp_stride) = cmake<C>(T(0), T(0));
         }
         buf[n * LS + r] = z;
     }
     __syncthreads();
-    fast_fft<M, false>(buf, p.tw_m, tid);
-    r2c_post_store<T, M>(buf, p.tw_l, p.spec, p.spec_map, row0, p.n_rows, tid);
+    fast_fft<M, W, false>(buf, tw_m, tid);
+    r2c_post_store<T, M, W>(buf, tw_l, p.spec, spec_off, row0, p.n_rows, tid);
 }
 
 // ---------------------------------------- curl + free stream + max |u| (2D)
