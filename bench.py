@@ -107,6 +107,20 @@ class Workload:
         return (1e-3 * rng.standard_normal(shape)).astype(real_t)
 
 
+def batch_members_spec(n=64, seed=42):
+    """64 uneven 2D cylinder flows: size class, Reynolds number and centre jitter per instance."""
+    rng = np.random.default_rng(seed)
+    classes = [(128, 256), (256, 512), (384, 768), (512, 1024)]
+    out = []
+    for _ in range(n):
+        ny, nx = classes[int(rng.integers(0, 4))]
+        re = float(rng.uniform(50, 400))
+        jit = rng.uniform(-0.02, 0.02, 2)
+        out.append(dict(grid=(ny, nx), nu=1.0 * 0.1 / re,
+                        centre=(0.25 + jit[0], 0.5 * ny / nx + jit[1], 0.0)))
+    return out
+
+
 def make_workload(name: str) -> Workload:
     if name == "rod128":
         length = 0.3
@@ -376,6 +390,137 @@ def run_gpu(args, wl: Workload, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def _batch_instances(spec, device):
+    import torch
+
+    import sopht_gb300.simulator as sps
+    sims, inters = [], []
+    for k, m in enumerate(spec):
+        sim = sps.UnboundedNavierStokesFlowSimulator2D(
+            grid_size=m["grid"], x_range=1.0, kinematic_viscosity=m["nu"], cfl=0.1, real_t=np.float32,
+            with_forcing=True, with_free_stream_flow=True, device=device)
+        rng = np.random.default_rng(1000 + k)
+        sim.vorticity_field.copy_(torch.from_numpy((1e-3 * rng.standard_normal(m["grid"])).astype(np.float32))
+                                  .to(device))
+        cyl = sps.Cylinder(m["centre"], base_radius=0.05)
+        inters.append(sps.RigidBodyFlowInteraction(
+            rigid_body=cyl, eul_grid_forcing_field=sim.eul_grid_forcing_field,
+            eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=-5e4,
+            virtual_boundary_damping_coeff=-20.0, dx=sim.dx, grid_dim=2, real_t=np.float32,
+            forcing_grid_cls=sps.CircularCylinderForcingGrid, num_forcing_points=96))
+        sims.append(sim)
+    return sims, inters
+
+
+def run_batch(args, rank, world):
+    """64 uneven 2D instances: batched persistent launches vs 64 sequential plain-GPU runs."""
+    import torch
+
+    from sopht_gb300.build import build
+    from sopht_gb300.simulator import BatchedFlowSimulator2D
+
+    build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    spec = batch_members_spec()
+    fs = np.array([1.0, 0.0])
+    sims, inters = _batch_instances(spec, device)
+    batch = BatchedFlowSimulator2D(sims, inters, free_stream_velocities=[fs] * len(sims))
+    batch.prime()
+    best = batch.autotune(steps=3)
+    stream = torch.cuda.Stream(device)
+    seg = min(args.steps, 25)
+    n_seg = max(1, args.steps // seg)
+    steps = seg * n_seg
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        stream.wait_stream(torch.cuda.current_stream())
+        for _ in range(args.warmup):
+            batch.step()
+        with torch.cuda.graph(graph, stream=stream):
+            for _ in range(seg):
+                batch.step()
+    graph.replay()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    start.record(stream)
+    for _ in range(n_seg):
+        graph.replay()
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    batch_ms = start.elapsed_time(stop)
+    n = len(sims)
+    cells = sum(int(np.prod(m["grid"])) for m in spec)
+    batched_rate = n * steps / (batch_ms * 1e-3)
+    graph.reset()
+    del graph, batch
+
+    # 64 sequential plain-GPU runs: each instance alone, its device-dt coupled step in its own graph
+    seq_steps = max(5, min(steps, 25))
+    seq_ms = 0.0
+    sims2, inters2 = _batch_instances(spec, device)
+    for sim, inter in zip(sims2, inters2, strict=True):
+        inter.upload_kinematics()
+        sim.device_stable_timestep(free_stream_velocity=fs, recompute_max=True)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            stream.wait_stream(torch.cuda.current_stream())
+            for _ in range(2):
+                dsc = sim.device_stable_timestep(free_stream_velocity=fs, recompute_max=False)
+                inter.device_call(dsc)
+                sim.time_step_device(dsc)
+            with torch.cuda.graph(g, stream=stream):
+                for _ in range(seq_steps):
+                    dsc = sim.device_stable_timestep(free_stream_velocity=fs, recompute_max=False)
+                    inter.device_call(dsc)
+                    sim.time_step_device(dsc)
+        torch.cuda.synchronize()
+        start.record(stream)
+        g.replay()
+        stop.record(stream)
+        torch.cuda.synchronize()
+        seq_ms += start.elapsed_time(stop)
+        g.reset()
+    sequential_rate = n * seq_steps / (seq_ms * 1e-3)
+    # the plain drop-in loop (host dt, per-call launches) for the same 64 instances
+    host_steps = 3
+    t0 = time.perf_counter()
+    for sim, inter in zip(sims2, inters2, strict=True):
+        for _ in range(host_steps):
+            dt = sim.compute_stable_timestep()
+            inter.time_step(dt=dt)
+            inter()
+            sim.time_step(dt=dt, free_stream_velocity=fs)
+    torch.cuda.synchronize()
+    host_rate = n * host_steps / (time.perf_counter() - t0)
+    if rank != 0:
+        return
+    out = {
+        "metric": "instance-steps/s (64 uneven 2D instances, batched vs 64 sequential plain-GPU runs)",
+        "value": round(world * batched_rate, 1), "unit": "instance-steps/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": round(batch_ms / steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "gcell_updates_per_s": round(world * cells * steps / (batch_ms * 1e-3) / 1e9, 3),
+        "config": {"workload": "batch of 64 2D cylinder flows, grids drawn from {128x256, 256x512, 384x768, "
+                               "512x1024}, Re ~ U[50, 400], centre jitter U[-0.02, 0.02]^2, seed 42",
+                   "instances": n, "total_cells": cells, "autotuned": {"sweep_tile_y": best[0],
+                                                                        "blocks_per_sm": best[1]}},
+        "sequential_plain_gpu": {"value": round(sequential_rate, 1), "unit": "instance-steps/s",
+                                 "note": f"each instance alone, device-dt coupled step in a CUDA graph of "
+                                         f"{seq_steps} steps, instances one after another"},
+        "speedup_vs_sequential": round(batched_rate / sequential_rate, 2),
+        "plain_dropin_host_loop": {"value": round(host_rate, 1), "unit": "instance-steps/s",
+                                   "note": "public API per step (host dt), instances one after another"},
+        "clocks": clock_info,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def accuracy_vs_fp64(wl, device, steps):
     """Relative L2 of the fp32 GPU path against the same path in fp64 after `steps` steps."""
     import torch
@@ -499,13 +644,16 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rod128", choices=["rod128", "cylinder2d", "carpet256"])
+    ap.add_argument("--workload", default="rod128", choices=["rod128", "cylinder2d", "carpet256", "batch64"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.workload == "batch64":
+        run_batch(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
+        return
     wl = make_workload(args.workload)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

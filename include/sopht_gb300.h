@@ -144,6 +144,51 @@ int sg_flow_device_dt(sg_flow_plan plan, const void* velocity, double cfl, doubl
                       double flow_density, double dt_prefac, const double* free_stream,
                       const sg_step_scalars** dev_scalars_out, void* stream);
 
+/* ----------------------------------------------------- batched 2D instances */
+/* Many independent 2D simulators (uneven grids and Reynolds numbers, one
+ * virtual-boundary body each) advanced together: one persistent launch per
+ * fused operator for the whole batch, dt evaluated per instance on the GPU.
+ * No reference counterpart (the reference steps one simulator at a time,
+ * navier_stokes_flow_simulators.py:200-209, with its interactor,
+ * VirtualBoundaryForcing.py:232-283).  Every member references an existing 2D
+ * fp32 flow plan and its fields; nx and 2 ny must be 256, 512, 768 or 1024. */
+typedef struct sg_batch2d_s* sg_batch2d;
+typedef struct sg_batch2d_member {
+    sg_flow_plan plan;
+    void* vorticity;
+    void* velocity;
+    void* forcing;
+    void* stream_func;
+    double cfl, nu, flow_density, dt_prefac;
+    double free_stream[2];
+    int n_lag;              /* 0: no immersed body */
+    int kernel_type;        /* 0 cosine, 1 Peskin */
+    double dx, shift;
+    const double* position;       /* (2, n_lag) device, double */
+    const double* body_velocity;  /* (2, n_lag) device, double */
+    int32_t* nearest;
+    void* weights;
+    void* flow_velocity;
+    void* velocity_mismatch;
+    void* position_mismatch;
+    void* lag_forcing;
+    double stiffness, damping;
+    int32_t* status;
+} sg_batch2d_member;
+int sg_batch2d_create(int n, const sg_batch2d_member* members, sg_batch2d* batch_out);
+/* Tuning knobs (picked by the Python autotuner): sweep tile height 8 or 16;
+ * persistent blocks per SM (0 = one block per work item). */
+int sg_batch2d_set_tuning(sg_batch2d batch, int sweep_tile_y, int blocks_per_sm);
+/* One coupled step of every member (8 launches).  Each member's velocity max
+ * must be primed once with sg_flow_device_dt before the first step. */
+int sg_batch2d_step(sg_batch2d batch, void* stream);
+int sg_batch2d_destroy(sg_batch2d batch);
+
+/* Simulated time accumulated on the GPU by sg_flow_device_dt / the batched
+ * step (the device-resident counterpart of FlowSimulator.time,
+ * flow_simulators.py:126-128).  Synchronous read into *host_out. */
+int sg_flow_read_device_time(sg_flow_plan plan, double* host_out);
+
 /* ------------------------------------------------ single operators (2D) */
 /* stencil_ops_2d/advection_timestep_2d.py:10-55 (flux buffer internal). */
 int sg_advection_eno3_step_2d(int dtype, int ny, int nx, const void* field_in, void* field_out,

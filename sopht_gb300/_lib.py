@@ -35,6 +35,20 @@ class StepScalars(ctypes.Structure):
     ]
 
 
+class Batch2DMember(ctypes.Structure):
+    """Mirror of ``sg_batch2d_member``."""
+
+    _fields_ = [
+        ("plan", c_void_p), ("vorticity", c_void_p), ("velocity", c_void_p), ("forcing", c_void_p),
+        ("stream_func", c_void_p), ("cfl", c_double), ("nu", c_double), ("flow_density", c_double),
+        ("dt_prefac", c_double), ("free_stream", c_double * 2), ("n_lag", c_int), ("kernel_type", c_int),
+        ("dx", c_double), ("shift", c_double), ("position", c_void_p), ("body_velocity", c_void_p),
+        ("nearest", c_void_p), ("weights", c_void_p), ("flow_velocity", c_void_p),
+        ("velocity_mismatch", c_void_p), ("position_mismatch", c_void_p), ("lag_forcing", c_void_p),
+        ("stiffness", c_double), ("damping", c_double), ("status", c_void_p),
+    ]
+
+
 _SIGNATURES = {
     "sg_last_error": (c_char_p, []),
     "sg_version": (c_int, []),
@@ -48,6 +62,7 @@ _SIGNATURES = {
     "sg_flow_plan_destroy": (c_int, [c_void_p]),
     "sg_flow_plan_bytes": (c_int64, [c_void_p]),
     "sg_flow_set_timing_events": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),
+    "sg_flow_read_device_time": (c_int, [c_void_p, POINTER(c_double)]),
     "sg_flow_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, POINTER(StepScalars), c_void_p,
                              c_void_p]),
     "sg_max_abs_sum": (c_int, [c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p]),
@@ -74,6 +89,10 @@ _SIGNATURES = {
     "sg_ib_spread": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_int, c_void_p]),
     "sg_ib_mismatch_step": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_batch2d_create": (c_int, [c_int, POINTER(Batch2DMember), POINTER(c_void_p)]),
+    "sg_batch2d_set_tuning": (c_int, [c_void_p, c_int, c_int]),
+    "sg_batch2d_step": (c_int, [c_void_p, c_void_p]),
+    "sg_batch2d_destroy": (c_int, [c_void_p]),
 }
 
 _lib = None

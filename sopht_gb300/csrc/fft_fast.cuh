@@ -126,17 +126,16 @@ __device__ __forceinline__ void stage_table(C* dst, const C* __restrict__ src, i
 
 // ----------------------------------------------------------- strided lines
 template <typename T, int N, int W, int MODE>
-__global__ void __launch_bounds__(FastShape<N, W>::NT) fast_lines_kernel(LinesParams<T> p) {
+__device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid, unsigned char* smem_raw) {
     using C = cplx_t<T>;
     using S = FastShape<N, W>;
     constexpr int LS = S::LS, NT = S::NT, PER = N * W / NT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw = buf + N * LS;
     const int tid = threadIdx.x;
     const int chunks = (p.inner + W - 1) / W;
-    const int outer = blockIdx.x / chunks;
-    const int c0 = (blockIdx.x % chunks) * W;
+    const int outer = bid / chunks;
+    const int c0 = (bid % chunks) * W;
     const int wcount = min(W, p.inner - c0);
     stage_table(tw, p.tw, N, tid, NT);
     const C* src = p.in + (int64_t)outer * p.outer_stride + c0;
@@ -186,6 +185,12 @@ __global__ void __launch_bounds__(FastShape<N, W>::NT) fast_lines_kernel(LinesPa
     }
 }
 
+template <typename T, int N, int W, int MODE>
+__global__ void __launch_bounds__(FastShape<N, W>::NT) fast_lines_kernel(LinesParams<T> p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    fast_lines_body<T, N, W, MODE>(p, blockIdx.x, smem_raw);
+}
+
 // -------------------------------------------------------------- row kernels
 // Rows of the x axis: W rows per block, element (row r, point n) at buf[n*LS + r].
 // Shared: buf [M][LS], twiddles tw_m [M] and tw_l [M + 1], row offsets [2 W].
@@ -217,11 +222,10 @@ __device__ __forceinline__ void r2c_post_store(const cplx_t<T>* buf, const cplx_
 }
 
 template <typename T, int M, int W>
-__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_r2c_kernel(RowsR2CParams<T> p) {
+__device__ __forceinline__ void fast_rows_r2c_body(const RowsR2CParams<T>& p, int bid, unsigned char* smem_raw) {
     using C = cplx_t<T>;
     using S = FastShape<M, W>;
     constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw_m = buf + M * LS;
     C* tw_l = tw_m + M;
@@ -229,7 +233,7 @@ __global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_r2c_kernel(Rows
         (reinterpret_cast<uintptr_t>(tw_l + M + 1) + 15) & ~uintptr_t(15));
     int64_t* out_off = in_off + W;
     const int tid = threadIdx.x;
-    const int row0 = blockIdx.x * W;
+    const int row0 = bid * W;
     if (tid < W) {
         in_off[tid] = p.in_map.offset(row0 + tid);
         out_off[tid] = p.out_map.offset(row0 + tid);
@@ -255,11 +259,16 @@ __global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_r2c_kernel(Rows
 }
 
 template <typename T, int M, int W>
-__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_c2r_kernel(RowsC2RParams<T> p) {
+__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_r2c_kernel(RowsR2CParams<T> p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    fast_rows_r2c_body<T, M, W>(p, blockIdx.x, smem_raw);
+}
+
+template <typename T, int M, int W>
+__device__ __forceinline__ void fast_rows_c2r_body(const RowsC2RParams<T>& p, int bid, unsigned char* smem_raw) {
     using C = cplx_t<T>;
     using S = FastShape<M, W>;
     constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw_m = buf + M * LS;
     C* tw_l = tw_m + M;
@@ -267,7 +276,7 @@ __global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_c2r_kernel(Rows
         (reinterpret_cast<uintptr_t>(tw_l + M + 1) + 15) & ~uintptr_t(15));
     int64_t* out_off = in_off + W;
     const int tid = threadIdx.x;
-    const int row0 = blockIdx.x * W;
+    const int row0 = bid * W;
     if (tid < W) {
         in_off[tid] = p.in_map.offset(row0 + tid);
         out_off[tid] = p.out_map.offset(row0 + tid);
@@ -303,6 +312,12 @@ __global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_c2r_kernel(Rows
         if (row0 + r >= p.n_rows) continue;
         *reinterpret_cast<C*>(p.out + out_off[r] + 2 * n) = buf[n * LS + r];
     }
+}
+
+template <typename T, int M, int W>
+__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_c2r_kernel(RowsC2RParams<T> p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    fast_rows_c2r_body<T, M, W>(p, blockIdx.x, smem_raw);
 }
 
 // ------------------------------------------------------------- dispatch

@@ -11,37 +11,9 @@
 #include <cfloat>
 #include <cstring>
 
-#include "flow_kernels.cuh"
-#include "poisson.cuh"
+#include "flow_plan.cuh"
 
-namespace sg {
-int poisson_plan_create_impl(int, int, int, int, double, int, int, sg_poisson_plan_s**);
-void poisson_plan_free(sg_poisson_plan_s*);
-}  // namespace sg
 
-struct sg_flow_plan_s {
-    int dim = 2, nz = 1, ny = 0, nx = 0, dtype = SG_F32;
-    int width = 0, filter_type = 0, filter_order = 0;
-    double x_range = 1.0, dx = 0.0;
-    sg_poisson_plan_s* poisson = nullptr;
-    void* scratch_a = nullptr;  // vector field
-    void* scratch_b = nullptr;  // vector field (3D)
-    void* filt_a = nullptr;     // scalar field (3D filter)
-    void* filt_b = nullptr;
-    void* coef_x = nullptr;
-    void* coef_y = nullptr;
-    void* coef_z = nullptr;
-    // device block: [0, 64) sg_step_scalars, [64, 72) umax (field type), [72, 80) time
-    unsigned char* dev_block = nullptr;
-    int64_t bytes = 0;
-    // optional one-shot timing events recorded between the passes of the next step
-    int n_events = 0;
-    cudaEvent_t events[16] = {};
-    sg_step_scalars* dev_scalars() const { return reinterpret_cast<sg_step_scalars*>(dev_block); }
-    void* umax_slot() const { return dev_block + 64; }
-    double* time_slot() const { return reinterpret_cast<double*>(dev_block + 72); }
-    int64_t cells() const { return (int64_t)nz * ny * nx; }
-};
 
 namespace sg {
 
@@ -446,6 +418,12 @@ extern "C" int sg_flow_set_timing_events(sg_flow_plan p, int n_events, void* con
     p->n_events = n_events;
     for (int i = 0; i < 16; ++i) p->events[i] = i < n_events ? (cudaEvent_t)events[i] : nullptr;
     return SG_OK;
+}
+
+extern "C" int sg_flow_read_device_time(sg_flow_plan p, double* host_out) {
+    SG_REQUIRE(p && host_out, SG_ERR_INVALID_ARG, "read device time: null argument");
+    return cuda_status(cudaMemcpy(host_out, p->time_slot(), sizeof(double), cudaMemcpyDeviceToHost),
+                       "read device time");
 }
 
 extern "C" int sg_flow_plan_destroy(sg_flow_plan p) {

@@ -51,7 +51,7 @@ __device__ __forceinline__ T eno3_face(T qm1, T q0, T qp1, T qp2, T u0, T up1) {
 }
 
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX * 8) sweep2d_kernel(Sweep2DParams<T> p) {
+__device__ __forceinline__ void sweep2d_body(const Sweep2DParams<T>& p, int bx, int by) {
     constexpr int HW = 3, HF = 4;
     constexpr int WX = TX + 2 * HW, WY = TY + 2 * HW;
     constexpr int FX = TX + 2 * HF, FY = TY + 2 * HF;
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(TX * 8) sweep2d_kernel(Sweep2DParams<T> p) {
     __shared__ T s_w2[W2Y * W2X];
     const int nthr = blockDim.x * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int x0 = bx * TX, y0 = by * TY;
     const int ny = p.ny, nx = p.nx;
     const int64_t plane = (int64_t)ny * nx;
     const bool forcing = p.f != nullptr;
@@ -150,6 +150,11 @@ __global__ void __launch_bounds__(TX * 8) sweep2d_kernel(Sweep2DParams<T> p) {
         }
         p.out[(int64_t)gy * nx + gx] = w3;
     }
+}
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX * 8) sweep2d_kernel(Sweep2DParams<T> p) {
+    sweep2d_body<T, TX, TY>(p, blockIdx.x, blockIdx.y);
 }
 
 // --------------------------------------------- fused Poisson load (x rows R2C)
@@ -260,11 +265,10 @@ template <int M, int W> struct FlowLoadSmem {
 };
 
 template <typename T, int M, int W>
-__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
+__device__ __forceinline__ void fast_flow_load_body(const FlowLoadParams<T>& p, int bid, unsigned char* smem_raw) {
     using C = cplx_t<T>;
     using S = FastShape<M, W>;
     constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw_m = buf + M * LS;
     C* tw_l = tw_m + M;
@@ -275,7 +279,7 @@ __global__ void __launch_bounds__(FastShape<M, W>::NT) fast_flow_load_kernel(Flo
     T* fy = reinterpret_cast<T*>(spec_off + W);
     T* fz = fy + W;
     const int tid = threadIdx.x;
-    const int row0 = blockIdx.x * W;
+    const int row0 = bid * W;
     const int nx = p.nx;  // == M
     if (tid < W) {
         const int q = row0 + tid;
@@ -338,6 +342,12 @@ __global__ void __launch_bounds__(FastShape<M, W>::NT) fast_flow_load_kernel(Flo
     r2c_post_store<T, M, W>(buf, tw_l, p.spec, spec_off, row0, p.n_rows, tid);
 }
 
+template <typename T, int M, int W>
+__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    fast_flow_load_body<T, M, W>(p, blockIdx.x, smem_raw);
+}
+
 // ---------------------------------------- curl + free stream + max |u| (2D)
 template <typename T>
 __device__ __forceinline__ void atomic_max_nonneg(T* slot, T v);
@@ -375,10 +385,11 @@ template <typename T> struct Curl2DParams {
     T* umax;   // may be null
 };
 
+// one 32 x 8 tile of the 2D curl (block shape 32 x 8)
 template <typename T>
-__global__ void __launch_bounds__(256) curl2d_kernel(Curl2DParams<T> p) {
-    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void curl2d_body(const Curl2DParams<T>& p, int bx, int by) {
+    const int gx = bx * 32 + threadIdx.x;
+    const int gy = by * 8 + threadIdx.y;
     const int ny = p.ny, nx = p.nx;
     T m = T(0);
     if (gx < nx && gy < ny) {
@@ -400,6 +411,11 @@ __global__ void __launch_bounds__(256) curl2d_kernel(Curl2DParams<T> p) {
         m = block_max(m);
         if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(p.umax, m);
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) curl2d_kernel(Curl2DParams<T> p) {
+    curl2d_body<T>(p, blockIdx.x, blockIdx.y);
 }
 
 // ------------------------------------------------------------ 3D kernels

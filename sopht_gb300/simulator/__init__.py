@@ -1,5 +1,6 @@
 """Flow simulators and immersed-body coupling (sopht.simulator counterparts)."""
 
+from .batch import BatchedFlowSimulator2D
 from .flow import (
     FlowSimulator,
     UnboundedNavierStokesFlowSimulator2D,
@@ -21,6 +22,7 @@ from .immersed_body import (
 )
 
 __all__ = [
+    "BatchedFlowSimulator2D",
     "CircularCylinderForcingGrid",
     "CosseratRodElementCentricForcingGrid",
     "CosseratRodFlowInteraction",

@@ -209,6 +209,12 @@ class _UnboundedNavierStokesBase(FlowSimulator):
                   ctypes.byref(out), stream_ptr(self.device))
         return out.value
 
+    def device_time(self) -> float:
+        """Time accumulated on the GPU by the device-resident dt (synchronises)."""
+        out = ctypes.c_double()
+        _lib.call("sg_flow_read_device_time", self._plan, ctypes.byref(out))
+        return self.time + out.value
+
     def time_step_device(self, dev_scalars: int) -> None:
         """One flow step with dt and prefactors read from device memory."""
         self._step(None, ctypes.c_void_p(dev_scalars))
