@@ -266,7 +266,7 @@ def run_gpu(args, wl: Workload, rank, world):
     sim, inters = make_gpu_case(wl, rt, device)
     for inter in inters:
         inter.upload_kinematics()
-    sim.device_stable_timestep(free_stream_velocity=wl.u_inf, recompute_max=True)
+    sim.prime_velocity_max()
     stream = torch.cuda.Stream(device)
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
@@ -291,7 +291,8 @@ def run_gpu(args, wl: Workload, rank, world):
             for k in range(seg):
                 device_step(wl, sim, inters, events[k])
     torch.cuda.synchronize()
-    graph.replay()  # one untimed replay after capture
+    with torch.cuda.stream(stream):
+        graph.replay()  # one untimed replay after capture
     torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local)
@@ -299,13 +300,18 @@ def run_gpu(args, wl: Workload, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    start.record(stream)
-    for _ in range(n_seg):
-        graph.replay()
-    stop.record(stream)
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(n_seg):
+            graph.replay()
+        stop.record(stream)
     torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t_wall) * 1e3
     clock_info = clocks.stop()
     elapsed_ms = start.elapsed_time(stop)
+    if elapsed_ms < 0.5 * wall_ms:
+        raise RuntimeError(f"event time {elapsed_ms:.3f} ms disagrees with wall time {wall_ms:.3f} ms")
     if world > 1:
         t = torch.tensor([elapsed_ms], device=device)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -442,18 +448,24 @@ def run_batch(args, rank, world):
         with torch.cuda.graph(graph, stream=stream):
             for _ in range(seg):
                 batch.step()
-    graph.replay()
+    with torch.cuda.stream(stream):
+        graph.replay()
     torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local)
     clocks.start()
-    start.record(stream)
-    for _ in range(n_seg):
-        graph.replay()
-    stop.record(stream)
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(n_seg):
+            graph.replay()
+        stop.record(stream)
     torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t_wall) * 1e3
     clock_info = clocks.stop()
     batch_ms = start.elapsed_time(stop)
+    if batch_ms < 0.5 * wall_ms:
+        raise RuntimeError(f"event time {batch_ms:.3f} ms disagrees with wall time {wall_ms:.3f} ms")
     n = len(sims)
     cells = sum(int(np.prod(m["grid"])) for m in spec)
     batched_rate = n * steps / (batch_ms * 1e-3)
@@ -466,7 +478,7 @@ def run_batch(args, rank, world):
     sims2, inters2 = _batch_instances(spec, device)
     for sim, inter in zip(sims2, inters2, strict=True):
         inter.upload_kinematics()
-        sim.device_stable_timestep(free_stream_velocity=fs, recompute_max=True)
+        sim.prime_velocity_max()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.stream(stream):
             stream.wait_stream(torch.cuda.current_stream())
@@ -480,9 +492,10 @@ def run_batch(args, rank, world):
                     inter.device_call(dsc)
                     sim.time_step_device(dsc)
         torch.cuda.synchronize()
-        start.record(stream)
-        g.replay()
-        stop.record(stream)
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            g.replay()
+            stop.record(stream)
         torch.cuda.synchronize()
         seq_ms += start.elapsed_time(stop)
         g.reset()

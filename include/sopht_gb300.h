@@ -184,6 +184,11 @@ int sg_batch2d_set_tuning(sg_batch2d batch, int sweep_tile_y, int blocks_per_sm)
 int sg_batch2d_step(sg_batch2d batch, void* stream);
 int sg_batch2d_destroy(sg_batch2d batch);
 
+/* Record max over cells of sum_d |u_d| of `velocity` in the plan (the value
+ * the next sg_flow_device_dt with velocity = NULL, or the next batched step,
+ * turns into dt) without evaluating dt or advancing the device time. */
+int sg_flow_prime_max(sg_flow_plan plan, const void* velocity, void* stream);
+
 /* Simulated time accumulated on the GPU by sg_flow_device_dt / the batched
  * step (the device-resident counterpart of FlowSimulator.time,
  * flow_simulators.py:126-128).  Synchronous read into *host_out. */

@@ -63,6 +63,7 @@ _SIGNATURES = {
     "sg_flow_plan_bytes": (c_int64, [c_void_p]),
     "sg_flow_set_timing_events": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),
     "sg_flow_read_device_time": (c_int, [c_void_p, POINTER(c_double)]),
+    "sg_flow_prime_max": (c_int, [c_void_p, c_void_p, c_void_p]),
     "sg_flow_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, POINTER(StepScalars), c_void_p,
                              c_void_p]),
     "sg_max_abs_sum": (c_int, [c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p]),

@@ -420,6 +420,14 @@ extern "C" int sg_flow_set_timing_events(sg_flow_plan p, int n_events, void* con
     return SG_OK;
 }
 
+extern "C" int sg_flow_prime_max(sg_flow_plan p, const void* velocity, void* stream_) {
+    SG_REQUIRE(p && velocity, SG_ERR_INVALID_ARG, "prime max: null argument");
+    auto stream = (cudaStream_t)stream_;
+    if (p->dtype == SG_F32)
+        return launch_max_abs_sum<float>(p->cells(), p->dim, (const float*)velocity, (float*)p->umax_slot(), stream);
+    return launch_max_abs_sum<double>(p->cells(), p->dim, (const double*)velocity, (double*)p->umax_slot(), stream);
+}
+
 extern "C" int sg_flow_read_device_time(sg_flow_plan p, double* host_out) {
     SG_REQUIRE(p && host_out, SG_ERR_INVALID_ARG, "read device time: null argument");
     return cuda_status(cudaMemcpy(host_out, p->time_slot(), sizeof(double), cudaMemcpyDeviceToHost),

@@ -106,7 +106,7 @@ class BatchedFlowSimulator2D:
     def prime(self) -> None:
         """Evaluate every instance's velocity max once (before the first step)."""
         for sim in self.simulators:
-            sim.device_stable_timestep(recompute_max=True)
+            sim.prime_velocity_max()
         self._primed = True
 
     def set_tuning(self, sweep_tile_y: int, blocks_per_sm: int) -> None:

@@ -209,6 +209,10 @@ class _UnboundedNavierStokesBase(FlowSimulator):
                   ctypes.byref(out), stream_ptr(self.device))
         return out.value
 
+    def prime_velocity_max(self) -> None:
+        """Record max sum_d |u_d| of the current velocity for the first device-resident dt."""
+        _lib.call("sg_flow_prime_max", self._plan, ptr(self.velocity_field), stream_ptr(self.device))
+
     def device_time(self) -> float:
         """Time accumulated on the GPU by the device-resident dt (synchronises)."""
         out = ctypes.c_double()

@@ -49,7 +49,7 @@ def test_batched_equals_individual(tuning):
     batch.set_tuning(*tuning)
     for sim, inter in single_members:
         inter.upload_kinematics()
-        sim.device_stable_timestep(free_stream_velocity=fs, recompute_max=True)
+        sim.prime_velocity_max()
     steps = 4
     for _ in range(steps):
         batch.step()
