@@ -534,6 +534,217 @@ def run_batch(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def _adjoint_case(wl, real_t, device, dts, checkpoint_every, use_graphs):
+    """The cylinder2d flow with a prescribed wall velocity, as a differentiable objective."""
+    from sopht_gb300.simulator import BodyForceObjective2D
+    sim, inters = make_gpu_case(wl, real_t, device)
+    obj = BodyForceObjective2D(sim, inters[0], dts, free_stream_velocity=wl.u_inf[:2], direction=(1.0, 0.0),
+                               checkpoint_every=checkpoint_every, use_graphs=use_graphs)
+    return sim, inters[0], obj
+
+
+def wall_velocity(wl, inter, seed=42):
+    """Tangential marker velocity with amplitude U[0, 0.2] per marker (seeded)."""
+    pos = inter.forcing_grid.position_field
+    c = np.asarray(wl.bodies[0]["centre"][:2]).reshape(2, 1)
+    rel = pos - c
+    tangent = np.stack([-rel[1], rel[0]]) / np.linalg.norm(rel, axis=0)
+    amp = np.random.default_rng(seed).uniform(0.0, 0.2, pos.shape[1])
+    return tangent * amp
+
+
+def frozen_dt_sequence(wl, device, V, n_steps):
+    """dt of each step of the forward run with the wall velocity (compute_stable_timestep, CFL 0.1)."""
+    import torch
+    sim, inters = make_gpu_case(wl, np.float32, device)
+    inter = inters[0]
+    inter.upload_kinematics()
+    Vd = torch.as_tensor(V, dtype=torch.float64, device=device)
+    dts = []
+    for _ in range(n_steps):
+        dt = float(sim.compute_stable_timestep())
+        inter._interaction(sim.velocity_field, inter._pos_stage.dev, Vd, xi_step=True, xi_dt=dt)
+        inter._spread(sim.eul_grid_forcing_field, reset=True)
+        sim.time_step(dt=dt, free_stream_velocity=wl.u_inf)
+        dts.append(dt)
+    return dts
+
+
+def run_adjoint(args, rank, world):
+    """Drag gradient through 200 steps of the 2D cylinder flow (wall velocity + viscosity)."""
+    import torch
+
+    from sopht_gb300.build import build
+    from sopht_gb300.simulator import time_integrated_body_force
+
+    build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    wl = make_workload("cylinder2d")
+    n_steps, ck = args.adjoint_steps, 20
+    _, inter0, _ = _adjoint_case(wl, np.float32, device, [1e-4], ck, False)
+    V = wall_velocity(wl, inter0)
+    dts = frozen_dt_sequence(wl, device, V, n_steps)
+    Vt = torch.as_tensor(V, dtype=torch.float64, device=device)
+    nu = wl.nu
+    # fp32 objective, both passes captured in CUDA graphs
+    sim, inter, obj = _adjoint_case(wl, np.float32, device, dts, ck, True)
+    for _ in range(max(1, args.warmup)):
+        obj.value_and_grad(Vt, nu)
+    torch.cuda.synchronize()
+    reps = max(1, args.steps // n_steps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    fwd_ms = bwd_ms = 0.0
+    for _ in range(reps):
+        ev[0].record()
+        obj.forward(Vt, nu)
+        ev[1].record()
+        obj._run("backward", obj._backward_pass)
+        ev[2].record()
+        torch.cuda.synchronize()
+        fwd_ms += ev[0].elapsed_time(ev[1])
+        bwd_ms += ev[1].elapsed_time(ev[2])
+    clock_info = clocks.stop()
+    fwd_step = fwd_ms / (reps * n_steps)
+    bwd_step = bwd_ms / (reps * n_steps)
+    # the plain drop-in forward step (device dt, graph) of the same flow, for reference
+    psim, pinters = make_gpu_case(wl, np.float32, device)
+    for pi in pinters:
+        pi.upload_kinematics()
+    psim.prime_velocity_max()
+    stream = torch.cuda.Stream(device)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        stream.wait_stream(torch.cuda.current_stream())
+        for _ in range(3):
+            device_step(wl, psim, pinters)
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(25):
+                device_step(wl, psim, pinters)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        g.replay()
+        ev[0].record(stream)
+        for _ in range(8):
+            g.replay()
+        ev[1].record(stream)
+    torch.cuda.synchronize()
+    plain_step = ev[0].elapsed_time(ev[1]) / (8 * 25)
+    # end to end through the autograd API: V from pinned host memory, gradient read back
+    Vh = torch.as_tensor(V, dtype=torch.float64).pin_memory()
+    gh = torch.empty_like(Vh).pin_memory()
+    t0 = time.perf_counter()
+    e2e_reps = 2
+    for _ in range(e2e_reps):
+        Vd = Vh.to(device, non_blocking=True).requires_grad_(True)
+        nut = torch.tensor(nu, dtype=torch.float64, device=device, requires_grad=True)
+        loss = time_integrated_body_force(obj, Vd, nut)
+        loss.backward()
+        gh.copy_(Vd.grad)
+        _ = float(nut.grad.item())
+    e2e_s = (time.perf_counter() - t0) / e2e_reps
+    # gradients: fp32 and fp64 adjoints, FP64 central differences, FP64 CPU oracle
+    L32, g32, n32 = obj.value_and_grad(Vt, nu)
+    _, _, obj64 = _adjoint_case(wl, np.float64, device, dts, ck, True)
+    L64, g64, n64 = obj64.value_and_grad(Vt, nu)
+    g32n, g64n = g32.cpu().numpy(), g64.cpu().numpy()
+    rel = lambda a, b: float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))  # noqa
+    rng = np.random.default_rng(7)
+    comps = [tuple(int(c) for c in rng.integers(0, (2, V.shape[1]))) for _ in range(6)]
+    # central differences in FP64 over a range of steps: large steps cross ENO3 upwind-branch switches
+    # (the flux is discontinuous where u_j = -u_{j+1}), small ones measure the derivative itself
+    fd = {"components": [list(c) for c in comps], "adjoint_fp64": [float(g64n[d, k]) for d, k in comps],
+          "adjoint_fp32": [float(g32n[d, k]) for d, k in comps], "nu_adjoint_fp64": n64, "nu_adjoint_fp32": n32,
+          "steps": {}}
+    for h in (1e-3, 1e-4, 1e-5, 1e-6):
+        rows = []
+        for (d, k) in comps:
+            E = torch.zeros_like(Vt)
+            E[d, k] = 1.0
+            rows.append((obj64.forward(Vt + h * E, nu).item() - obj64.forward(Vt - h * E, nu).item()) / (2 * h))
+        fnu = (obj64.forward(Vt, nu + h * nu).item() - obj64.forward(Vt, nu - h * nu).item()) / (2 * h * nu)
+        fdv = np.array(rows)
+        fd["steps"][f"{h:g}"] = {
+            "fd": [float(x) for x in fdv],
+            "rel_err_fp64_adjoint": rel([g64n[d, k] for d, k in comps], fdv),
+            "rel_err_fp32_adjoint": rel([g32n[d, k] for d, k in comps], fdv),
+            "nu_fd": float(fnu), "nu_rel_err_fp64": abs(n64 - fnu) / abs(fnu),
+            "nu_rel_err_fp32": abs(n32 - fnu) / abs(fnu)}
+    fd["note"] = "h is absolute for V and relative for nu"
+    cpu_ref = None
+    if not args.skip_cpu:
+        from oracle.adjoint import DragProblem2D
+        from oracle.flow import CircularCylinderOracle, NavierStokes2DOracle
+        w0 = wl.initial_vorticity(np.float64)
+        b = wl.bodies[0]
+
+        def make_flow():
+            f = NavierStokes2DOracle(wl.grid, wl.x_range, nu, cfl=wl.cfl, real_t=np.float64, with_forcing=True,
+                                     with_free_stream_flow=True)
+            f.vorticity_field[...] = w0
+            return f
+
+        cyl = CircularCylinderOracle(b["centre"], b["radius"], wl.n_markers)
+        hsp = cyl.get_maximum_lagrangian_grid_spacing()
+        n_cpu = min(n_steps, args.adjoint_cpu_steps)
+        prob = DragProblem2D(make_flow, cyl.position_field, wl.K * hsp, wl.C * hsp, dts[:n_cpu], wl.u_inf[:2])
+        t0 = time.perf_counter()
+        Lc, gc, nc = prob.gradient(V, nu)
+        cpu_s = time.perf_counter() - t0
+        if n_cpu == n_steps:
+            gpu64, gpu32, Lg, ng64, ng32 = g64n, g32n, L64, n64, n32
+        else:
+            _, _, o64s = _adjoint_case(wl, np.float64, device, dts[:n_cpu], ck, False)
+            _, _, o32s = _adjoint_case(wl, np.float32, device, dts[:n_cpu], ck, False)
+            Lg, g_a, ng64 = o64s.value_and_grad(Vt, nu)
+            _, g_b, ng32 = o32s.value_and_grad(Vt, nu)
+            gpu64, gpu32 = g_a.cpu().numpy(), g_b.cpu().numpy()
+        cpu_ref = {"steps": n_cpu, "seconds": round(cpu_s, 2),
+                   "loss_rel_err_fp64_gpu": abs(Lg - Lc) / abs(Lc),
+                   "grad_rel_l2_fp64_gpu": rel(gpu64, gc), "grad_rel_l2_fp32_gpu": rel(gpu32, gc),
+                   "nu_rel_err_fp64_gpu": abs(ng64 - nc) / abs(nc), "nu_rel_err_fp32_gpu": abs(ng32 - nc) / abs(nc),
+                   "kind": "the oracle's FP64 hand-written adjoint (numpy), itself pinned to oracle FD in tests"}
+    if rank != 0:
+        return
+    # forward step: interaction, spread (zero + spread), loss sum, flow step (sweep, load, column
+    # convolution, C2R, curl); reverse step adds curl^T, the 3-pass solve, the reverse sweep, the
+    # partial sum, the IB transpose and interpolation^T after the 8-kernel recompute
+    launches_fwd = 9 * n_steps
+    launches_bwd = (8 + 8) * n_steps
+    out = {
+        "metric": "adjoint steps/s (drag gradient through the 2D cylinder step; adjoint step / forward step)",
+        "value": round(1e3 / bwd_step, 1), "unit": "adjoint steps/s", "n_gpus": world,
+        "steps": reps * n_steps, "warmup": args.warmup, "ms_per_step": round(bwd_step, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "2D 256x512 fp32 cylinder flow (D=0.1 at (0.25,0.25), 96 markers, K=-5e4, C=-20, "
+                               "U=1, Re=200 on D), tangential wall velocity U[0,0.2] per marker (seed 42); "
+                               "loss = drag integrated over the steps with the dt sequence frozen",
+                   "steps_per_gradient": n_steps, "checkpoint_every": ck, "params": int(V.size) + 1,
+                   "l2": "no flush: every step reads and writes the whole working set"},
+        "forward_ms_per_step": round(fwd_step, 5),
+        "adjoint_ms_per_step": round(bwd_step, 5),
+        "adjoint_over_forward": round(bwd_step / fwd_step, 3),
+        "plain_dropin_forward_ms_per_step": round(plain_step, 5),
+        "adjoint_over_plain_forward": round(bwd_step / plain_step, 3),
+        "e2e": {"value": round(n_steps / e2e_s, 1), "unit": "forward+adjoint steps/s",
+                "h2d_bytes_per_step": round(V.size * 8 / n_steps, 3),
+                "d2h_bytes_per_step": round((V.size + 1) * 8 / n_steps, 3),
+                "note": "loss.backward() through time_integrated_body_force, V from pinned host memory, "
+                        "dL/dV and dL/dnu read back; graphs already captured"},
+        "gpu_launches": reps * (launches_fwd + launches_bwd),
+        "loss": {"fp32": L32, "fp64": L64},
+        "grad_fp32_vs_fp64_rel_l2": rel(g32n, g64n),
+        "nu_grad": {"fp32": n32, "fp64": n64},
+        "finite_differences_fp64_gpu": fd,
+        "cpu_reference_gradient": cpu_ref,
+        "clocks": clock_info,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def accuracy_vs_fp64(wl, device, steps):
     """Relative L2 of the fp32 GPU path against the same path in fp64 after `steps` steps."""
     import torch
@@ -657,7 +868,10 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rod128", choices=["rod128", "cylinder2d", "carpet256", "batch64"])
+    ap.add_argument("--workload", default="rod128",
+                    choices=["rod128", "cylinder2d", "carpet256", "batch64", "adjoint2d"])
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--adjoint-cpu-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--skip-cpu", action="store_true")
@@ -666,6 +880,9 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.workload == "batch64":
         run_batch(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
+        return
+    if args.workload == "adjoint2d":
+        run_adjoint(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
         return
     wl = make_workload(args.workload)
     world = int(os.environ.get("WORLD_SIZE", "1"))

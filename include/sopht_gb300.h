@@ -270,6 +270,93 @@ int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag,
 int sg_ib_mismatch_step(int dtype, int n, void* position_mismatch,
                         const void* velocity_mismatch, double dt, void* stream);
 
+/* ------------------------------------------------------------- adjoints */
+/* Transposes of the 2D step's operators and of the virtual-boundary
+ * coupling, for gradients of time-integrated body forces.  The reference has
+ * no adjoint; each entry names the forward operator it transposes.  The ENO3
+ * upwind branch of each face is held at its forward choice.  All adjoint
+ * kernels are gathers without atomics (bitwise reproducible).  `*_bar` arrays
+ * have the layout of the forward quantity they are the adjoint of. */
+
+/* Number of doubles a `partials` buffer needs for the 2D adjoint entries
+ * (one per 32 x 8 tile; the fused reverse sweep needs fewer). */
+int64_t sg_adj_partials_count_2d(int ny, int nx);
+/* acc[0] += sum(partials[0:n]) in a fixed order (device pointers). */
+int sg_sum_partials(int64_t n, const double* partials, double* acc, void* stream);
+
+/* Transpose of outplane_field_curl_2d.py (sg_outplane_curl_2d):
+ * psi_bar = curl^T(curl_bar); the free stream adds no term. */
+int sg_outplane_curl_adj_2d(int dtype, int ny, int nx, const void* curl_bar, void* psi_bar,
+                            double prefactor, void* stream);
+/* Transpose of penalise_field_boundary_2d.py (sg_penalise_2d), same tables. */
+int sg_penalise_adj_2d(int dtype, int ny, int nx, const void* in_bar, void* out_bar, int width,
+                       const void* cx, const void* cy, void* stream);
+/* Transpose of diffusion_timestep_2d.py (sg_diffusion_step_2d with prefactor k):
+ * out_bar = in_bar + k lap^T(m in_bar).  With `field` (the forward input) and
+ * `partials`, per-tile partials of sum m lap(field) in_bar (= d loss / d k) are
+ * written; reduce them with sg_sum_partials. */
+int sg_diffusion_adj_2d(int dtype, int ny, int nx, const void* in_bar, void* out_bar, double k,
+                        const void* field, double* partials, void* stream);
+/* Transpose of the linearised advection_timestep_2d.py / advection_flux_2d.py
+ * (sg_advection_eno3_step_2d) at (field, velocity):
+ * out_bar = in_bar + (d flux / d field)^T in_bar, and velocity_bar (2, ny, nx)
+ * += (d flux / d velocity)^T in_bar when not NULL. */
+int sg_advection_eno3_adj_2d(int dtype, int ny, int nx, const void* field, const void* velocity,
+                             double dt_by_dx, const void* in_bar, void* out_bar, void* velocity_bar,
+                             void* stream);
+/* Transpose of update_vorticity_from_velocity_forcing_2d.py
+ * (sg_forcing_curl_update_2d): forcing_bar (2, ny, nx) += p curl^T(in_bar);
+ * the vorticity adjoint passes through unchanged. */
+int sg_forcing_curl_adj_2d(int dtype, int ny, int nx, const void* in_bar, void* forcing_bar,
+                           double prefactor, void* stream);
+/* Transpose of UnboundedPoissonSolverPYFFTW{2,3}D.solve (sg_poisson_solve).
+ * The domain-doubled convolution with a real, even Green's function is
+ * symmetric, so this is the same solve. */
+int sg_poisson_solve_adj(sg_poisson_plan plan, const void* sol_bar, void* rhs_bar, int ncomp,
+                         int64_t comp_stride, void* stream);
+/* The Poisson plan owned by a flow plan (valid while the flow plan lives). */
+sg_poisson_plan sg_flow_poisson_plan(sg_flow_plan plan);
+
+/* Arm a one-shot tape for the next 2D sg_flow_step: the vorticity after the
+ * forcing curl and after the advection update are written to the two
+ * buffers (ny, nx).  Both NULL disarms. */
+int sg_flow_set_tape(sg_flow_plan plan, void* w_after_forcing, void* w_after_advection);
+/* Transpose of one 2D step's sweep chain (forcing curl, ENO3 advection,
+ * diffusion, penalisation) in one pass, given the adjoint of the vorticity
+ * after the step (w_bar_after, plus poisson_bar when not NULL) and the step's
+ * tape and velocity.  Writes w_bar_before, velocity_bar (advection part,
+ * overwritten), forcing_bar (overwritten, may be NULL) and, when
+ * w_after_advection is given, viscosity partials (d loss / d diffusion
+ * prefactor, reduce with sg_sum_partials).  `scalars` are the forward step's
+ * host scalars. */
+int sg_ns2d_reverse_sweep(sg_flow_plan plan, const void* w_bar_after, const void* poisson_bar,
+                          const void* w_after_forcing, const void* w_after_advection,
+                          const void* velocity, const sg_step_scalars* scalars, void* w_bar_before,
+                          void* velocity_bar, void* forcing_bar, double* partials, void* stream);
+/* Transpose of one virtual-boundary call (VirtualBoundaryForcing.py:132-185,
+ * 232-283 with the spreading of EulerianLagrangianGridCommunicator{2,3}D):
+ * F_bar = spread^T(eul_forcing_bar) + lag_forcing_bar_const[d] (host, may be
+ * NULL); position_mismatch_bar += K F_bar; dU_bar = C F_bar +
+ * velocity_mismatch_bar_carry; body_velocity_bar (device float64) -= dU_bar;
+ * flow_velocity_bar = dx^dim dU_bar; then velocity_mismatch_bar_carry =
+ * xi_dt * position_mismatch_bar (the transpose of time_step(xi_dt) before the
+ * call).  nearest and weights are those of the forward call. */
+int sg_ib_interaction_adj(int dtype, int dim, int nz, int ny, int nx, double dx, int n_lag,
+                          const int32_t* nearest, const void* weights, const void* eul_forcing_bar,
+                          const double* lag_forcing_bar_const, double stiffness, double damping,
+                          double xi_dt, void* position_mismatch_bar,
+                          void* velocity_mismatch_bar_carry, double* body_velocity_bar,
+                          void* flow_velocity_bar, void* stream);
+/* Transpose of the Eulerian-to-Lagrangian interpolation
+ * (eulerian_to_lagrangian_grid_interpolation_kernel): eul_velocity_bar +=
+ * sum_i phi_i flow_velocity_bar_i (deterministic spreading). */
+int sg_ib_interp_adj(int dtype, int dim, int nz, int ny, int nx, int n_lag,
+                     const int32_t* nearest, const void* weights, const void* flow_velocity_bar,
+                     void* eul_velocity_bar, void* stream);
+/* acc[0] (device double) += sum_d weights3[d] sum_i lag_field[d, i] (fixed order). */
+int sg_lag_weighted_sum(int dtype, int dim, int n_lag, const void* lag_field,
+                        const double* weights3, double* acc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,6 +90,27 @@ _SIGNATURES = {
     "sg_ib_spread": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_int, c_void_p]),
     "sg_ib_mismatch_step": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    # adjoints
+    "sg_adj_partials_count_2d": (c_int64, [c_int, c_int]),
+    "sg_sum_partials": (c_int, [c_int64, c_void_p, c_void_p, c_void_p]),
+    "sg_outplane_curl_adj_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_penalise_adj_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "sg_diffusion_adj_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
+                                    c_void_p]),
+    "sg_advection_eno3_adj_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
+                                         c_void_p, c_void_p]),
+    "sg_forcing_curl_adj_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_poisson_solve_adj": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int64, c_void_p]),
+    "sg_flow_poisson_plan": (c_void_p, [c_void_p]),
+    "sg_flow_set_tape": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "sg_ns2d_reverse_sweep": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_ib_interaction_adj": (c_int, [c_int, c_int, c_int, c_int, c_int, c_double, c_int, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_double, c_double, c_double, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p]),
+    "sg_ib_interp_adj": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p]),
+    "sg_lag_weighted_sum": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "sg_batch2d_create": (c_int, [c_int, POINTER(Batch2DMember), POINTER(c_void_p)]),
     "sg_batch2d_set_tuning": (c_int, [c_void_p, c_int, c_int]),
     "sg_batch2d_step": (c_int, [c_void_p, c_void_p]),

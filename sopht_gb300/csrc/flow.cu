@@ -185,6 +185,8 @@ int flow_step_2d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
     s.out = (T*)p->scratch_a;
     s.sc = sc;
     s.flags = SWEEP_ADVECT | SWEEP_DIFFUSE;
+    s.tape_w1 = (T*)p->tape_w1;
+    s.tape_w2 = (T*)p->tape_w2;
     mark(p, 0, stream);
     SG_TRY(launch_sweep2d<T>(s, stream));
     mark(p, 1, stream);
@@ -420,6 +422,16 @@ extern "C" int sg_flow_set_timing_events(sg_flow_plan p, int n_events, void* con
     return SG_OK;
 }
 
+extern "C" int sg_flow_set_tape(sg_flow_plan p, void* w_after_forcing, void* w_after_advection) {
+    SG_REQUIRE(p, SG_ERR_INVALID_ARG, "tape: null plan");
+    SG_REQUIRE(p->dim == 2, SG_ERR_UNSUPPORTED, "tape: only the 2D step records a tape");
+    SG_REQUIRE((w_after_forcing == nullptr) == (w_after_advection == nullptr), SG_ERR_INVALID_ARG,
+               "tape: give both buffers or neither");
+    p->tape_w1 = w_after_forcing;
+    p->tape_w2 = w_after_advection;
+    return SG_OK;
+}
+
 extern "C" int sg_flow_prime_max(sg_flow_plan p, const void* velocity, void* stream_) {
     SG_REQUIRE(p && velocity, SG_ERR_INVALID_ARG, "prime max: null argument");
     auto stream = (cudaStream_t)stream_;
@@ -460,7 +472,8 @@ extern "C" int sg_flow_step(sg_flow_plan p, void* w, void* u, void* f, void* psi
         st = p->dim == 2 ? flow_step_2d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream)
                          : flow_step_3d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream);
     }
-    p->n_events = 0;  // timing events are armed for one step only
+    p->n_events = 0;  // timing events and the tape are armed for one step only
+    p->tape_w1 = p->tape_w2 = nullptr;
     return st;
 }
 

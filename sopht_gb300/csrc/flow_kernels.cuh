@@ -40,6 +40,8 @@ template <typename T> struct Sweep2DParams {
     T* out;
     ScalarSrc sc;
     int flags;    // SWEEP_ADVECT | SWEEP_DIFFUSE
+    T* tape_w1;   // optional: w1 (after the forcing curl) on the tile, for the adjoint
+    T* tape_w2;   // optional: w2 (after advection)
 };
 
 template <typename T>
@@ -149,6 +151,10 @@ __device__ __forceinline__ void sweep2d_body(const Sweep2DParams<T>& p, int bx, 
             w3 = w3 + k * lap;
         }
         p.out[(int64_t)gy * nx + gx] = w3;
+        if (p.tape_w1) {
+            p.tape_w1[(int64_t)gy * nx + gx] = s_w1[(ly + HW) * WX + (lx + HW)];
+            p.tape_w2[(int64_t)gy * nx + gx] = s_w2[c];
+        }
     }
 }
 

@@ -23,6 +23,9 @@ struct sg_flow_plan_s {
     // optional one-shot timing events recorded between the passes of the next step
     int n_events = 0;
     cudaEvent_t events[16] = {};
+    // optional one-shot tape of the next 2D step's sweep intermediates (adjoint)
+    void* tape_w1 = nullptr;
+    void* tape_w2 = nullptr;
     sg_step_scalars* dev_scalars() const { return reinterpret_cast<sg_step_scalars*>(dev_block); }
     void* umax_slot() const { return dev_block + 64; }
     double* time_slot() const { return reinterpret_cast<double*>(dev_block + 72); }

@@ -1,5 +1,6 @@
 """Flow simulators and immersed-body coupling (sopht.simulator counterparts)."""
 
+from .adjoint import BodyForceObjective2D, time_integrated_body_force
 from .batch import BatchedFlowSimulator2D
 from .flow import (
     FlowSimulator,
@@ -23,6 +24,7 @@ from .immersed_body import (
 
 __all__ = [
     "BatchedFlowSimulator2D",
+    "BodyForceObjective2D",
     "CircularCylinderForcingGrid",
     "CosseratRodElementCentricForcingGrid",
     "CosseratRodFlowInteraction",
@@ -38,4 +40,5 @@ __all__ = [
     "UnboundedNavierStokesFlowSimulator3D",
     "create_unbounded_flow_simulator_2d",
     "create_unbounded_flow_simulator_3d",
+    "time_integrated_body_force",
 ]
