@@ -54,8 +54,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "flow steps/s & Gcell-updates/s vs plain GPU path at stated FP64-oracle L2 error"
 
 # algorithmic bytes per cell per pass of the fp32 step (read + write)
-PASSES_3D = {"forcing_curl": 36, "uxw_update": 36, "diffusion": 24, "poisson_load": 60, "y_fft": 72,
-             "z_conv": 108, "y_ifft": 72, "x_c2r": 36, "curl": 24}
+PASSES_3D = {"stencils": 96, "poisson_load": 60, "y_fft": 72, "z_conv": 108, "y_ifft": 72, "x_c2r": 36, "curl": 24}
 PASSES_2D = {"sweep": 24, "poisson_load": 32, "y_conv": 20, "x_c2r": 12, "curl": 12}
 
 
@@ -72,6 +71,15 @@ class RodState:
         self.mass[[0, -1]] *= 0.5
         self.lengths = np.full(n_elem, length / n_elem)
         self.director_collection = np.repeat(np.eye(3)[:, :, None], n_elem, axis=2)
+        self.base = np.asarray(base, dtype=np.float64)
+        self.s = s
+
+    def set_pose(self, theta, theta_dot):
+        """Rigid rotation about the base, in the x-z plane, by theta (rad) at rate theta_dot."""
+        d = np.array([np.sin(theta), 0.0, np.cos(theta)])
+        dd = np.array([np.cos(theta), 0.0, -np.sin(theta)]) * theta_dot
+        self.position_collection[...] = self.base[:, None] + np.outer(d, self.s)
+        self.velocity_collection[...] = np.outer(dd, self.s)
 
 
 @dataclass
@@ -88,6 +96,8 @@ class Workload:
     x_range: float = 1.0
     cfl: float = 0.1
     n_markers: int = 96
+    actuation: dict = None         # rods: {"amplitude", "frequency", "phases"} of a sinusoidal base rotation
+    accuracy_checkpoints: tuple = (1, 10, 100)
 
     @property
     def dim(self):
@@ -129,13 +139,14 @@ def make_workload(name: str) -> Workload:
                   "element-centric cosine-delta forcing), U=1 inflow, Re=100 on rod length, CFL 0.1",
             (128, 128, 128), 1.0 * length / 100.0, np.array([1.0, 0.0, 0.0]), "rods",
             bodies=[dict(base=(0.5, 0.5, 0.5 - length / 2), length=length, radius=0.01, n_elem=64)],
-            K=-2e4, C=-1e2)
+            K=-2e4, C=-1e2, accuracy_checkpoints=(1, 10, 100, 500))
     if name == "cylinder2d":
         return Workload(
             name, "2D unbounded vorticity NS 256x512 fp32, cylinder D=0.1 at (0.25, 0.25), 96 markers, "
                   "U=1, Re=200 on the diameter, CFL 0.1",
             (256, 512), 1.0 * 0.1 / 200.0, np.array([1.0, 0.0]), "cylinder",
-            bodies=[dict(centre=(0.25, 0.25, 0.0), radius=0.05)], K=-5e4, C=-20.0, n_markers=96)
+            bodies=[dict(centre=(0.25, 0.25, 0.0), radius=0.05)], K=-5e4, C=-20.0, n_markers=96,
+            accuracy_checkpoints=(1, 10, 100, 1000))
     if name == "carpet256":
         n = 256
         dx = 1.0 / n
@@ -145,10 +156,14 @@ def make_workload(name: str) -> Workload:
             for j in range(4):
                 bodies.append(dict(base=(0.3 + 0.13 * i, 0.3 + 0.13 * j, 6 * dx), length=length,
                                    radius=0.005, n_elem=100))
+        phases = np.random.default_rng(42).uniform(0.0, 2 * np.pi, len(bodies))
         return Workload(
-            name, "3D unbounded vorticity NS 256^3 fp32 (512^3 doubled FFT), 4x4 carpet of 16 clamped rods "
-                  "(100 elements each, one interactor per rod), U=1 along x, Re=500 on rod length, CFL 0.1",
-            (n, n, n), 1.0 * length / 500.0, np.array([1.0, 0.0, 0.0]), "rods", bodies=bodies, K=-2e4, C=-1e2)
+            name, "3D unbounded vorticity NS 256^3 fp32 (512^3 doubled FFT), 4x4 carpet of 16 rods (100 elements "
+                  "each, one interactor per rod) clamped at z0 = 6 dx with a sinusoidal base rotation (frequency 1, "
+                  "amplitude 0.2 rad, seeded phases), U=1 along x, Re=500 on rod length, CFL 0.1",
+            (n, n, n), 1.0 * length / 500.0, np.array([1.0, 0.0, 0.0]), "rods", bodies=bodies, K=-2e4, C=-1e2,
+            actuation={"amplitude": 0.2, "frequency": 1.0, "phases": phases},
+            accuracy_checkpoints=tuple(range(20, 201, 20)))
     raise ValueError(f"unknown workload {name}")
 
 
@@ -231,8 +246,19 @@ def make_gpu_case(wl: Workload, real_t, device):
     return sim, inters
 
 
+def actuate(wl, inters, t):
+    """Prescribed base rotation of every rod at time t (the host body update of a coupled loop)."""
+    if not wl.actuation:
+        return
+    a, f = wl.actuation["amplitude"], wl.actuation["frequency"]
+    for inter, phi in zip(inters, wl.actuation["phases"], strict=True):
+        w = 2 * np.pi * f
+        inter.forcing_grid.cosserat_rod.set_pose(a * np.sin(w * t + phi), a * w * np.cos(w * t + phi))
+
+
 def public_api_step(wl, sim, inters):
     """One coupled step through the drop-in API (the reference example loops' order)."""
+    actuate(wl, inters, sim.time)
     dt = sim.compute_stable_timestep()
     for inter in inters:
         inter.time_step(dt=dt)
@@ -284,10 +310,16 @@ def run_gpu(args, wl: Workload, rank, world):
             for e in ev_list:
                 e.record(stream)
     torch.cuda.synchronize()
+    # the timed graph has no timing nodes; a second, instrumented graph of the same steps gives
+    # the per-pass breakdown (event nodes between the passes add a little time of their own)
     graph = torch.cuda.CUDAGraph()
+    graph_inst = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
         stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.graph(graph, stream=stream):
+            for _ in range(seg):
+                device_step(wl, sim, inters)
+        with torch.cuda.graph(graph_inst, stream=stream):
             for k in range(seg):
                 device_step(wl, sim, inters, events[k])
     torch.cuda.synchronize()
@@ -317,6 +349,9 @@ def run_gpu(args, wl: Workload, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed_ms = float(t.item())
         torch.distributed.barrier()
+    with torch.cuda.stream(stream):
+        graph_inst.replay()
+    torch.cuda.synchronize()
     cells = wl.cells
     kernels = {}
     for i, name in enumerate(pass_names):
@@ -324,6 +359,8 @@ def run_gpu(args, wl: Workload, rank, world):
         ms = float(np.mean(vals))
         kernels[name] = {"ms": round(ms, 5), "GB_s": round(wl.passes[name] * cells / (ms * 1e-3) / 1e9, 1),
                          "launches_timed": len(vals)}
+    graph_inst.reset()
+    del graph_inst
     value = world * steps / (elapsed_ms * 1e-3)
     graph.reset()
     del graph
@@ -351,7 +388,8 @@ def run_gpu(args, wl: Workload, rank, world):
 
     accuracy = None
     if rank == 0 and not args.skip_accuracy:
-        accuracy = accuracy_vs_fp64(wl, device, min(steps, args.accuracy_steps))
+        accuracy = accuracy_checkpoints(wl, device, [c for c in wl.accuracy_checkpoints if c <= args.accuracy_steps],
+                                        cpu_oracle=(wl.dim == 2 and not args.skip_cpu))
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = run_cpu_sample(wl, args.cpu_seconds)
@@ -376,7 +414,9 @@ def run_gpu(args, wl: Workload, rank, world):
         "gcell_updates_per_s": round(world * cells * steps / (elapsed_ms * 1e-3) / 1e9, 3),
         "config": {"workload": wl.description, "name": wl.name, "grid": list(wl.grid),
                    "dt_rule": "compute_stable_timestep, CFL 0.1", "bodies": len(wl.bodies),
-                   "body_kinematics": "clamped/fixed pose on the host; body integrator not timed",
+                   "body_kinematics": ("sinusoidal base rotation on the host in e2e and the accuracy run; initial "
+                                       "pose in the device-resident graph" if wl.actuation else
+                                       "clamped/fixed pose on the host; body integrator not timed"),
                    "parallelism": "replicas only" if world > 1 else "single GPU",
                    "l2": "no flush: the step working set exceeds the 126 MB L2" if cells * 4 * 20 > 126e6 else
                          "working set fits in L2 (launch-latency-bound size)"},
@@ -521,7 +561,7 @@ def run_batch(args, rank, world):
         "gcell_updates_per_s": round(world * cells * steps / (batch_ms * 1e-3) / 1e9, 3),
         "config": {"workload": "batch of 64 2D cylinder flows, grids drawn from {128x256, 256x512, 384x768, "
                                "512x1024}, Re ~ U[50, 400], centre jitter U[-0.02, 0.02]^2, seed 42",
-                   "instances": n, "total_cells": cells, "autotuned": {"sweep_tile_y": best[0],
+                   "instances": n, "total_cells": cells, "autotuned": {"sweep_tile_y": best[0], "fft_threads": best[2],
                                                                         "blocks_per_sm": best[1]}},
         "sequential_plain_gpu": {"value": round(sequential_rate, 1), "unit": "instance-steps/s",
                                  "note": f"each instance alone, device-dt coupled step in a CUDA graph of "
@@ -745,28 +785,49 @@ def run_adjoint(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def accuracy_vs_fp64(wl, device, steps):
-    """Relative L2 of the fp32 GPU path against the same path in fp64 after `steps` steps."""
+def accuracy_checkpoints(wl, device, checkpoints, cpu_oracle=False):
+    """Relative L2 of the fp32 GPU path against the same path in FP64 on the GPU (and, in 2D, the FP64
+    CPU oracle) at the checkpoint steps.  All runs take the FP64 GPU run's dt sequence, so the errors
+    measure arithmetic precision only."""
     import torch
-    fields = {}
-    for rt in (np.float32, np.float64):
-        sim, inters = make_gpu_case(wl, rt, device)
-        for _ in range(steps):
-            dt = sim.compute_stable_timestep()
+    if not checkpoints:
+        return None
+    runs = {rt: make_gpu_case(wl, rt, device) for rt in (np.float32, np.float64)}
+    orc = make_cpu_case(wl, np.float64) if cpu_oracle else None
+    out = {"checkpoints": [], "fp64_reference": "this path in FP64 on the GPU (validated against the CPU oracle "
+                                                "in tests)" + ("; plus the FP64 CPU oracle" if orc else "")}
+    t = 0.0
+    for step in range(1, max(checkpoints) + 1):
+        dt = float(runs[np.float64][0].compute_stable_timestep())
+        for rt, (sim, inters) in runs.items():
+            actuate(wl, inters, t)
             for inter in inters:
                 inter.time_step(dt=dt)
                 inter()
             sim.time_step(dt=dt, free_stream_velocity=wl.u_inf)
-        torch.cuda.synchronize()
-        fields[rt] = (sim.vorticity_field.double().cpu().numpy(), sim.velocity_field.double().cpu().numpy())
-        del sim, inters
-    res = {}
-    for i, name in enumerate(("vorticity", "velocity")):
-        a, b = fields[np.float32][i], fields[np.float64][i]
-        res[f"{name}_rel_l2_vs_fp64"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    res["steps"] = steps
-    res["fp64_reference"] = "this path in FP64 on the GPU (validated against the CPU oracle in tests)"
-    return res
+        if orc:
+            osim, ointers = orc
+            for inter in ointers:
+                inter.time_step(dt)
+                inter()
+            osim.time_step(dt, wl.u_inf)
+        t += dt
+        if step in checkpoints:
+            torch.cuda.synchronize()
+            f = {rt: (sim.vorticity_field.double().cpu().numpy(), sim.velocity_field.double().cpu().numpy())
+                 for rt, (sim, _) in runs.items()}
+            row = {"step": step}
+            for i, name in enumerate(("vorticity", "velocity")):
+                a, b = f[np.float32][i], f[np.float64][i]
+                row[f"{name}_rel_l2_fp32_vs_fp64_gpu"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+                if orc:
+                    ref = (orc[0].vorticity_field, orc[0].velocity_field)[i]
+                    row[f"{name}_rel_l2_fp32_vs_fp64_oracle"] = float(np.linalg.norm(a - ref) / np.linalg.norm(ref))
+                    row[f"{name}_rel_l2_fp64_gpu_vs_fp64_oracle"] = float(np.linalg.norm(b - ref) /
+                                                                          np.linalg.norm(ref))
+            out["checkpoints"].append(row)
+    del runs
+    return out
 
 
 def load_peaks():
@@ -793,7 +854,7 @@ def traffic_from_profiles(workload, kernel):
 # ------------------------------------------------------------ CPU (oracle)
 
 
-def make_cpu_case(wl: Workload):
+def make_cpu_case(wl: Workload, real_t=np.float32):
     from oracle.flow import (
         CircularCylinderOracle,
         ImmersedBodyInteractionOracle,
@@ -801,7 +862,7 @@ def make_cpu_case(wl: Workload):
         NavierStokes3DOracle,
         RodElementCentricGridOracle,
     )
-    rt = np.float32
+    rt = real_t
     Sim = NavierStokes2DOracle if wl.dim == 2 else NavierStokes3DOracle
     sim = Sim(wl.grid, wl.x_range, wl.nu, cfl=wl.cfl, real_t=rt, with_forcing=True, with_free_stream_flow=True)
     sim.vorticity_field[...] = wl.initial_vorticity(rt)
@@ -873,7 +934,7 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-cpu-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     args = ap.parse_args()

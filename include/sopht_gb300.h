@@ -116,8 +116,9 @@ int64_t sg_flow_plan_bytes(sg_flow_plan plan);
  * cudaEvent_t handles that the next sg_flow_step records between its passes,
  * event i before pass i and the last one after the final pass.  2D passes:
  * sweep, Poisson load, column convolution, row C2R, curl (6 events).  3D
- * passes: forcing curl, u x w update, diffusion(+filter), Poisson load, y FFT,
- * z convolution, y IFFT, x C2R, curl (10 events).  One-shot. */
+ * passes: stencils (forcing curl, u x w update, diffusion; + filter),
+ * Poisson load, y FFT, z convolution, y IFFT, x C2R, curl (8 events).
+ * One-shot. */
 int sg_flow_set_timing_events(sg_flow_plan plan, int n_events, void* const* events);
 
 /* One flow time step, in place on the caller's fields.  Replaces
@@ -177,10 +178,11 @@ typedef struct sg_batch2d_member {
 } sg_batch2d_member;
 int sg_batch2d_create(int n, const sg_batch2d_member* members, sg_batch2d* batch_out);
 /* Tuning knobs (picked by the Python autotuner): sweep tile height 8 or 16;
- * persistent blocks per SM (0 = one block per work item). */
-int sg_batch2d_set_tuning(sg_batch2d batch, int sweep_tile_y, int blocks_per_sm);
+ * persistent blocks per SM (0 = one block per work item); block size of the
+ * FFT passes, 256 or 512 threads (512: twice the lines per work item). */
+int sg_batch2d_set_tuning(sg_batch2d batch, int sweep_tile_y, int blocks_per_sm, int fft_threads);
 /* One coupled step of every member (8 launches).  Each member's velocity max
- * must be primed once with sg_flow_device_dt before the first step. */
+ * must be primed once (sg_flow_prime_max) before the first step. */
 int sg_batch2d_step(sg_batch2d batch, void* stream);
 int sg_batch2d_destroy(sg_batch2d batch);
 

@@ -45,8 +45,9 @@ template <int N> struct FastElems {
     static constexpr int E = (N % 3 == 0) ? 24 : 16;
 };
 
-template <int N, int W> struct FastShape {
-    static constexpr int E = FastElems<N>::E;
+
+template <int N, int W, int E_ = FastElems<N>::E> struct FastShape {
+    static constexpr int E = E_;
     static constexpr int NT = N * W / E;
     static constexpr int LS = W + 1;
     static_assert(NT >= 32 && NT <= 1024 && NT % 32 == 0, "block size must be whole warps");
@@ -66,21 +67,83 @@ SG_FAST_WIDTH(384, 16, 2)
 SG_FAST_WIDTH(768, 8, 1)
 #undef SG_FAST_WIDTH
 
-template <int N, int S, int NS, bool INV, int W, int LS, int NT, typename C>
-__device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid) {
+// Elements per thread of the standalone kernels (E must be a multiple of every
+// radix of N's schedule; radix-3 lengths keep 24).  Measured on GB300: the row
+// kernels (x R2C, flow load, x C2R) run faster with E = 8 (twice the threads,
+// half the registers) at every power-of-two length; the strided line kernels
+// run faster with E = 8 only at their narrow width, and with E = 16 at the
+// wide one, where E = 8 lost 10-15 % at N = 256 and 512.
+template <int N, int W> struct FastPickRows {
+    static constexpr int E = (N % 3 == 0) ? 24 : ((N * W / 8 <= 1024) ? 8 : 16);
+};
+template <int N, int W> struct FastPickLines {
+    static constexpr int E = (N % 3 == 0) ? 24 : ((W == FastWidth<N>::narrow && N * W / 8 >= 32) ? 8 : 16);
+};
+
+// Length-R DFT of inputs whose upper half (v[R/2 .. R-1]) is zero, for the
+// even radices.  Same operations as dft_r without the additions of zero, so
+// every non-zero result is bitwise the same.
+template <int R, bool INV, typename C> __device__ __forceinline__ void dft_r_half_in(C* v) {
+    auto rot = [](C e) { return INV ? cmake<C>(-e.y, e.x) : cmake<C>(e.y, -e.x); };  // dft4's d
+    if constexpr (R == 2) {
+        v[1] = v[0];
+    } else if constexpr (R == 4) {
+        const C x0 = v[0], x1 = v[1];
+        v[0] = cadd(x0, x1);
+        v[1] = cadd(x0, rot(x1));
+        v[2] = csub(x0, x1);
+        v[3] = csub(x0, rot(x1));
+    } else {
+        static_assert(R == 8, "half-input DFT for radices 2, 4, 8");
+        using T = typename Cx<C>::T;
+        const C e0 = v[0], e1 = v[2], o0 = v[1], o1 = v[3];
+        C E0 = cadd(e0, e1), E1 = cadd(e0, rot(e1)), E2 = csub(e0, e1), E3 = csub(e0, rot(e1));
+        C O0 = cadd(o0, o1), O1 = cadd(o0, rot(o1)), O2 = csub(o0, o1), O3 = csub(o0, rot(o1));
+        const T r = T(0.70710678118654752440);
+        const C w1 = INV ? cmake<C>(r, r) : cmake<C>(r, -r);
+        const C w3 = INV ? cmake<C>(-r, r) : cmake<C>(-r, -r);
+        O1 = cmul(O1, w1);
+        O2 = INV ? cmake<C>(-O2.y, O2.x) : cmake<C>(O2.y, -O2.x);
+        O3 = cmul(O3, w3);
+        v[0] = cadd(E0, O0); v[4] = csub(E0, O0);
+        v[1] = cadd(E1, O1); v[5] = csub(E1, O1);
+        v[2] = cadd(E2, O2); v[6] = csub(E2, O2);
+        v[3] = cadd(E3, O3); v[7] = csub(E3, O3);
+    }
+}
+
+struct IdentityPost {
+    template <typename C> __device__ __forceinline__ C operator()(int, C v) const { return v; }
+};
+
+// The first stage reads points j + r N/R: with HIN (points N/2 .. N-1 zero,
+// an even first radix) the upper half is neither read nor summed.  The last
+// stage writes point base + r N/R: with HOUT (only points < N/2 wanted, an even
+// last radix) the upper half is not written.  `post(k, v)` is applied to every
+// value the last stage writes (point k of the thread's line).
+template <int N> struct FastEnds {
+    static constexpr bool first_even = sched_radix(N, 0) % 2 == 0;
+    static constexpr bool last_even = sched_radix(N, sched_count(N) - 1) % 2 == 0;
+};
+
+template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, typename C, typename Post>
+__device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid, const Post& post) {
     constexpr int R = sched_radix(N, S);
     constexpr int NB = N / R;
     constexpr int TOT = NB * W;
     static_assert(TOT % NT == 0, "butterflies must divide evenly over the block");
     constexpr int PER = TOT / NT;
     constexpr int TSTRIDE = N / (NS * R);
+    constexpr bool LAST = S == sched_count(N) - 1;
+    constexpr bool SKIP_IN = HIN && S == 0 && R % 2 == 0;
+    constexpr bool SKIP_OUT = HOUT && LAST && R % 2 == 0;
     C v[PER][R];
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int t = tid + b * NT;
         const int line = t % W, j = t / W;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[b][r] = buf[(j + r * NB) * LS + line];
+        for (int r = 0; r < (SKIP_IN ? R / 2 : R); ++r) v[b][r] = buf[(j + r * NB) * LS + line];
     }
     __syncthreads();
 #pragma unroll
@@ -96,27 +159,34 @@ __device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid) {
                 v[b][r] = cmul(v[b][r], w);
             }
         }
-        dft_r<R, INV>(v[b]);
+        if constexpr (SKIP_IN) dft_r_half_in<R, INV>(v[b]);
+        else dft_r<R, INV>(v[b]);
         const int base = (j / NS) * NS * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) buf[(base + r * NS) * LS + line] = v[b][r];
+        for (int r = 0; r < (SKIP_OUT ? R / 2 : R); ++r) {
+            C o = v[b][r];
+            if constexpr (LAST) o = post(base + r * NS, o);
+            buf[(base + r * NS) * LS + line] = o;
+        }
     }
     __syncthreads();
 }
 
-template <int N, int S, int NS, bool INV, int W, int LS, int NT, typename C>
-__device__ __forceinline__ void fast_stages(C* buf, const C* tw, int tid) {
+template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, typename C, typename Post>
+__device__ __forceinline__ void fast_stages(C* buf, const C* tw, int tid, const Post& post) {
     if constexpr (S < sched_count(N)) {
-        fast_stage<N, S, NS, INV, W, LS, NT>(buf, tw, tid);
-        fast_stages<N, S + 1, NS * sched_radix(N, S), INV, W, LS, NT>(buf, tw, tid);
+        fast_stage<N, S, NS, INV, W, LS, NT, HIN, HOUT>(buf, tw, tid, post);
+        fast_stages<N, S + 1, NS * sched_radix(N, S), INV, W, LS, NT, HIN, HOUT>(buf, tw, tid, post);
     }
 }
 
 // Whole in-place transform of the W lines in `buf` (ends synchronised).
-template <int N, int W, bool INV, typename C>
-__device__ __forceinline__ void fast_fft(C* buf, const C* tw, int tid) {
-    using S = FastShape<N, W>;
-    fast_stages<N, 0, 1, INV, W, S::LS, S::NT>(buf, tw, tid);
+template <int N, int W, bool INV, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false, typename C,
+          typename Post = IdentityPost>
+__device__ __forceinline__ void fast_fft(C* buf, const C* tw, int tid, const Post& post = Post()) {
+    using S = FastShape<N, W, E>;
+    fast_stages<N, 0, 1, INV, W, S::LS, S::NT, HIN && FastEnds<N>::first_even, HOUT && FastEnds<N>::last_even>(
+        buf, tw, tid, post);
 }
 
 template <typename C>
@@ -125,11 +195,21 @@ __device__ __forceinline__ void stage_table(C* dst, const C* __restrict__ src, i
 }
 
 // ----------------------------------------------------------- strided lines
-template <typename T, int N, int W, int MODE>
-__device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid, unsigned char* smem_raw) {
+// HIN: the points n_in .. N-1 of each line are zero with n_in <= N/2 (the
+// zero padding of the doubled domain), so the upper half is neither loaded nor
+// transformed.  HOUT: only the points < n_out <= N/2 are stored (the crop), so
+// the inverse transform's last stage computes only those.  In LINE_CONV the
+// Green's factor multiplies the forward transform's last-stage outputs in
+// registers.
+// stage_tw = false: the block staged this length's twiddles for an earlier
+// work item (persistent batched kernels) and they are still in shared memory.
+template <typename T, int N, int W, int MODE, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false>
+__device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid, unsigned char* smem_raw,
+                                                bool stage_tw = true) {
     using C = cplx_t<T>;
-    using S = FastShape<N, W>;
+    using S = FastShape<N, W, E>;
     constexpr int LS = S::LS, NT = S::NT, PER = N * W / NT;
+    constexpr bool SKIP_LOAD = HIN && FastEnds<N>::first_even;
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw = buf + N * LS;
     const int tid = threadIdx.x;
@@ -137,10 +217,10 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
     const int outer = bid / chunks;
     const int c0 = (bid % chunks) * W;
     const int wcount = min(W, p.inner - c0);
-    stage_table(tw, p.tw, N, tid, NT);
+    if (stage_tw) stage_table(tw, p.tw, N, tid, NT);
     const C* src = p.in + (int64_t)outer * p.outer_stride + c0;
 #pragma unroll
-    for (int b = 0; b < PER; ++b) {
+    for (int b = 0; b < (SKIP_LOAD ? PER / 2 : PER); ++b) {
         const int e = tid + b * NT;
         const int pt = e / W, w = e % W;
         C v = cmake<C>(T(0), T(0));
@@ -149,32 +229,31 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
     }
     __syncthreads();
     if (MODE == LINE_INV) {
-        fast_fft<N, W, true>(buf, tw, tid);
+        fast_fft<N, W, true, E, false, HOUT>(buf, tw, tid);
+    } else if (MODE == LINE_FWD) {
+        fast_fft<N, W, false, E, HIN, false>(buf, tw, tid);
     } else {
-        fast_fft<N, W, false>(buf, tw, tid);
-        if (MODE == LINE_CONV) {
-            // every element a thread touches has the same line w, so the table
-            // row of that line is computed once
-            const int w = tid % W;
-            const int k0 = tid / W;
-            int64_t gbase = 0;
-            if (w < wcount) {
-                const int inner = c0 + w;
-                const int m = inner / p.g.inner_div;
-                const int kx = inner - m * p.g.inner_div;
-                const int ms = p.g.m_mod > 0 ? min(m, p.g.m_mod - m) : 0;
-                gbase = (int64_t)ms * p.g.m_stride + kx;
-            }
-#pragma unroll
-            for (int b = 0; b < PER; ++b) {
-                const int k = k0 + b * (NT / W);
-                const int ks = min(k, N - k);
-                const T gv = (w < wcount) ? p.g.table[(int64_t)ks * p.g.k_stride + gbase] : T(0);
-                buf[k * LS + w] = cscale(buf[k * LS + w], gv);
-            }
-            __syncthreads();
-            fast_fft<N, W, true>(buf, tw, tid);
+        // every element a thread touches has the same line w, so the table row
+        // of that line is computed once
+        const int w = tid % W;
+        int64_t gbase = 0;
+        if (w < wcount) {
+            const int inner = c0 + w;
+            const int m = inner / p.g.inner_div;
+            const int kx = inner - m * p.g.inner_div;
+            const int ms = p.g.m_mod > 0 ? min(m, p.g.m_mod - m) : 0;
+            gbase = (int64_t)ms * p.g.m_stride + kx;
         }
+        const T* table = p.g.table;
+        const int64_t k_stride = p.g.k_stride;
+        const bool live = w < wcount;
+        auto green = [&](int k, C v) {
+            const int ks = min(k, N - k);
+            const T gv = live ? table[(int64_t)ks * k_stride + gbase] : T(0);
+            return cscale(v, gv);
+        };
+        fast_fft<N, W, false, E, HIN, false>(buf, tw, tid, green);
+        fast_fft<N, W, true, E, false, HOUT>(buf, tw, tid);
     }
     C* dst = p.out + (int64_t)outer * p.outer_stride + c0;
 #pragma unroll
@@ -185,10 +264,10 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
     }
 }
 
-template <typename T, int N, int W, int MODE>
-__global__ void __launch_bounds__(FastShape<N, W>::NT) fast_lines_kernel(LinesParams<T> p) {
+template <typename T, int N, int W, int MODE, int E, bool HIN, bool HOUT>
+__global__ void __launch_bounds__(FastShape<N, W, E>::NT) fast_lines_kernel(LinesParams<T> p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    fast_lines_body<T, N, W, MODE>(p, blockIdx.x, smem_raw);
+    fast_lines_body<T, N, W, MODE, E, HIN, HOUT>(p, blockIdx.x, smem_raw);
 }
 
 // -------------------------------------------------------------- row kernels
@@ -202,11 +281,11 @@ template <int M, int W> struct RowSmem {
     }
 };
 
-template <typename T, int M, int W>
+template <typename T, int M, int W, int E = FastElems<M>::E>
 __device__ __forceinline__ void r2c_post_store(const cplx_t<T>* buf, const cplx_t<T>* tw_l, cplx_t<T>* out,
                                                const int64_t* out_off, int row0, int n_rows, int tid) {
     using C = cplx_t<T>;
-    using S = FastShape<M, W>;
+    using S = FastShape<M, W, E>;
     constexpr int LS = S::LS, NT = S::NT;
     // each row emits M + 1 bins; threads walk bins of one row (coalesced store)
     for (int e = tid; e < W * (M + 1); e += NT) {
@@ -221,11 +300,14 @@ __device__ __forceinline__ void r2c_post_store(const cplx_t<T>* buf, const cplx_
     }
 }
 
-template <typename T, int M, int W>
+// HIN: the row's real input is zero beyond n_in <= M, so the packed complex
+// points M/2 .. M-1 are zero and the first stage skips them.
+template <typename T, int M, int W, int E = FastElems<M>::E, bool HIN = false>
 __device__ __forceinline__ void fast_rows_r2c_body(const RowsR2CParams<T>& p, int bid, unsigned char* smem_raw) {
     using C = cplx_t<T>;
-    using S = FastShape<M, W>;
+    using S = FastShape<M, W, E>;
     constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
+    constexpr bool SKIP_LOAD = HIN && FastEnds<M>::first_even;
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw_m = buf + M * LS;
     C* tw_l = tw_m + M;
@@ -245,6 +327,7 @@ __device__ __forceinline__ void fast_rows_r2c_body(const RowsR2CParams<T>& p, in
     for (int b = 0; b < PER; ++b) {
         const int e = tid + b * NT;
         const int r = e / M, n = e % M;
+        if (SKIP_LOAD && n >= M / 2) continue;
         C z = cmake<C>(T(0), T(0));
         if (row0 + r < p.n_rows) {
             const T* src = p.in + in_off[r];
@@ -254,20 +337,23 @@ __device__ __forceinline__ void fast_rows_r2c_body(const RowsR2CParams<T>& p, in
         buf[n * LS + r] = z;
     }
     __syncthreads();
-    fast_fft<M, W, false>(buf, tw_m, tid);
-    r2c_post_store<T, M, W>(buf, tw_l, p.out, out_off, row0, p.n_rows, tid);
+    fast_fft<M, W, false, E, HIN, false>(buf, tw_m, tid);
+    r2c_post_store<T, M, W, E>(buf, tw_l, p.out, out_off, row0, p.n_rows, tid);
 }
 
-template <typename T, int M, int W>
-__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_r2c_kernel(RowsR2CParams<T> p) {
+template <typename T, int M, int W, int E, bool HIN>
+__global__ void __launch_bounds__(FastShape<M, W, E>::NT) fast_rows_r2c_kernel(RowsR2CParams<T> p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    fast_rows_r2c_body<T, M, W>(p, blockIdx.x, smem_raw);
+    fast_rows_r2c_body<T, M, W, E, HIN>(p, blockIdx.x, smem_raw);
 }
 
-template <typename T, int M, int W>
-__device__ __forceinline__ void fast_rows_c2r_body(const RowsC2RParams<T>& p, int bid, unsigned char* smem_raw) {
+// HOUT: only the first n_out = M real points (M/2 packed complex points) are
+// stored, so the inverse transform's last stage computes only those.
+template <typename T, int M, int W, int E = FastElems<M>::E, bool HOUT = false>
+__device__ __forceinline__ void fast_rows_c2r_body(const RowsC2RParams<T>& p, int bid, unsigned char* smem_raw,
+                                                   bool stage_tw = true) {
     using C = cplx_t<T>;
-    using S = FastShape<M, W>;
+    using S = FastShape<M, W, E>;
     constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw_m = buf + M * LS;
@@ -281,8 +367,10 @@ __device__ __forceinline__ void fast_rows_c2r_body(const RowsC2RParams<T>& p, in
         in_off[tid] = p.in_map.offset(row0 + tid);
         out_off[tid] = p.out_map.offset(row0 + tid);
     }
-    stage_table(tw_m, p.tw_m, M, tid, NT);
-    stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    if (stage_tw) {
+        stage_table(tw_m, p.tw_m, M, tid, NT);
+        stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    }
     __syncthreads();
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
@@ -304,7 +392,7 @@ __device__ __forceinline__ void fast_rows_c2r_body(const RowsC2RParams<T>& p, in
         buf[k * LS + r] = Zk;
     }
     __syncthreads();
-    fast_fft<M, W, true>(buf, tw_m, tid);
+    fast_fft<M, W, true, E, false, HOUT>(buf, tw_m, tid);
     // n_out real points = n_out/2 complex values per row (n_out even)
     const int half = p.n_out >> 1;
     for (int e = tid; e < W * half; e += NT) {
@@ -314,10 +402,10 @@ __device__ __forceinline__ void fast_rows_c2r_body(const RowsC2RParams<T>& p, in
     }
 }
 
-template <typename T, int M, int W>
-__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_rows_c2r_kernel(RowsC2RParams<T> p) {
+template <typename T, int M, int W, int E, bool HOUT>
+__global__ void __launch_bounds__(FastShape<M, W, E>::NT) fast_rows_c2r_kernel(RowsC2RParams<T> p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    fast_rows_c2r_body<T, M, W>(p, blockIdx.x, smem_raw);
+    fast_rows_c2r_body<T, M, W, E, HOUT>(p, blockIdx.x, smem_raw);
 }
 
 // ------------------------------------------------------------- dispatch
@@ -328,34 +416,44 @@ inline int fast_pick_width(long long units, int wide, int narrow) {
 
 template <typename T, int N, int W>
 int launch_fast_rows_r2c(const RowsR2CParams<T>& p, cudaStream_t stream) {
+    constexpr int E = FastPickRows<N, W>::E;
     const size_t smem = RowSmem<N, W>::template bytes<cplx_t<T>>();
-    auto kern = fast_rows_r2c_kernel<T, N, W>;
+    // real input zero beyond n_in <= N: the upper half of the packed points is zero
+    auto kern = p.n_in <= N ? fast_rows_r2c_kernel<T, N, W, E, true> : fast_rows_r2c_kernel<T, N, W, E, false>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast rows_r2c smem attribute"));
-    kern<<<ceil_div(p.n_rows, W), FastShape<N, W>::NT, smem, stream>>>(p);
+    kern<<<ceil_div(p.n_rows, W), FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast rows_r2c");
 }
 
 template <typename T, int N, int W>
 int launch_fast_rows_c2r(const RowsC2RParams<T>& p, cudaStream_t stream) {
+    constexpr int E = FastPickRows<N, W>::E;
     const size_t smem = RowSmem<N, W>::template bytes<cplx_t<T>>();
-    auto kern = fast_rows_c2r_kernel<T, N, W>;
+    // cropped output: only n_out <= N real points (N/2 packed points) are stored
+    auto kern = p.n_out <= N ? fast_rows_c2r_kernel<T, N, W, E, true> : fast_rows_c2r_kernel<T, N, W, E, false>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast rows_c2r smem attribute"));
-    kern<<<ceil_div(p.n_rows, W), FastShape<N, W>::NT, smem, stream>>>(p);
+    kern<<<ceil_div(p.n_rows, W), FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast rows_c2r");
 }
 
 template <typename T, int N, int W, int MODE>
 int launch_fast_lines(LinesParams<T> p, cudaStream_t stream) {
-    const size_t smem = sizeof(cplx_t<T>) * ((size_t)N * FastShape<N, W>::LS + N);
-    auto kern = fast_lines_kernel<T, N, W, MODE>;
+    constexpr int E = FastPickLines<N, W>::E;
+    const size_t smem = sizeof(cplx_t<T>) * ((size_t)N * FastShape<N, W, E>::LS + N);
+    // zero-padded input (n_in <= N/2) and cropped output (n_out <= N/2) select the pruned transforms
+    const bool hin = 2 * p.n_in <= N, hout = 2 * p.n_out <= N;
+    auto kern = hin ? (hout ? fast_lines_kernel<T, N, W, MODE, E, true, true>
+                            : fast_lines_kernel<T, N, W, MODE, E, true, false>)
+                    : (hout ? fast_lines_kernel<T, N, W, MODE, E, false, true>
+                            : fast_lines_kernel<T, N, W, MODE, E, false, false>);
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast lines smem attribute"));
     p.W = W;
     const long long blocks = (long long)p.n_outer * ((p.inner + W - 1) / W);
     SG_REQUIRE(blocks < (1LL << 31), SG_ERR_SHAPE, "lines: too many blocks (%lld)", blocks);
-    kern<<<(unsigned)blocks, FastShape<N, W>::NT, smem, stream>>>(p);
+    kern<<<(unsigned)blocks, FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast lines");
 }
 

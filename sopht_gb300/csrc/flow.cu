@@ -62,11 +62,12 @@ int launch_sweep2d(const Sweep2DParams<T>& p, cudaStream_t stream) {
 
 template <typename T, int N, int W>
 int launch_fast_flow_load(const FlowLoadParams<T>& p, cudaStream_t stream) {
+    constexpr int E = FastPickRows<N, W>::E;
     const size_t smem = FlowLoadSmem<N, W>::template bytes<T>();
-    auto kern = fast_flow_load_kernel<T, N, W>;
+    auto kern = fast_flow_load_kernel<T, N, W, E>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast flow_load smem attribute"));
-    kern<<<ceil_div(p.n_rows, W), FastShape<N, W>::NT, smem, stream>>>(p);
+    kern<<<ceil_div(p.n_rows, W), FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast flow_load");
 }
 
@@ -217,9 +218,9 @@ int flow_step_2d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
 template <typename T>
 int poisson_spectral_passes_marked(sg_flow_plan_s* p, int ncomp, cudaStream_t stream) {
     SG_TRY(poisson_spectral_pass3d<T>(p->poisson, ncomp, 0, stream));
-    mark(p, 5, stream);
+    mark(p, 3, stream);
     SG_TRY(poisson_spectral_pass3d<T>(p->poisson, ncomp, 1, stream));
-    mark(p, 6, stream);
+    mark(p, 4, stream);
     return poisson_spectral_pass3d<T>(p->poisson, ncomp, 2, stream);
 }
 
@@ -231,8 +232,10 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
     Grid3 G{p->nz, p->ny, p->nx};
     T* A = (T*)p->scratch_a;
     T* B = (T*)p->scratch_b;
-    const T* w1 = w;
+    // timing marks: 0 forcing curl, u x w update, diffusion (+ filter) 1 Poisson load 2 y FFT 3 z conv
+    // 4 y IFFT 5 x C2R 6 curl 7
     mark(p, 0, stream);
+    const T* w1 = w;
     if (f) {
         Stencil3DParams<T> s{};
         s.grid = G;
@@ -245,7 +248,6 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         SG_TRY(launch_status("forcing_curl3d"));
         w1 = A;
     }
-    mark(p, 1, stream);
     {
         Stencil3DParams<T> s{};
         s.grid = G;
@@ -256,7 +258,6 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         rotational_update3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
         SG_TRY(launch_status("rotational_update3d"));
     }
-    mark(p, 2, stream);
     {
         Stencil3DParams<T> s{};
         s.grid = G;
@@ -268,14 +269,14 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         SG_TRY(launch_status("diffusion3d"));
     }
     SG_TRY(filter3d<T>(G, A, p->filter_type, p->filter_order, (T*)p->filt_a, (T*)p->filt_b, stream));
-    mark(p, 3, stream);
+    mark(p, 1, stream);
     FlowLoadParams<T> l = load_params<T>(p, A, w, f);
     SG_TRY(launch_flow_load<T>(l, stream));
-    mark(p, 4, stream);
+    mark(p, 2, stream);
     SG_TRY(poisson_spectral_passes_marked<T>(p, 3, stream));
-    mark(p, 7, stream);
+    mark(p, 5, stream);
     SG_TRY(poisson_store_rows<T>(p->poisson, psi, 3, n, stream));
-    mark(p, 8, stream);
+    mark(p, 6, stream);
     SG_TRY(cuda_status(cudaMemsetAsync(p->umax_slot(), 0, 8, stream), "umax reset"));
     Curl3DParams<T> c{};
     c.grid = G;
@@ -286,7 +287,7 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
     c.add_free_stream = free_stream;
     c.umax = (T*)p->umax_slot();
     SG_TRY(launch_curl3d<T>(c, n, stream));
-    mark(p, 9, stream);
+    mark(p, 7, stream);
     return SG_OK;
 }
 

@@ -270,11 +270,15 @@ template <int M, int W> struct FlowLoadSmem {
     }
 };
 
-template <typename T, int M, int W>
-__device__ __forceinline__ void fast_flow_load_body(const FlowLoadParams<T>& p, int bid, unsigned char* smem_raw) {
+// The row's packed complex points M/2 .. M-1 are the zero padding (2n >= nx),
+// so they are not loaded and the first stage skips them.
+template <typename T, int M, int W, int E = FastElems<M>::E>
+__device__ __forceinline__ void fast_flow_load_body(const FlowLoadParams<T>& p, int bid, unsigned char* smem_raw,
+                                                    bool stage_tw = true) {
     using C = cplx_t<T>;
-    using S = FastShape<M, W>;
+    using S = FastShape<M, W, E>;
     constexpr int LS = S::LS, NT = S::NT, PER = M * W / NT;
+    constexpr bool SKIP_LOAD = FastEnds<M>::first_even;
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw_m = buf + M * LS;
     C* tw_l = tw_m + M;
@@ -306,13 +310,16 @@ __device__ __forceinline__ void fast_flow_load_body(const FlowLoadParams<T>& p, 
         fy[tid] = p.width > 0 ? p.cy[y] : T(1);
         fz[tid] = (p.width > 0 && p.dim == 3) ? p.cz[zi] : T(1);
     }
-    stage_table(tw_m, p.tw_m, M, tid, NT);
-    stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    if (stage_tw) {
+        stage_table(tw_m, p.tw_m, M, tid, NT);
+        stage_table(tw_l, p.tw_l, M + 1, tid, NT);
+    }
     __syncthreads();
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int e = tid + b * NT;
         const int r = e / M, n = e % M;
+        if (SKIP_LOAD && n >= M / 2) continue;
         C z = cmake<C>(T(0), T(0));
         if (row0 + r < p.n_rows && 2 * n < nx) {
             const int x0 = 2 * n;
@@ -344,14 +351,14 @@ __device__ __forceinline__ void fast_flow_load_body(const FlowLoadParams<T>& p, 
         buf[n * LS + r] = z;
     }
     __syncthreads();
-    fast_fft<M, W, false>(buf, tw_m, tid);
-    r2c_post_store<T, M, W>(buf, tw_l, p.spec, spec_off, row0, p.n_rows, tid);
+    fast_fft<M, W, false, E, true, false>(buf, tw_m, tid);
+    r2c_post_store<T, M, W, E>(buf, tw_l, p.spec, spec_off, row0, p.n_rows, tid);
 }
 
-template <typename T, int M, int W>
-__global__ void __launch_bounds__(FastShape<M, W>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
+template <typename T, int M, int W, int E>
+__global__ void __launch_bounds__(FastShape<M, W, E>::NT) fast_flow_load_kernel(FlowLoadParams<T> p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    fast_flow_load_body<T, M, W>(p, blockIdx.x, smem_raw);
+    fast_flow_load_body<T, M, W, E>(p, blockIdx.x, smem_raw);
 }
 
 // ---------------------------------------- curl + free stream + max |u| (2D)

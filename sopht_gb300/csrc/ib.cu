@@ -18,6 +18,14 @@
 
 using namespace sg;
 
+template <typename T>
+static void ib_interaction_launch(const IBParams<T>& p, cudaStream_t stream) {
+    // two markers (warps) per block: bodies of ~100 markers spread over many SMs
+    const unsigned blocks = ceil_div((int64_t)p.n_lag * 32, 64);
+    if (p.dim == 2) ib_interaction_kernel<T, 2><<<blocks, 64, 0, stream>>>(p);
+    else ib_interaction_kernel<T, 3><<<blocks, 64, 0, stream>>>(p);
+}
+
 extern "C" int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, double dx, double shift, int n_lag,
                                  int kernel_type, const double* position, const double* body_velocity,
                                  const void* eul_velocity, int32_t* nearest, void* weights, void* flow_velocity,
@@ -33,22 +41,39 @@ extern "C" int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, dou
     SG_REQUIRE(dx > 0, SG_ERR_INVALID_ARG, "ib interaction: dx must be positive");
     if (dim == 2) nz = 1;
     auto stream = (cudaStream_t)stream_;
-    const unsigned blocks = ceil_div((int64_t)n_lag * 32, 256);
     if (dtype == SG_F32) {
         IBParams<float> p{dim, nz, ny, nx, n_lag, kernel_type, dx, shift, position, body_velocity,
                           (const float*)eul_velocity, nearest, (float*)weights, (float*)flow_velocity,
                           (float*)velocity_mismatch, (float*)position_mismatch, (float*)forcing,
                           stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev};
-        ib_interaction_kernel<float><<<blocks, 256, 0, stream>>>(p);
+        ib_interaction_launch<float>(p, stream);
     } else {
         SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "ib interaction: bad dtype");
         IBParams<double> p{dim, nz, ny, nx, n_lag, kernel_type, dx, shift, position, body_velocity,
                            (const double*)eul_velocity, nearest, (double*)weights, (double*)flow_velocity,
                            (double*)velocity_mismatch, (double*)position_mismatch, (double*)forcing,
                            stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev};
-        ib_interaction_kernel<double><<<blocks, 256, 0, stream>>>(p);
+        ib_interaction_launch<double>(p, stream);
     }
     return launch_status("ib_interaction");
+}
+
+template <typename T>
+static void ib_spread_launch(const SpreadParams<T>& p, cudaStream_t stream) {
+    const int cells = p.dim == 2 ? 16 : 64;
+    const int64_t threads = (int64_t)p.n_lag * cells;
+    // one warp per (marker, window cell) with the markers' nearest indices
+    // staged in shared memory, when they fit in 48 KB
+    const size_t staged = (size_t)p.dim * p.n_lag * sizeof(int);
+    if (staged <= 48 * 1024) {
+        const unsigned blocks = ceil_div(threads * 32, 256);
+        if (p.dim == 2) ib_spread_warp_kernel<T, 2><<<blocks, 256, staged, stream>>>(p);
+        else ib_spread_warp_kernel<T, 3><<<blocks, 256, staged, stream>>>(p);
+    } else {
+        const unsigned blocks = ceil_div(threads, 256);
+        if (p.dim == 2) ib_spread_kernel<T, 2><<<blocks, 256, 0, stream>>>(p);
+        else ib_spread_kernel<T, 3><<<blocks, 256, 0, stream>>>(p);
+    }
 }
 
 extern "C" int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag, const int32_t* nearest,
@@ -58,16 +83,14 @@ extern "C" int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_la
                "ib spread: bad argument");
     if (dim == 2) nz = 1;
     auto stream = (cudaStream_t)stream_;
-    const int cells = dim == 2 ? 16 : 64;
     const int64_t ncell = (int64_t)nz * ny * nx;
-    const unsigned blocks = ceil_div((int64_t)n_lag * cells, 256);
     if (dtype == SG_F32) {
         if (reset) {
             zero_kernel<float><<<ceil_div(dim * ncell, 256), 256, 0, stream>>>(dim * ncell, (float*)eul_forcing);
         }
         SpreadParams<float> p{dim, nz, ny, nx, n_lag, 0, nearest, (const float*)weights, (const float*)forcing,
                               (float*)eul_forcing};
-        ib_spread_kernel<float><<<blocks, 256, 0, stream>>>(p);
+        ib_spread_launch<float>(p, stream);
     } else {
         SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "ib spread: bad dtype");
         if (reset) {
@@ -75,7 +98,7 @@ extern "C" int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_la
         }
         SpreadParams<double> p{dim, nz, ny, nx, n_lag, 0, nearest, (const double*)weights, (const double*)forcing,
                                (double*)eul_forcing};
-        ib_spread_kernel<double><<<blocks, 256, 0, stream>>>(p);
+        ib_spread_launch<double>(p, stream);
     }
     return launch_status("ib_spread");
 }

@@ -58,70 +58,90 @@ template <typename T> struct IBParams {
     int32_t* status;
 };
 
-// marker i is handled by one whole warp (lane = threadIdx.x & 31)
-template <typename T>
+// Marker i is handled by one whole warp.  Lane 4 d + k (d < DIM, k < 4)
+// evaluates axis d's nearest index and the 1D weight of offset k - 1; the other
+// lanes read them by shuffles, so each value is computed once per marker.  DIM
+// is a template parameter so every per-axis array stays in registers.
+template <typename T, int DIM>
 __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i) {
+    constexpr int CELLS = DIM == 2 ? 16 : 64;
     const int lane = threadIdx.x & 31;
     if (i >= p.n_lag) return;
-    const int dim = p.dim;
     const int n = p.n_lag;
     const T dxT = (T)p.dx;
-    int near[3] = {0, 0, 0};
-    T phi[3][4];
-    const int ext[3] = {p.nx, p.ny, p.nz};
-    bool inside = true;
-    for (int d = 0; d < dim; ++d) {
+    int my_near = 0;
+    T my_phi = T(0);
+    if (lane < 4 * DIM) {
+        const int d = lane >> 2, k = lane & 3;
         const double X = p.pos[d * n + i];
-        const double nd = np_floor_divide(X - p.shift, p.dx);
-        near[d] = (int)nd;
-        if (near[d] - 1 < 0 || near[d] + 2 > ext[d] - 1) inside = false;
-        for (int k = 0; k < 4; ++k) {
-            // support: stored in the field precision, then scaled by 1/dx in it
-            const T r = (T)((double)(near[d] + k - 1) * p.dx + p.shift - X);
-            const T rn = r / dxT;
-            if (p.kernel == 0) phi[d][k] = T(1) + dev_cos<T>((T)(0.5 * 3.14159265358979323846) * rn);
-            else phi[d][k] = peskin_phi<T>(fabs(rn));
-        }
+        my_near = (int)np_floor_divide(X - p.shift, p.dx);
+        // support: stored in the field precision, then scaled by 1/dx in it
+        const T r = (T)((double)(my_near + k - 1) * p.dx + p.shift - X);
+        const T rn = r / dxT;
+        if (p.kernel == 0) my_phi = T(1) + dev_cos<T>((T)(0.5 * 3.14159265358979323846) * rn);
+        else my_phi = peskin_phi<T>(fabs(rn));
     }
-    if (lane < dim) p.nearest[lane * n + i] = near[lane];
+    int near[DIM];
+    bool inside = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        near[d] = __shfl_sync(0xffffffffu, my_near, 4 * d);
+        const int ext = d == 0 ? p.nx : (d == 1 ? p.ny : p.nz);
+        if (near[d] - 1 < 0 || near[d] + 2 > ext - 1) inside = false;
+    }
+    if ((lane & 3) == 0 && (lane >> 2) < DIM) p.nearest[(lane >> 2) * n + i] = my_near;
     // optional VirtualBoundaryForcing.time_step: xi += dt * dU (previous dU)
-    if (p.xi_step && lane < dim) {
+    if (p.xi_step && lane < DIM) {
         const T dt = (T)(p.dev ? p.dev->dt : p.xi_dt);
         p.pos_mismatch[lane * n + i] = p.pos_mismatch[lane * n + i] + dt * p.vel_mismatch[lane * n + i];
     }
     if (!inside) {
         if (lane == 0) atomicExch(p.status, SG_ERR_OUT_OF_DOMAIN);
-        const int cells = dim == 2 ? 16 : 64;
-        for (int c = lane; c < cells; c += 32) p.weights[c * n + i] = T(0);
+        for (int c = lane; c < CELLS; c += 32) p.weights[c * n + i] = T(0);
         return;
     }
     T pref;
     if (p.kernel == 0) {
         const T q = T(0.25) / dxT;
-        pref = dim == 2 ? q * q : (T)((double)q * (double)q * (double)q);
+        pref = DIM == 2 ? q * q : (T)((double)q * (double)q * (double)q);
     } else {
         const T q = T(0.125) / dxT;
-        pref = dim == 2 ? q * q : (T)((double)q * (double)q * (double)q);
+        pref = DIM == 2 ? q * q : (T)((double)q * (double)q * (double)q);
     }
-    const int cells = dim == 2 ? 16 : 64;
     const int64_t plane = (int64_t)p.ny * p.nx;
-    const int64_t ncell = plane * (dim == 3 ? p.nz : 1);
-    T acc[3] = {T(0), T(0), T(0)};
-    for (int c = lane; c < cells; c += 32) {
-        const int bx = c & 3, by = (c >> 2) & 3, bz = c >> 4;
-        T w = pref * phi[0][bx] * phi[1][by];
-        if (dim == 3) w = w * phi[2][bz];
-        p.weights[c * n + i] = w;
-        const int gx = near[0] - 1 + bx, gy = near[1] - 1 + by;
-        const int gz = dim == 3 ? near[2] - 1 + bz : 0;
-        const int64_t g = (int64_t)gz * plane + (int64_t)gy * p.nx + gx;
-        for (int d = 0; d < dim; ++d) acc[d] += p.u[d * ncell + g] * w;
+    const int64_t ncell = plane * (DIM == 3 ? p.nz : 1);
+    T acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = T(0);
+#pragma unroll
+    for (int c0 = 0; c0 < CELLS; c0 += 32) {
+        const int c = c0 + lane;
+        const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
+        const T px = __shfl_sync(0xffffffffu, my_phi, bx);
+        const T py = __shfl_sync(0xffffffffu, my_phi, 4 + by);
+        T pz = T(0);
+        if constexpr (DIM == 3) pz = __shfl_sync(0xffffffffu, my_phi, 8 + bz);
+        if (c < CELLS) {
+            T w = pref * px * py;
+            int gz = 0;
+            if constexpr (DIM == 3) {
+                w = w * pz;
+                gz = near[2] - 1 + bz;
+            }
+            p.weights[c * n + i] = w;
+            const int gx = near[0] - 1 + bx, gy = near[1] - 1 + by;
+            const int64_t g = (int64_t)gz * plane + (int64_t)gy * p.nx + gx;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) acc[d] += p.u[d * ncell + g] * w;
+        }
     }
-    for (int d = 0; d < dim; ++d)
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
         for (int o = 16; o > 0; o >>= 1) acc[d] += __shfl_xor_sync(0xffffffffu, acc[d], o);
-    if (lane < dim) {
-        const int d = lane;
-        const T dxd = dim == 2 ? dxT * dxT : dxT * dxT * dxT;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        if (lane != d) continue;
+        const T dxd = DIM == 2 ? dxT * dxT : dxT * dxT * dxT;
         const T U = acc[d] * dxd;
         p.flow_vel[d * n + i] = U;
         const T dU = (T)((double)U - p.body_vel[d * n + i]);
@@ -130,9 +150,9 @@ __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i)
     }
 }
 
-template <typename T>
+template <typename T, int DIM>
 __global__ void __launch_bounds__(256) ib_interaction_kernel(IBParams<T> p) {
-    ib_interaction_body<T>(p, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    ib_interaction_body<T, DIM>(p, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 }
 
 template <typename T> struct SpreadParams {
@@ -143,49 +163,144 @@ template <typename T> struct SpreadParams {
     T* eul;
 };
 
-// thread t owns (marker t / 4^dim, window cell t % 4^dim)
-template <typename T>
-__device__ __forceinline__ void ib_spread_body(const SpreadParams<T>& p, int64_t t) {
-    const int cells = p.dim == 2 ? 16 : 64;
-    if (t >= (int64_t)p.n_lag * cells) return;
-    const int i = (int)(t / cells), c = (int)(t % cells);
+// Cell c of marker i's window: the thread whose marker is the lowest-index
+// marker touching the cell owns it and sums every marker's F * phi into it in
+// marker index order (the per-cell order of the reference's serial loop), so
+// no atomics are needed and the result is bitwise repeatable.  near(d, j) gives
+// marker j's nearest index along axis d.
+template <typename T, int DIM, typename NearF>
+__device__ __forceinline__ void ib_spread_at(const SpreadParams<T>& p, int i, int c, NearF near) {
     const int n = p.n_lag;
-    const int dim = p.dim;
-    int cell[3];
-    cell[0] = p.nearest[i] - 1 + (c & 3);
-    cell[1] = p.nearest[n + i] - 1 + ((c >> 2) & 3);
-    cell[2] = dim == 3 ? p.nearest[2 * n + i] - 1 + (c >> 4) : 0;
-    const int ext[3] = {p.nx, p.ny, dim == 3 ? p.nz : 1};
-    for (int d = 0; d < dim; ++d)
-        if (cell[d] < 0 || cell[d] >= ext[d]) return;  // marker reported out of domain
+    int cell[DIM];
+    cell[0] = near(0, i) - 1 + (c & 3);
+    cell[1] = near(1, i) - 1 + ((c >> 2) & 3);
+    if constexpr (DIM == 3) cell[2] = near(2, i) - 1 + (c >> 4);
+    // a marker whose window leaves the grid was reported out of domain
+    if (cell[0] < 0 || cell[0] >= p.nx || cell[1] < 0 || cell[1] >= p.ny) return;
+    if constexpr (DIM == 3)
+        if (cell[2] < 0 || cell[2] >= p.nz) return;
     auto offset_in = [&](int j, int& k) -> bool {
-        int o[3] = {0, 0, 0};
-        for (int d = 0; d < dim; ++d) {
-            o[d] = cell[d] - (p.nearest[d * n + j] - 1);
-            if (o[d] < 0 || o[d] > 3) return false;
+        const int o0 = cell[0] - (near(0, j) - 1);
+        if (o0 < 0 || o0 > 3) return false;
+        const int o1 = cell[1] - (near(1, j) - 1);
+        if (o1 < 0 || o1 > 3) return false;
+        int o2 = 0;
+        if constexpr (DIM == 3) {
+            o2 = cell[2] - (near(2, j) - 1);
+            if (o2 < 0 || o2 > 3) return false;
         }
-        k = o[0] + 4 * o[1] + 16 * o[2];
+        k = o0 + 4 * o1 + 16 * o2;
         return true;
     };
     int k;
     for (int j = 0; j < i; ++j)
         if (offset_in(j, k)) return;  // a lower-index marker owns this cell
     const int64_t plane = (int64_t)p.ny * p.nx;
-    const int64_t ncell = plane * (dim == 3 ? p.nz : 1);
-    const int64_t g = (int64_t)cell[2] * plane + (int64_t)cell[1] * p.nx + cell[0];
-    T acc[3];
-    for (int d = 0; d < dim; ++d) acc[d] = p.reset ? T(0) : p.eul[d * ncell + g];
+    const int64_t ncell = plane * (DIM == 3 ? p.nz : 1);
+    const int64_t g = (int64_t)(DIM == 3 ? cell[DIM - 1] : 0) * plane + (int64_t)cell[1] * p.nx + cell[0];
+    T acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = p.reset ? T(0) : p.eul[d * ncell + g];
     for (int j = i; j < n; ++j) {
         if (!offset_in(j, k)) continue;
         const T w = p.weights[k * n + j];
-        for (int d = 0; d < dim; ++d) acc[d] = acc[d] + p.forcing[d * n + j] * w;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] = acc[d] + p.forcing[d * n + j] * w;
     }
-    for (int d = 0; d < dim; ++d) p.eul[d * ncell + g] = acc[d];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) p.eul[d * ncell + g] = acc[d];
 }
 
-template <typename T>
+// thread t owns (marker t / 4^DIM, window cell t % 4^DIM); nearest read from global memory
+template <typename T, int DIM>
+__device__ __forceinline__ void ib_spread_body(const SpreadParams<T>& p, int64_t t) {
+    constexpr int CELLS = DIM == 2 ? 16 : 64;
+    if (t >= (int64_t)p.n_lag * CELLS) return;
+    const int n = p.n_lag;
+    ib_spread_at<T, DIM>(p, (int)(t / CELLS), (int)(t % CELLS),
+                         [&](int d, int j) { return (int)p.nearest[d * n + j]; });
+}
+
+template <typename T, int DIM>
 __global__ void __launch_bounds__(256) ib_spread_kernel(SpreadParams<T> p) {
-    ib_spread_body<T>(p, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    ib_spread_body<T, DIM>(p, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// The same spreading with one warp per (marker i, window cell c), the markers'
+// nearest indices read from `s_near` (shared memory, DIM * n_lag ints).  The
+// lanes scan 32 markers at a time: a ballot tells whether a lower-index marker
+// touches the cell (then another warp owns it), and lane 0 adds the touching
+// markers' F * phi in ascending marker order -- the order of ib_spread_at, so
+// the sums are the same to the bit.  Every lane of the warp must call it.
+template <typename T, int DIM>
+__device__ __forceinline__ void ib_spread_warp_pair(const SpreadParams<T>& p, const int* s_near, int i, int c,
+                                                    int lane) {
+    const int n = p.n_lag;
+    int cell[DIM];
+    cell[0] = s_near[i] - 1 + (c & 3);
+    cell[1] = s_near[n + i] - 1 + ((c >> 2) & 3);
+    if constexpr (DIM == 3) cell[2] = s_near[2 * n + i] - 1 + (c >> 4);
+    if (cell[0] < 0 || cell[0] >= p.nx || cell[1] < 0 || cell[1] >= p.ny) return;
+    if constexpr (DIM == 3)
+        if (cell[2] < 0 || cell[2] >= p.nz) return;
+    auto offset_in = [&](int j, int& k) -> bool {
+        const int o0 = cell[0] - (s_near[j] - 1);
+        if (o0 < 0 || o0 > 3) return false;
+        const int o1 = cell[1] - (s_near[n + j] - 1);
+        if (o1 < 0 || o1 > 3) return false;
+        int o2 = 0;
+        if constexpr (DIM == 3) {
+            o2 = cell[2] - (s_near[2 * n + j] - 1);
+            if (o2 < 0 || o2 > 3) return false;
+        }
+        k = o0 + 4 * o1 + 16 * o2;
+        return true;
+    };
+    for (int j0 = 0; j0 < i; j0 += 32) {
+        const int j = j0 + lane;
+        int k;
+        const bool hit = j < i && offset_in(j, k);
+        if (__any_sync(0xffffffffu, hit)) return;  // a lower-index marker owns this cell
+    }
+    const int64_t plane = (int64_t)p.ny * p.nx;
+    const int64_t ncell = plane * (DIM == 3 ? p.nz : 1);
+    const int64_t g = (int64_t)(DIM == 3 ? cell[DIM - 1] : 0) * plane + (int64_t)cell[1] * p.nx + cell[0];
+    T acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = p.reset ? T(0) : p.eul[d * ncell + g];
+    for (int j0 = i; j0 < n; j0 += 32) {
+        const int j = j0 + lane;
+        int k = 0;
+        const bool hit = j < n && offset_in(j, k);
+        unsigned mask = __ballot_sync(0xffffffffu, hit);
+        while (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int kb = __shfl_sync(0xffffffffu, k, b);
+            if (lane == 0) {
+                const int jb = j0 + b;
+                const T w = p.weights[kb * n + jb];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) acc[d] = acc[d] + p.forcing[d * n + jb] * w;
+            }
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p.eul[d * ncell + g] = acc[d];
+    }
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) ib_spread_warp_kernel(SpreadParams<T> p) {
+    extern __shared__ int s_near[];
+    constexpr int CELLS = DIM == 2 ? 16 : 64;
+    const int n = p.n_lag;
+    for (int e = threadIdx.x; e < DIM * n; e += blockDim.x) s_near[e] = p.nearest[e];
+    __syncthreads();
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wid >= (int64_t)n * CELLS) return;  // uniform over the warp
+    ib_spread_warp_pair<T, DIM>(p, s_near, (int)(wid / CELLS), (int)(wid % CELLS), threadIdx.x & 31);
 }
 
 template <typename T>

@@ -9,9 +9,9 @@ own velocity, exactly as ``compute_stable_timestep`` would give it, so every
 instance follows the same trajectory it would follow stepped on its own with
 ``device_stable_timestep`` / ``time_step_device``.
 
-The step is graph-capturable (``capture_graph``).  ``autotune`` times the
-launch-shape candidates (sweep tile height 8 or 16 rows; persistent blocks per
-SM) on the actual batch and keeps the fastest.
+The step is graph-capturable.  ``autotune`` times the launch-shape candidates
+(sweep tile height 8 or 16 rows; persistent blocks per SM; 256- or 512-thread
+blocks for the FFT passes) on the actual batch and keeps the fastest.
 """
 
 from __future__ import annotations
@@ -84,7 +84,7 @@ class BatchedFlowSimulator2D:
         self._members = members
         self._batch = ctypes.c_void_p()
         _lib.call("sg_batch2d_create", n, members, ctypes.byref(self._batch))
-        self.tuning = (16, 8)
+        self.tuning = (16, 8, 256)
         self._primed = False
 
     def __len__(self):
@@ -109,9 +109,9 @@ class BatchedFlowSimulator2D:
             sim.prime_velocity_max()
         self._primed = True
 
-    def set_tuning(self, sweep_tile_y: int, blocks_per_sm: int) -> None:
-        _lib.call("sg_batch2d_set_tuning", self._batch, int(sweep_tile_y), int(blocks_per_sm))
-        self.tuning = (int(sweep_tile_y), int(blocks_per_sm))
+    def set_tuning(self, sweep_tile_y: int, blocks_per_sm: int, fft_threads: int = 256) -> None:
+        _lib.call("sg_batch2d_set_tuning", self._batch, int(sweep_tile_y), int(blocks_per_sm), int(fft_threads))
+        self.tuning = (int(sweep_tile_y), int(blocks_per_sm), int(fft_threads))
 
     def step(self) -> None:
         """One coupled step of every instance (no synchronisation)."""
@@ -130,9 +130,9 @@ class BatchedFlowSimulator2D:
         """Time the launch-shape candidates on this batch; keep the fastest.
 
         The candidates advance the batch (``steps`` steps each), like any
-        other steps.  Returns (sweep tile height, blocks per SM)."""
+        other steps.  Returns (sweep tile height, blocks per SM, FFT block size)."""
         if candidates is None:
-            candidates = list(itertools.product((16, 8), (0, 2, 4, 8, 16)))
+            candidates = list(itertools.product((16, 8), (0, 2, 4, 8, 16), (256, 512)))
         if not self._primed:
             self.prime()
         best, best_ms = None, float("inf")

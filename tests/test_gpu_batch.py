@@ -36,7 +36,7 @@ def _make(i, ny, nx):
     return sim, inter
 
 
-@pytest.mark.parametrize("tuning", [(16, 8), (8, 0), (16, 2)])
+@pytest.mark.parametrize("tuning", [(16, 8, 256), (8, 0, 256), (16, 2, 512), (8, 8, 512)])
 def test_batched_equals_individual(tuning):
     from sopht_gb300.build import build
     from sopht_gb300.simulator import BatchedFlowSimulator2D
@@ -92,6 +92,6 @@ def test_autotune_picks_a_candidate():
     from sopht_gb300.simulator import BatchedFlowSimulator2D
     members = [_make(i, *s) for i, s in enumerate(SIZES[:3])]
     batch = BatchedFlowSimulator2D([m[0] for m in members], [m[1] for m in members])
-    best = batch.autotune(steps=2, candidates=[(16, 0), (8, 4)])
-    assert best in [(16, 0), (8, 4)]
+    best = batch.autotune(steps=2, candidates=[(16, 0, 256), (8, 4, 512)])
+    assert best in [(16, 0, 256), (8, 4, 512)]
     assert batch.tuning == best
