@@ -264,8 +264,28 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
     }
 }
 
+// Occupancy of the fp32 line kernels with E <= 16: registers capped at 64 per
+// thread (two 512-thread or four 256-thread blocks per SM), and every FFT
+// kernel asks for the largest shared-memory carveout.  Measured on GB300 the
+// 512-thread convolution and inverse passes otherwise run one block per SM
+// (256^3 z convolution 1.26 -> 1.14 ms, y IFFT 0.47 -> 0.43 ms); giving the
+// carveout to only some of the step's FFT kernels was slower than giving it to
+// all of them (the SMs reconfigure shared memory between kernels).  fp64 and
+// E = 24 kernels keep their registers: a cap would spill them.
+template <typename T, int NT, int E> struct FastOccupancy {
+    static constexpr int min_blocks =
+        (sizeof(T) == 8 || E > 16) ? 1 : (NT >= 512 ? 2048 / NT / 2 : (NT >= 256 ? 4 : 1));
+};
+
+template <typename K> inline int fast_max_carveout(K kern, const char* what) {
+    return cuda_status(
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared),
+        what);
+}
+
 template <typename T, int N, int W, int MODE, int E, bool HIN, bool HOUT>
-__global__ void __launch_bounds__(FastShape<N, W, E>::NT) fast_lines_kernel(LinesParams<T> p) {
+__global__ void __launch_bounds__(FastShape<N, W, E>::NT, FastOccupancy<T, FastShape<N, W, E>::NT, E>::min_blocks)
+    fast_lines_kernel(LinesParams<T> p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     fast_lines_body<T, N, W, MODE, E, HIN, HOUT>(p, blockIdx.x, smem_raw);
 }
@@ -422,6 +442,7 @@ int launch_fast_rows_r2c(const RowsR2CParams<T>& p, cudaStream_t stream) {
     auto kern = p.n_in <= N ? fast_rows_r2c_kernel<T, N, W, E, true> : fast_rows_r2c_kernel<T, N, W, E, false>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast rows_r2c smem attribute"));
+    SG_TRY(fast_max_carveout(kern, "fast rows_r2c carveout attribute"));
     kern<<<ceil_div(p.n_rows, W), FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast rows_r2c");
 }
@@ -434,6 +455,7 @@ int launch_fast_rows_c2r(const RowsC2RParams<T>& p, cudaStream_t stream) {
     auto kern = p.n_out <= N ? fast_rows_c2r_kernel<T, N, W, E, true> : fast_rows_c2r_kernel<T, N, W, E, false>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast rows_c2r smem attribute"));
+    SG_TRY(fast_max_carveout(kern, "fast rows_c2r carveout attribute"));
     kern<<<ceil_div(p.n_rows, W), FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast rows_c2r");
 }
@@ -450,6 +472,7 @@ int launch_fast_lines(LinesParams<T> p, cudaStream_t stream) {
                             : fast_lines_kernel<T, N, W, MODE, E, false, false>);
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast lines smem attribute"));
+    SG_TRY(fast_max_carveout(kern, "fast lines carveout attribute"));
     p.W = W;
     const long long blocks = (long long)p.n_outer * ((p.inner + W - 1) / W);
     SG_REQUIRE(blocks < (1LL << 31), SG_ERR_SHAPE, "lines: too many blocks (%lld)", blocks);

@@ -67,6 +67,7 @@ int launch_fast_flow_load(const FlowLoadParams<T>& p, cudaStream_t stream) {
     auto kern = fast_flow_load_kernel<T, N, W, E>;
     SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "fast flow_load smem attribute"));
+    SG_TRY(fast_max_carveout(kern, "fast flow_load carveout attribute"));
     kern<<<ceil_div(p.n_rows, W), FastShape<N, W, E>::NT, smem, stream>>>(p);
     return launch_status("fast flow_load");
 }
