@@ -140,8 +140,67 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_prime
     for (int q = 0; q < R; ++q) v[q] = out[q];
 }
 
+// cos and sin of 2 pi m / 16 for the twiddles inside a 16-point DFT
+__host__ __device__ constexpr double w16_cos(int m) {
+    return m == 0 ? 1.0 : m == 1 ? 0.92387953251128674 : m == 2 ? 0.70710678118654752 : m == 3 ? 0.38268343236508977
+         : m == 4 ? 0.0 : m == 6 ? -0.70710678118654752 : -0.92387953251128674;  // m == 9
+}
+__host__ __device__ constexpr double w16_sin(int m) {
+    return m == 0 ? 0.0 : m == 1 ? 0.38268343236508977 : m == 2 ? 0.70710678118654752 : m == 3 ? 0.92387953251128674
+         : m == 4 ? 1.0 : m == 6 ? 0.70710678118654752 : -0.38268343236508977;  // m == 9
+}
+
+// 16-point DFT as 4 x 4: DFT-4 over n1 for each n2 (input n = 4 n1 + n2), the
+// twiddles w16^(n2 k1), then DFT-4 over n2 (output k = k1 + 4 k2).  HALF_IN:
+// inputs 8..15 are zero and the first DFT-4s skip them.
+template <bool INV, bool HALF_IN = false, typename C> __device__ __forceinline__ void dft16(C* v) {
+    using T = typename Cx<C>::T;
+    C y[4][4];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+        if constexpr (HALF_IN) {
+            const C x0 = v[n2], x1 = v[n2 + 4];
+            const C r1 = INV ? cmake<C>(-x1.y, x1.x) : cmake<C>(x1.y, -x1.x);
+            y[n2][0] = cadd(x0, x1);
+            y[n2][1] = cadd(x0, r1);
+            y[n2][2] = csub(x0, x1);
+            y[n2][3] = csub(x0, r1);
+        } else {
+            y[n2][0] = v[n2];
+            y[n2][1] = v[n2 + 4];
+            y[n2][2] = v[n2 + 8];
+            y[n2][3] = v[n2 + 12];
+            dft4<INV>(y[n2][0], y[n2][1], y[n2][2], y[n2][3]);
+        }
+    }
+#pragma unroll
+    for (int n2 = 1; n2 < 4; ++n2) {
+#pragma unroll
+        for (int k1 = 1; k1 < 4; ++k1) {
+            const int m = n2 * k1;
+            if (m == 4) {
+                const C a = y[n2][k1];  // w16^4 = -i (forward), +i (inverse)
+                y[n2][k1] = INV ? cmake<C>(-a.y, a.x) : cmake<C>(a.y, -a.x);
+            } else {
+                const T c = (T)w16_cos(m), sn = (T)w16_sin(m);
+                y[n2][k1] = cmul(y[n2][k1], cmake<C>(c, INV ? sn : -sn));
+            }
+        }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        C z0 = y[0][k1], z1 = y[1][k1], z2 = y[2][k1], z3 = y[3][k1];
+        dft4<INV>(z0, z1, z2, z3);
+        v[k1] = z0;
+        v[k1 + 4] = z1;
+        v[k1 + 8] = z2;
+        v[k1 + 12] = z3;
+    }
+}
+
 template <int R, bool INV, typename C> __device__ __forceinline__ void dft_r(C* v) {
-    if constexpr (R == 2) dft2<INV>(v[0], v[1]);
+    if constexpr (R == 16) dft16<INV>(v);
+    else if constexpr (R == 2) dft2<INV>(v[0], v[1]);
     else if constexpr (R == 3) dft3<INV>(v[0], v[1], v[2]);
     else if constexpr (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
     else if constexpr (R == 5 || R == 7) dft_prime<R, INV>(v);

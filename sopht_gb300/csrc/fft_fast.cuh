@@ -23,16 +23,20 @@
 namespace sg {
 
 // ------------------------------------------------------ compile-time schedule
-__host__ __device__ constexpr int sched_count(int n) {
+// Radix schedule of a length: 16s first when R16 (fewer stages for 128, 256
+// and 1024), then 8s, 4s, 2s, 3s.
+__host__ __device__ constexpr int sched_count(int n, bool r16 = false) {
     int c = 0;
+    while (r16 && n % 16 == 0) { n /= 16; ++c; }
     while (n % 8 == 0) { n /= 8; ++c; }
     while (n % 4 == 0) { n /= 4; ++c; }
     while (n % 2 == 0) { n /= 2; ++c; }
     while (n % 3 == 0) { n /= 3; ++c; }
     return n == 1 ? c : -1;
 }
-__host__ __device__ constexpr int sched_radix(int n, int s) {
+__host__ __device__ constexpr int sched_radix(int n, int s, bool r16 = false) {
     int c = 0;
+    while (r16 && n % 16 == 0) { if (c++ == s) return 16; n /= 16; }
     while (n % 8 == 0) { if (c++ == s) return 8; n /= 8; }
     while (n % 4 == 0) { if (c++ == s) return 4; n /= 4; }
     while (n % 2 == 0) { if (c++ == s) return 2; n /= 2; }
@@ -85,7 +89,9 @@ template <int N, int W> struct FastPickLines {
 // every non-zero result is bitwise the same.
 template <int R, bool INV, typename C> __device__ __forceinline__ void dft_r_half_in(C* v) {
     auto rot = [](C e) { return INV ? cmake<C>(-e.y, e.x) : cmake<C>(e.y, -e.x); };  // dft4's d
-    if constexpr (R == 2) {
+    if constexpr (R == 16) {
+        dft16<INV, true>(v);
+    } else if constexpr (R == 2) {
         v[1] = v[0];
     } else if constexpr (R == 4) {
         const C x0 = v[0], x1 = v[1];
@@ -94,7 +100,7 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_r_hal
         v[2] = csub(x0, x1);
         v[3] = csub(x0, rot(x1));
     } else {
-        static_assert(R == 8, "half-input DFT for radices 2, 4, 8");
+        static_assert(R == 8, "half-input DFT for radices 2, 4, 8, 16");
         using T = typename Cx<C>::T;
         const C e0 = v[0], e1 = v[2], o0 = v[1], o1 = v[3];
         C E0 = cadd(e0, e1), E1 = cadd(e0, rot(e1)), E2 = csub(e0, e1), E3 = csub(e0, rot(e1));
@@ -121,20 +127,21 @@ struct IdentityPost {
 // stage writes point base + r N/R: with HOUT (only points < N/2 wanted, an even
 // last radix) the upper half is not written.  `post(k, v)` is applied to every
 // value the last stage writes (point k of the thread's line).
-template <int N> struct FastEnds {
-    static constexpr bool first_even = sched_radix(N, 0) % 2 == 0;
-    static constexpr bool last_even = sched_radix(N, sched_count(N) - 1) % 2 == 0;
+template <int N, bool R16 = false> struct FastEnds {
+    static constexpr bool first_even = sched_radix(N, 0, R16) % 2 == 0;
+    static constexpr bool last_even = sched_radix(N, sched_count(N, R16) - 1, R16) % 2 == 0;
 };
 
-template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, typename C, typename Post>
+template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, bool R16, typename C,
+          typename Post>
 __device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid, const Post& post) {
-    constexpr int R = sched_radix(N, S);
+    constexpr int R = sched_radix(N, S, R16);
     constexpr int NB = N / R;
     constexpr int TOT = NB * W;
     static_assert(TOT % NT == 0, "butterflies must divide evenly over the block");
     constexpr int PER = TOT / NT;
     constexpr int TSTRIDE = N / (NS * R);
-    constexpr bool LAST = S == sched_count(N) - 1;
+    constexpr bool LAST = S == sched_count(N, R16) - 1;
     constexpr bool SKIP_IN = HIN && S == 0 && R % 2 == 0;
     constexpr bool SKIP_OUT = HOUT && LAST && R % 2 == 0;
     C v[PER][R];
@@ -172,22 +179,34 @@ __device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid, const P
     __syncthreads();
 }
 
-template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, typename C, typename Post>
+template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, bool R16, typename C,
+          typename Post>
 __device__ __forceinline__ void fast_stages(C* buf, const C* tw, int tid, const Post& post) {
-    if constexpr (S < sched_count(N)) {
-        fast_stage<N, S, NS, INV, W, LS, NT, HIN, HOUT>(buf, tw, tid, post);
-        fast_stages<N, S + 1, NS * sched_radix(N, S), INV, W, LS, NT, HIN, HOUT>(buf, tw, tid, post);
+    if constexpr (S < sched_count(N, R16)) {
+        fast_stage<N, S, NS, INV, W, LS, NT, HIN, HOUT, R16>(buf, tw, tid, post);
+        fast_stages<N, S + 1, NS * sched_radix(N, S, R16), INV, W, LS, NT, HIN, HOUT, R16>(buf, tw, tid, post);
     }
 }
 
-// Whole in-place transform of the W lines in `buf` (ends synchronised).
-template <int N, int W, bool INV, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false, typename C,
-          typename Post = IdentityPost>
+// Whole in-place transform of the W lines in `buf` (ends synchronised).  R16
+// selects the schedule with radix-16 stages (E a multiple of 16).
+template <int N, int W, bool INV, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false, bool R16 = false,
+          typename C, typename Post = IdentityPost>
 __device__ __forceinline__ void fast_fft(C* buf, const C* tw, int tid, const Post& post = Post()) {
     using S = FastShape<N, W, E>;
-    fast_stages<N, 0, 1, INV, W, S::LS, S::NT, HIN && FastEnds<N>::first_even, HOUT && FastEnds<N>::last_even>(
-        buf, tw, tid, post);
+    static_assert(!R16 || E % 16 == 0, "radix-16 stages need 16 elements per thread");
+    fast_stages<N, 0, 1, INV, W, S::LS, S::NT, HIN && FastEnds<N, R16>::first_even,
+                HOUT && FastEnds<N, R16>::last_even, R16>(buf, tw, tid, post);
 }
+
+// Line kernels with 16 elements per thread take radix-16 stages where that
+// removes a stage (N = 128, 256, 1024).  The batched 2D step and the 2D
+// single-instance column pass keep the radix-8 schedule (the same rounding
+// in both, so they stay bitwise equal).
+template <int N, int E> struct FastR16 {
+    static constexpr bool value =
+        E % 16 == 0 && N % 3 != 0 && sched_count(N, true) < sched_count(N, false);
+};
 
 template <typename C>
 __device__ __forceinline__ void stage_table(C* dst, const C* __restrict__ src, int n, int tid, int nt) {
@@ -203,13 +222,14 @@ __device__ __forceinline__ void stage_table(C* dst, const C* __restrict__ src, i
 // registers.
 // stage_tw = false: the block staged this length's twiddles for an earlier
 // work item (persistent batched kernels) and they are still in shared memory.
-template <typename T, int N, int W, int MODE, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false>
+template <typename T, int N, int W, int MODE, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false,
+          bool R16 = false>
 __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid, unsigned char* smem_raw,
                                                 bool stage_tw = true) {
     using C = cplx_t<T>;
     using S = FastShape<N, W, E>;
     constexpr int LS = S::LS, NT = S::NT, PER = N * W / NT;
-    constexpr bool SKIP_LOAD = HIN && FastEnds<N>::first_even;
+    constexpr bool SKIP_LOAD = HIN && FastEnds<N, R16>::first_even;
     C* buf = reinterpret_cast<C*>(smem_raw);
     C* tw = buf + N * LS;
     const int tid = threadIdx.x;
@@ -229,9 +249,9 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
     }
     __syncthreads();
     if (MODE == LINE_INV) {
-        fast_fft<N, W, true, E, false, HOUT>(buf, tw, tid);
+        fast_fft<N, W, true, E, false, HOUT, R16>(buf, tw, tid);
     } else if (MODE == LINE_FWD) {
-        fast_fft<N, W, false, E, HIN, false>(buf, tw, tid);
+        fast_fft<N, W, false, E, HIN, false, R16>(buf, tw, tid);
     } else {
         // every element a thread touches has the same line w, so the table row
         // of that line is computed once
@@ -252,8 +272,8 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
             const T gv = live ? table[(int64_t)ks * k_stride + gbase] : T(0);
             return cscale(v, gv);
         };
-        fast_fft<N, W, false, E, HIN, false>(buf, tw, tid, green);
-        fast_fft<N, W, true, E, false, HOUT>(buf, tw, tid);
+        fast_fft<N, W, false, E, HIN, false, R16>(buf, tw, tid, green);
+        fast_fft<N, W, true, E, false, HOUT, R16>(buf, tw, tid);
     }
     C* dst = p.out + (int64_t)outer * p.outer_stride + c0;
 #pragma unroll
@@ -287,7 +307,7 @@ template <typename T, int N, int W, int MODE, int E, bool HIN, bool HOUT>
 __global__ void __launch_bounds__(FastShape<N, W, E>::NT, FastOccupancy<T, FastShape<N, W, E>::NT, E>::min_blocks)
     fast_lines_kernel(LinesParams<T> p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    fast_lines_body<T, N, W, MODE, E, HIN, HOUT>(p, blockIdx.x, smem_raw);
+    fast_lines_body<T, N, W, MODE, E, HIN, HOUT, FastR16<N, E>::value>(p, blockIdx.x, smem_raw);
 }
 
 // -------------------------------------------------------------- row kernels

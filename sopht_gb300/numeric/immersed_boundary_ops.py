@@ -20,16 +20,26 @@ KERNEL_TYPES = {"cosine": 0, "peskin": 1}
 
 
 class _PinnedStage:
-    """Pinned host staging of a float64 (dim, n) array, reused across calls.
+    """Pinned host staging of a float64 (..., dim, n) array, reused across calls.
 
     Before the buffer is overwritten, the event recorded after the previous
-    copy is waited on, so an in-flight upload never sees new data."""
+    copy is waited on, so an in-flight upload never sees new data.  ``dev``
+    may be a view into a larger device buffer (``_KinematicsStage``)."""
 
-    def __init__(self, shape, device):
+    def __init__(self, shape, device, dev=None):
         self.host = torch.empty(shape, dtype=torch.float64, pin_memory=True)
-        self.dev = torch.empty(shape, dtype=torch.float64, device=device)
+        self.dev = torch.empty(shape, dtype=torch.float64, device=device) if dev is None else dev
         self.event = torch.cuda.Event()
         self.pending = False
+
+    def _wait(self):
+        if self.pending:
+            self.event.synchronize()
+
+    def _send(self):
+        self.dev.copy_(self.host, non_blocking=True)
+        self.event.record()
+        self.pending = True
 
     def upload(self, arr) -> torch.Tensor:
         if isinstance(arr, torch.Tensor) and arr.is_cuda:
@@ -37,13 +47,37 @@ class _PinnedStage:
                 return arr
             self.dev.copy_(arr)
             return self.dev
-        if self.pending:
-            self.event.synchronize()
+        self._wait()
         self.host.numpy()[...] = np.asarray(arr if not isinstance(arr, torch.Tensor) else arr.numpy())
-        self.dev.copy_(self.host, non_blocking=True)
-        self.event.record()
-        self.pending = True
+        self._send()
         return self.dev
+
+
+class _KinematicsStage:
+    """Marker positions and velocities staged together: one pinned copy per call.
+
+    ``pos`` and ``vel`` are the per-array stages; their device buffers are the
+    two halves of one (2, dim, n) device array, so a call that has both on the
+    host sends them in a single transfer."""
+
+    def __init__(self, dim, n, device):
+        self.both = _PinnedStage((2, dim, n), device)
+        self.pos = _PinnedStage((dim, n), device, dev=self.both.dev[0])
+        self.vel = _PinnedStage((dim, n), device, dev=self.both.dev[1])
+
+    def upload(self, position, velocity):
+        host_pair = not (isinstance(position, torch.Tensor) and position.is_cuda) and not (
+            isinstance(velocity, torch.Tensor) and velocity.is_cuda)
+        if not host_pair:
+            return self.pos.upload(position), self.vel.upload(velocity)
+        self.pos._wait()
+        self.vel._wait()
+        self.both._wait()
+        h = self.both.host.numpy()
+        h[0] = np.asarray(position if not isinstance(position, torch.Tensor) else position.numpy())
+        h[1] = np.asarray(velocity if not isinstance(velocity, torch.Tensor) else velocity.numpy())
+        self.both._send()
+        return self.pos.dev, self.vel.dev
 
 
 class VirtualBoundaryForcing:
@@ -82,8 +116,9 @@ class VirtualBoundaryForcing:
         self.lag_grid_velocity_mismatch_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
         self.lag_grid_forcing_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self._pos_stage = _PinnedStage((grid_dim, n), dev)
-        self._vel_stage = _PinnedStage((grid_dim, n), dev)
+        self._kin_stage = _KinematicsStage(grid_dim, n, dev)
+        self._pos_stage = self._kin_stage.pos
+        self._vel_stage = self._kin_stage.vel
         self.enable_eul_grid_forcing_reset = enable_eul_grid_forcing_reset
         if enable_eul_grid_forcing_reset:
             self.compute_interaction_forcing = (
@@ -102,8 +137,7 @@ class VirtualBoundaryForcing:
     def _interaction(self, eul_velocity, position, body_velocity, xi_step=False, xi_dt=0.0, dev_scalars=None):
         if eul_velocity.dtype != torch_dtype(self.real_t):
             raise ValueError("Eulerian velocity dtype does not match real_t")
-        pos = self._pos_stage.upload(position)
-        vel = self._vel_stage.upload(body_velocity)
+        pos, vel = self._kin_stage.upload(position, body_velocity)
         nz, ny, nx = self._extent(eul_velocity)
         _lib.call("sg_ib_interaction", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, float(self.dx),
                   float(self.eul_grid_coord_shift), self.num_lag_nodes, KERNEL_TYPES[self.interp_kernel_type],

@@ -255,8 +255,7 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
         """Refresh the device copies of the marker positions and velocities."""
         self.forcing_grid.compute_lag_grid_position_field()
         self.forcing_grid.compute_lag_grid_velocity_field()
-        self._pos_stage.upload(self.forcing_grid.position_field)
-        self._vel_stage.upload(self.forcing_grid.velocity_field)
+        self._kin_stage.upload(self.forcing_grid.position_field, self.forcing_grid.velocity_field)
 
     def lag_grid_forcing_host(self) -> np.ndarray:
         """The Lagrangian forcing on the host (synchronises)."""

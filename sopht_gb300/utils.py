@@ -64,8 +64,24 @@ def default_device(device=None) -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+_cuda_ready = False
+
+
 def stream_ptr(device: torch.device | None = None) -> int:
-    """Raw cudaStream_t of torch's current stream on ``device``."""
+    """Raw cudaStream_t of torch's current stream on ``device``.
+
+    Read straight from torch's C++ stream registry when that entry point exists
+    (it does in the torch releases this package supports): the public
+    ``torch.cuda.current_stream(device)`` builds a Stream object per call,
+    which costs several microseconds on every operator call."""
+    global _cuda_ready
+    if _raw_stream is not None:
+        if not _cuda_ready:
+            torch.cuda.init()  # the raw lookup does not initialise CUDA itself
+            _cuda_ready = True
+        idx = device.index if device is not None and device.index is not None else torch.cuda.current_device()
+        return _raw_stream(idx)
     return torch.cuda.current_stream(device).cuda_stream
 
 
