@@ -118,6 +118,53 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_r_hal
     }
 }
 
+// v[r] *= w^r, r = 1 .. R-1, with w = tw[step] (conjugated for the inverse).
+// The powers of two are read from the table and the other powers are formed
+// as products of at most two of them, each used as soon as it exists: a
+// radix-8 butterfly reads 3 twiddles (not 7) and a radix-16 one 4 (not 15).
+// In the line passes the twiddle reads had been as many shared-memory
+// accesses as the butterfly data itself.
+template <int R, bool INV, typename C>
+__device__ __forceinline__ void apply_stage_twiddles(C* v, const C* tw, int step) {
+    auto ld = [&](int r) {
+        C w = tw[r * step];
+        if (INV) w.y = -w.y;
+        return w;
+    };
+    if constexpr (R == 3 || R == 5 || R == 7) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], ld(r));
+    } else {
+        const C w1 = ld(1);
+        v[1] = cmul(v[1], w1);
+        if constexpr (R >= 4) {
+            const C w2 = ld(2);
+            v[2] = cmul(v[2], w2);
+            const C w3 = cmul(w2, w1);
+            v[3] = cmul(v[3], w3);
+            if constexpr (R >= 8) {
+                const C w4 = ld(4);
+                v[4] = cmul(v[4], w4);
+                v[5] = cmul(v[5], cmul(w4, w1));
+                v[6] = cmul(v[6], cmul(w4, w2));
+                v[7] = cmul(v[7], cmul(w4, w3));
+                if constexpr (R >= 16) {
+                    const C w8 = ld(8);
+                    v[8] = cmul(v[8], w8);
+                    v[9] = cmul(v[9], cmul(w8, w1));
+                    v[10] = cmul(v[10], cmul(w8, w2));
+                    v[11] = cmul(v[11], cmul(w8, w3));
+                    const C w12 = cmul(w8, w4);
+                    v[12] = cmul(v[12], w12);
+                    v[13] = cmul(v[13], cmul(w12, w1));
+                    v[14] = cmul(v[14], cmul(w12, w2));
+                    v[15] = cmul(v[15], cmul(w12, w3));
+                }
+            }
+        }
+    }
+}
+
 struct IdentityPost {
     template <typename C> __device__ __forceinline__ C operator()(int, C v) const { return v; }
 };
@@ -132,8 +179,8 @@ template <int N, bool R16 = false> struct FastEnds {
     static constexpr bool last_even = sched_radix(N, sched_count(N, R16) - 1, R16) % 2 == 0;
 };
 
-template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, bool R16, typename C,
-          typename Post>
+template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, bool R16, bool TWP,
+          typename C, typename Post>
 __device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid, const Post& post) {
     constexpr int R = sched_radix(N, S, R16);
     constexpr int NB = N / R;
@@ -159,11 +206,15 @@ __device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid, const P
         const int line = t % W, j = t / W;
         const int k = j % NS;
         if (NS > 1) {
+            if constexpr (TWP) {
+                apply_stage_twiddles<R, INV>(v[b], tw, k * TSTRIDE);
+            } else {
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                C w = tw[r * k * TSTRIDE];
-                if (INV) w.y = -w.y;
-                v[b][r] = cmul(v[b][r], w);
+                for (int r = 1; r < R; ++r) {
+                    C w = tw[r * k * TSTRIDE];
+                    if (INV) w.y = -w.y;
+                    v[b][r] = cmul(v[b][r], w);
+                }
             }
         }
         if constexpr (SKIP_IN) dft_r_half_in<R, INV>(v[b]);
@@ -179,24 +230,27 @@ __device__ __forceinline__ void fast_stage(C* buf, const C* tw, int tid, const P
     __syncthreads();
 }
 
-template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, bool R16, typename C,
-          typename Post>
+template <int N, int S, int NS, bool INV, int W, int LS, int NT, bool HIN, bool HOUT, bool R16, bool TWP,
+          typename C, typename Post>
 __device__ __forceinline__ void fast_stages(C* buf, const C* tw, int tid, const Post& post) {
     if constexpr (S < sched_count(N, R16)) {
-        fast_stage<N, S, NS, INV, W, LS, NT, HIN, HOUT, R16>(buf, tw, tid, post);
-        fast_stages<N, S + 1, NS * sched_radix(N, S, R16), INV, W, LS, NT, HIN, HOUT, R16>(buf, tw, tid, post);
+        fast_stage<N, S, NS, INV, W, LS, NT, HIN, HOUT, R16, TWP>(buf, tw, tid, post);
+        fast_stages<N, S + 1, NS * sched_radix(N, S, R16), INV, W, LS, NT, HIN, HOUT, R16, TWP>(buf, tw, tid, post);
     }
 }
 
 // Whole in-place transform of the W lines in `buf` (ends synchronised).  R16
-// selects the schedule with radix-16 stages (E a multiple of 16).
+// selects the schedule with radix-16 stages (E a multiple of 16).  TWP forms
+// the stage twiddles from their powers of two (apply_stage_twiddles): measured
+// on GB300 it helps the shared-memory-bound line passes and slows the row
+// passes, which read the whole table.
 template <int N, int W, bool INV, int E = FastElems<N>::E, bool HIN = false, bool HOUT = false, bool R16 = false,
-          typename C, typename Post = IdentityPost>
+          bool TWP = false, typename C, typename Post = IdentityPost>
 __device__ __forceinline__ void fast_fft(C* buf, const C* tw, int tid, const Post& post = Post()) {
     using S = FastShape<N, W, E>;
     static_assert(!R16 || E % 16 == 0, "radix-16 stages need 16 elements per thread");
     fast_stages<N, 0, 1, INV, W, S::LS, S::NT, HIN && FastEnds<N, R16>::first_even,
-                HOUT && FastEnds<N, R16>::last_even, R16>(buf, tw, tid, post);
+                HOUT && FastEnds<N, R16>::last_even, R16, TWP>(buf, tw, tid, post);
 }
 
 // Line kernels with 16 elements per thread take radix-16 stages where that
@@ -249,9 +303,9 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
     }
     __syncthreads();
     if (MODE == LINE_INV) {
-        fast_fft<N, W, true, E, false, HOUT, R16>(buf, tw, tid);
+        fast_fft<N, W, true, E, false, HOUT, R16, true>(buf, tw, tid);
     } else if (MODE == LINE_FWD) {
-        fast_fft<N, W, false, E, HIN, false, R16>(buf, tw, tid);
+        fast_fft<N, W, false, E, HIN, false, R16, true>(buf, tw, tid);
     } else {
         // every element a thread touches has the same line w, so the table row
         // of that line is computed once
@@ -272,8 +326,8 @@ __device__ __forceinline__ void fast_lines_body(const LinesParams<T>& p, int bid
             const T gv = live ? table[(int64_t)ks * k_stride + gbase] : T(0);
             return cscale(v, gv);
         };
-        fast_fft<N, W, false, E, HIN, false, R16>(buf, tw, tid, green);
-        fast_fft<N, W, true, E, false, HOUT, R16>(buf, tw, tid);
+        fast_fft<N, W, false, E, HIN, false, R16, true>(buf, tw, tid, green);
+        fast_fft<N, W, true, E, false, HOUT, R16, true>(buf, tw, tid);
     }
     C* dst = p.out + (int64_t)outer * p.outer_stride + c0;
 #pragma unroll
