@@ -19,9 +19,11 @@
  *    call: SG_F32 (float) or SG_F64 (double).  Marker positions and body
  *    velocities are always double, as the reference's forcing grids hold them.
  *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
- *  - Only the *_create functions allocate device memory (and synchronise).
- *    Step and operator calls never allocate and never synchronise, so they can
- *    be recorded in a CUDA graph.
+ *  - Only the *_create functions and sg_ib_bind allocate memory (and the
+ *    *_create functions synchronise).  Step and operator calls never allocate
+ *    and never synchronise, so they can be recorded in a CUDA graph; the host
+ *    reads (sg_flow_host_max, sg_flow_read_device_time, sg_ib_binding_wait)
+ *    block and say so.
  *
  * Each declaration cites the reference interface it replaces (file:line within
  * the SophT repository).
@@ -136,6 +138,11 @@ int sg_flow_step(sg_flow_plan plan, void* vorticity, void* velocity, void* forci
  * Written as a double to the device pointer `out` (an 8-byte slot).  */
 int sg_max_abs_sum(int dtype, int dim, int64_t n_cells, const void* velocity, double* out,
                    void* stream);
+/* The same max of the plan's grid for a host-side stable dt
+ * (navier_stokes_flow_simulators.py:212-223 read the max on the host):
+ * reduced into the plan's slot, copied through a plan-owned pinned word and
+ * returned in *host_out after `stream` has drained (synchronous). */
+int sg_flow_host_max(sg_flow_plan plan, const void* velocity, double* host_out, void* stream);
 /* Device-resident stable dt: recomputes the plan's max from `velocity` when it
  * is not NULL, then evaluates compute_advection_diffusion_stable_timestep
  * (passive_transport_flow_simulators.py:139-155) times dt_prefac, and the step
@@ -271,6 +278,35 @@ int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag,
 /* VirtualBoundaryForcing.time_step (:276-283): xi += dt * dU. */
 int sg_ib_mismatch_step(int dtype, int n, void* position_mismatch,
                         const void* velocity_mismatch, double dt, void* stream);
+
+/* Bound coupling of one interactor: the per-step call of an immersed body,
+ * ImmersedBodyFlowInteraction.__call__ (immersed_body_flow_interaction.py:
+ * 113-122: upload the marker kinematics, interact, spread), as one host call.
+ * sg_ib_bind records the interactor's fixed arguments (those of
+ * sg_ib_interaction, the Eulerian extent, and a (2, dim, n_lag) float64
+ * device buffer receiving positions then velocities) and allocates two
+ * pinned staging slots of that layout plus a pinned (dim, n_lag) buffer of
+ * the field type for the Lagrangian forcing; sg_ib_binding_buffers returns
+ * their host addresses. */
+typedef struct sg_ib_binding_s* sg_ib_binding;
+int sg_ib_bind(int dtype, int dim, int nz, int ny, int nx, double dx, double shift, int n_lag,
+               int kernel_type, int32_t* nearest, void* weights, void* flow_velocity,
+               void* velocity_mismatch, void* position_mismatch, void* forcing,
+               int32_t* status_dev, double* dev_kinematics, sg_ib_binding* binding_out);
+int sg_ib_binding_buffers(sg_ib_binding binding, double** kin_slot0, double** kin_slot1,
+                          void** forcing_host);
+/* Blocks until staging slot `which` (0 or 1) may be overwritten (its upload
+ * has run), or, for which = 2, until the last queued forcing copy has landed. */
+int sg_ib_binding_wait(sg_ib_binding binding, int which);
+/* On `stream`: when kin_slot is 0 or 1, copy that staging slot to the device
+ * kinematics buffer; then sg_ib_interaction on it (xi step as there, host dt
+ * only); then, when spread_mode >= 0, sg_ib_spread with reset = spread_mode;
+ * then, when copy_forcing != 0, copy the Lagrangian forcing to the pinned
+ * forcing buffer (completion: sg_ib_binding_wait(binding, 2)). */
+int sg_ib_bound_step(sg_ib_binding binding, int kin_slot, const void* eul_velocity,
+                     void* eul_forcing, int spread_mode, double stiffness, double damping,
+                     int do_xi_step, double xi_dt, int copy_forcing, void* stream);
+int sg_ib_unbind(sg_ib_binding binding);
 
 /* ------------------------------------------------------------- adjoints */
 /* Transposes of the 2D step's operators and of the virtual-boundary

@@ -67,6 +67,7 @@ _SIGNATURES = {
     "sg_flow_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, POINTER(StepScalars), c_void_p,
                              c_void_p]),
     "sg_max_abs_sum": (c_int, [c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p]),
+    "sg_flow_host_max": (c_int, [c_void_p, c_void_p, POINTER(c_double), c_void_p]),
     "sg_flow_device_dt": (c_int, [c_void_p, c_void_p, c_double, c_double, c_double, c_double, POINTER(c_double),
                                   POINTER(c_void_p), c_void_p]),
     "sg_advection_eno3_step_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p]),
@@ -90,6 +91,13 @@ _SIGNATURES = {
     "sg_ib_spread": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_int, c_void_p]),
     "sg_ib_mismatch_step": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, c_void_p]),
+    "sg_ib_bind": (c_int, [c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int, c_int, c_void_p, c_void_p,
+                           c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, POINTER(c_void_p)]),
+    "sg_ib_binding_buffers": (c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p)]),
+    "sg_ib_binding_wait": (c_int, [c_void_p, c_int]),
+    "sg_ib_bound_step": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_double, c_double, c_int, c_double,
+                                 c_int, c_void_p]),
+    "sg_ib_unbind": (c_int, [c_void_p]),
     # adjoints
     "sg_adj_partials_count_2d": (c_int64, [c_int, c_int]),
     "sg_sum_partials": (c_int, [c_int64, c_void_p, c_void_p, c_void_p]),

@@ -18,10 +18,16 @@
 namespace sg {
 
 // Record timing event `i` of the armed set (no-op when none is armed).
-// The external flag makes the record a node of a graph being captured (a plain
-// record during capture only orders streams); outside capture it is a normal record.
+// While `stream` is being captured the external flag makes the record a node of
+// the graph (a plain record during capture only orders streams); outside capture
+// the record is a plain one (the external flag is refused there).
 static inline void mark(sg_flow_plan_s* p, int i, cudaStream_t stream) {
-    if (i < p->n_events && p->events[i]) cudaEventRecordWithFlags(p->events[i], stream, cudaEventRecordExternal);
+    if (i >= p->n_events || !p->events[i]) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(p->events[i], stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(p->events[i], stream);
 }
 
 static void flow_plan_free(sg_flow_plan_s* p) {
@@ -35,6 +41,9 @@ static void flow_plan_free(sg_flow_plan_s* p) {
     cudaFree(p->coef_y);
     cudaFree(p->coef_z);
     cudaFree(p->dev_block);
+    cudaFreeHost(p->host_word);
+    if (p->step_exec) cudaGraphExecDestroy(p->step_exec);
+    if (p->capture_stream) cudaStreamDestroy(p->capture_stream);
     delete p;
 }
 
@@ -406,6 +415,7 @@ extern "C" int sg_flow_plan_create(int dim, int nz, int ny, int nx, double x_ran
         }
         if ((st = alloc_into((void**)&p->dev_block, 128, &p->bytes, "flow device block alloc"))) break;
         if ((st = cuda_status(cudaMemset(p->dev_block, 0, 128), "flow device block init"))) break;
+        if ((st = cuda_status(cudaMallocHost(&p->host_word, 16), "flow pinned word alloc"))) break;
         st = cuda_status(cudaDeviceSynchronize(), "flow plan create");
     } while (0);
     if (st != SG_OK) {
@@ -442,6 +452,22 @@ extern "C" int sg_flow_prime_max(sg_flow_plan p, const void* velocity, void* str
     return launch_max_abs_sum<double>(p->cells(), p->dim, (const double*)velocity, (double*)p->umax_slot(), stream);
 }
 
+extern "C" int sg_flow_host_max(sg_flow_plan p, const void* velocity, double* host_out, void* stream_) {
+    SG_REQUIRE(p && velocity && host_out, SG_ERR_INVALID_ARG, "host max: null argument");
+    auto stream = (cudaStream_t)stream_;
+    const size_t esz = p->dtype == SG_F32 ? sizeof(float) : sizeof(double);
+    if (p->dtype == SG_F32)
+        SG_TRY(launch_max_abs_sum<float>(p->cells(), p->dim, (const float*)velocity, (float*)p->umax_slot(), stream));
+    else
+        SG_TRY(launch_max_abs_sum<double>(p->cells(), p->dim, (const double*)velocity, (double*)p->umax_slot(),
+                                          stream));
+    SG_TRY(cuda_status(cudaMemcpyAsync(p->host_word, p->umax_slot(), esz, cudaMemcpyDeviceToHost, stream),
+                       "host max copy"));
+    SG_TRY(cuda_status(cudaStreamSynchronize(stream), "host max sync"));
+    *host_out = p->dtype == SG_F32 ? (double)*(const float*)p->host_word : *(const double*)p->host_word;
+    return SG_OK;
+}
+
 extern "C" int sg_flow_read_device_time(sg_flow_plan p, double* host_out) {
     SG_REQUIRE(p && host_out, SG_ERR_INVALID_ARG, "read device time: null argument");
     return cuda_status(cudaMemcpy(host_out, p->time_slot(), sizeof(double), cudaMemcpyDeviceToHost),
@@ -455,6 +481,87 @@ extern "C" int sg_flow_plan_destroy(sg_flow_plan p) {
 
 extern "C" int64_t sg_flow_plan_bytes(sg_flow_plan p) { return p ? p->bytes : 0; }
 
+static int flow_step_dispatch(sg_flow_plan_s* p, void* w, void* u, void* f, void* psi, const ScalarSrc& sc, bool fs,
+                              cudaStream_t stream) {
+    if (p->dtype == SG_F32)
+        return p->dim == 2 ? flow_step_2d<float>(p, (float*)w, (float*)u, (float*)f, (float*)psi, sc, fs, stream)
+                           : flow_step_3d<float>(p, (float*)w, (float*)u, (float*)f, (float*)psi, sc, fs, stream);
+    return p->dim == 2 ? flow_step_2d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream)
+                       : flow_step_3d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream);
+}
+
+__global__ void set_step_scalars_kernel(sg_step_scalars v, sg_step_scalars* dst) { *dst = v; }
+
+static void flow_graph_disable(sg_flow_plan_s* p) {
+    cudaGetLastError();  // a failed capture leaves no sticky error: the direct launches follow
+    p->graph_disabled = true;
+    if (p->step_exec) cudaGraphExecDestroy(p->step_exec);
+    p->step_exec = nullptr;
+}
+
+// The host-scalar step as one graph replay (2 launches instead of 6 to 10).  The graph is the
+// device-scalar form of the same step, so every kernel gets the same scalars and pointers as a direct
+// launch.  *used = false leaves the step to the direct launches (caller stream being captured,
+// graphs disabled, capture failed).
+static int flow_step_graph(sg_flow_plan_s* p, void* w, void* u, void* f, void* psi, const sg_step_scalars& host,
+                           bool fs, cudaStream_t stream, bool* used) {
+    *used = false;
+    if (p->graph_disabled) return SG_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return SG_OK;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return SG_OK;
+    const bool match = p->step_exec && p->graph_fields[0] == w && p->graph_fields[1] == u &&
+                       p->graph_fields[2] == f && p->graph_fields[3] == psi && p->graph_free_stream == fs;
+    if (!match) {
+        if (p->graph_builds >= 8) {  // fields that keep moving: direct launches from now on
+            flow_graph_disable(p);
+            return SG_OK;
+        }
+        ++p->graph_builds;
+        if (p->step_exec) cudaGraphExecDestroy(p->step_exec);
+        p->step_exec = nullptr;
+        if (!p->capture_stream && cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            p->capture_stream = nullptr;
+            flow_graph_disable(p);
+            return SG_OK;
+        }
+        if (cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            flow_graph_disable(p);
+            return SG_OK;
+        }
+        ScalarSrc dsc{};
+        dsc.dev = p->dev_scalars();
+        const int st = flow_step_dispatch(p, w, u, f, psi, dsc, fs, p->capture_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(p->capture_stream, &g);
+        if (st != SG_OK || e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            flow_graph_disable(p);
+            return SG_OK;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&p->step_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            p->step_exec = nullptr;
+            flow_graph_disable(p);
+            return SG_OK;
+        }
+        p->graph_fields[0] = w;
+        p->graph_fields[1] = u;
+        p->graph_fields[2] = f;
+        p->graph_fields[3] = psi;
+        p->graph_free_stream = fs;
+    }
+    set_step_scalars_kernel<<<1, 1, 0, stream>>>(host, p->dev_scalars());
+    SG_TRY(launch_status("flow step scalars"));
+    SG_TRY(cuda_status(cudaGraphLaunch(p->step_exec, stream), "flow step graph launch"));
+    *used = true;
+    return SG_OK;
+}
+
 extern "C" int sg_flow_step(sg_flow_plan p, void* w, void* u, void* f, void* psi, const sg_step_scalars* scalars,
                             const sg_step_scalars* dev_scalars, void* stream_) {
     SG_REQUIRE(p && w && u && psi, SG_ERR_INVALID_ARG, "flow step: null argument");
@@ -466,14 +573,11 @@ extern "C" int sg_flow_step(sg_flow_plan p, void* w, void* u, void* f, void* psi
                                                           scalars->free_stream[1] != 0.0 ||
                                                           scalars->free_stream[2] != 0.0));
     auto stream = (cudaStream_t)stream_;
-    int st;
-    if (p->dtype == SG_F32) {
-        st = p->dim == 2 ? flow_step_2d<float>(p, (float*)w, (float*)u, (float*)f, (float*)psi, sc, fs, stream)
-                         : flow_step_3d<float>(p, (float*)w, (float*)u, (float*)f, (float*)psi, sc, fs, stream);
-    } else {
-        st = p->dim == 2 ? flow_step_2d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream)
-                         : flow_step_3d<double>(p, (double*)w, (double*)u, (double*)f, (double*)psi, sc, fs, stream);
-    }
+    int st = SG_OK;
+    bool done = false;
+    if (!dev_scalars && p->n_events == 0 && !p->tape_w1)
+        st = flow_step_graph(p, w, u, f, psi, *scalars, fs, stream, &done);
+    if (st == SG_OK && !done) st = flow_step_dispatch(p, w, u, f, psi, sc, fs, stream);
     p->n_events = 0;  // timing events and the tape are armed for one step only
     p->tape_w1 = p->tape_w2 = nullptr;
     return st;

@@ -19,6 +19,8 @@ struct sg_flow_plan_s {
     void* coef_z = nullptr;
     // device block: [0, 64) sg_step_scalars, [64, 72) umax (field type), [72, 80) time
     unsigned char* dev_block = nullptr;
+    // pinned host word the host-side stable dt reads the max through
+    void* host_word = nullptr;
     int64_t bytes = 0;
     // optional one-shot timing events recorded between the passes of the next step
     int n_events = 0;
@@ -26,6 +28,15 @@ struct sg_flow_plan_s {
     // optional one-shot tape of the next 2D step's sweep intermediates (adjoint)
     void* tape_w1 = nullptr;
     void* tape_w2 = nullptr;
+    // CUDA graph of the step with host scalars: captured once per set of field pointers from the
+    // device-scalar form of the step (the scalars are written to dev_scalars() by a one-thread
+    // kernel before each replay); disabled after repeated rebuilds or a failed capture
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t step_exec = nullptr;
+    void* graph_fields[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool graph_free_stream = false;
+    bool graph_disabled = false;
+    int graph_builds = 0;
     sg_step_scalars* dev_scalars() const { return reinterpret_cast<sg_step_scalars*>(dev_block); }
     void* umax_slot() const { return dev_block + 64; }
     double* time_slot() const { return reinterpret_cast<double*>(dev_block + 72); }

@@ -26,12 +26,12 @@ static void ib_interaction_launch(const IBParams<T>& p, cudaStream_t stream) {
     else ib_interaction_kernel<T, 3><<<blocks, 64, 0, stream>>>(p);
 }
 
-extern "C" int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, double dx, double shift, int n_lag,
-                                 int kernel_type, const double* position, const double* body_velocity,
-                                 const void* eul_velocity, int32_t* nearest, void* weights, void* flow_velocity,
-                                 void* velocity_mismatch, void* position_mismatch, void* forcing, double stiffness,
-                                 double damping, int do_xi_step, double xi_dt, const sg_step_scalars* dev_scalars,
-                                 int32_t* status_dev, void* stream_) {
+static int ib_interaction_impl(int dtype, int dim, int nz, int ny, int nx, double dx, double shift, int n_lag,
+                               int kernel_type, const double* position, const double* body_velocity,
+                               const void* eul_velocity, int32_t* nearest, void* weights, void* flow_velocity,
+                               void* velocity_mismatch, void* position_mismatch, void* forcing, double stiffness,
+                               double damping, int do_xi_step, double xi_dt, const sg_step_scalars* dev_scalars,
+                               int32_t* status_dev, cudaStream_t stream) {
     SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "ib interaction: dim must be 2 or 3");
     SG_REQUIRE(n_lag >= 1, SG_ERR_INVALID_ARG, "ib interaction: n_lag must be >= 1");
     SG_REQUIRE(kernel_type == 0 || kernel_type == 1, SG_ERR_INVALID_ARG, "ib interaction: bad kernel type");
@@ -40,7 +40,6 @@ extern "C" int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, dou
                SG_ERR_INVALID_ARG, "ib interaction: null argument");
     SG_REQUIRE(dx > 0, SG_ERR_INVALID_ARG, "ib interaction: dx must be positive");
     if (dim == 2) nz = 1;
-    auto stream = (cudaStream_t)stream_;
     if (dtype == SG_F32) {
         IBParams<float> p{dim, nz, ny, nx, n_lag, kernel_type, dx, shift, position, body_velocity,
                           (const float*)eul_velocity, nearest, (float*)weights, (float*)flow_velocity,
@@ -56,6 +55,18 @@ extern "C" int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, dou
         ib_interaction_launch<double>(p, stream);
     }
     return launch_status("ib_interaction");
+}
+
+extern "C" int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, double dx, double shift, int n_lag,
+                                 int kernel_type, const double* position, const double* body_velocity,
+                                 const void* eul_velocity, int32_t* nearest, void* weights, void* flow_velocity,
+                                 void* velocity_mismatch, void* position_mismatch, void* forcing, double stiffness,
+                                 double damping, int do_xi_step, double xi_dt, const sg_step_scalars* dev_scalars,
+                                 int32_t* status_dev, void* stream_) {
+    return ib_interaction_impl(dtype, dim, nz, ny, nx, dx, shift, n_lag, kernel_type, position, body_velocity,
+                               eul_velocity, nearest, weights, flow_velocity, velocity_mismatch, position_mismatch,
+                               forcing, stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev,
+                               (cudaStream_t)stream_);
 }
 
 template <typename T>
@@ -76,13 +87,12 @@ static void ib_spread_launch(const SpreadParams<T>& p, cudaStream_t stream) {
     }
 }
 
-extern "C" int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag, const int32_t* nearest,
-                            const void* weights, const void* forcing, void* eul_forcing, int reset, void* stream_) {
+static int ib_spread_impl(int dtype, int dim, int nz, int ny, int nx, int n_lag, const int32_t* nearest,
+                          const void* weights, const void* forcing, void* eul_forcing, int reset, cudaStream_t stream) {
     SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "ib spread: dim must be 2 or 3");
     SG_REQUIRE(nearest && weights && forcing && eul_forcing && n_lag >= 1, SG_ERR_INVALID_ARG,
                "ib spread: bad argument");
     if (dim == 2) nz = 1;
-    auto stream = (cudaStream_t)stream_;
     const int64_t ncell = (int64_t)nz * ny * nx;
     if (dtype == SG_F32) {
         if (reset) {
@@ -103,10 +113,149 @@ extern "C" int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_la
     return launch_status("ib_spread");
 }
 
+extern "C" int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag, const int32_t* nearest,
+                            const void* weights, const void* forcing, void* eul_forcing, int reset, void* stream_) {
+    return ib_spread_impl(dtype, dim, nz, ny, nx, n_lag, nearest, weights, forcing, eul_forcing, reset,
+                          (cudaStream_t)stream_);
+}
+
 extern "C" int sg_ib_mismatch_step(int dtype, int n, void* xi, const void* du, double dt, void* stream_) {
     SG_REQUIRE(xi && du && n >= 1, SG_ERR_INVALID_ARG, "ib mismatch step: bad argument");
     auto stream = (cudaStream_t)stream_;
     if (dtype == SG_F32) mismatch_step_kernel<float><<<ceil_div(n, 256), 256, 0, stream>>>(n, (float*)xi, (const float*)du, dt);
     else mismatch_step_kernel<double><<<ceil_div(n, 256), 256, 0, stream>>>(n, (double*)xi, (const double*)du, dt);
     return launch_status("ib_mismatch_step");
+}
+
+// ---------------------------------------------------------------- bound coupling
+// One interactor's fixed arguments, its pinned staging and its events, so that
+// the per-step host call (VirtualBoundaryForcing.__call__ of an immersed body:
+// upload the marker kinematics, interact, spread, and queue the copy of the
+// Lagrangian forcing a host body integrator reads) is one call of few arguments.
+struct sg_ib_binding_s {
+    int dtype = SG_F32, dim = 2, nz = 1, ny = 0, nx = 0, n_lag = 0, kernel = 0;
+    double dx = 0.0, shift = 0.0;
+    int32_t* nearest = nullptr;
+    void* weights = nullptr;
+    void* flow_velocity = nullptr;
+    void* vel_mismatch = nullptr;
+    void* pos_mismatch = nullptr;
+    void* lag_forcing = nullptr;
+    int32_t* status = nullptr;
+    double* dev_kin = nullptr;          // (2, dim, n_lag) float64 on the device: positions, velocities
+    double* kin_host[2] = {nullptr, nullptr};  // pinned staging slots, same layout
+    cudaEvent_t kin_done[2] = {nullptr, nullptr};
+    void* forcing_host = nullptr;       // pinned (dim, n_lag) of the field type
+    cudaEvent_t forcing_done = nullptr;
+};
+
+static void ib_binding_free(sg_ib_binding_s* b) {
+    if (!b) return;
+    for (int k = 0; k < 2; ++k) {
+        if (b->kin_done[k]) cudaEventDestroy(b->kin_done[k]);
+        cudaFreeHost(b->kin_host[k]);
+    }
+    if (b->forcing_done) cudaEventDestroy(b->forcing_done);
+    cudaFreeHost(b->forcing_host);
+    delete b;
+}
+
+extern "C" int sg_ib_bind(int dtype, int dim, int nz, int ny, int nx, double dx, double shift, int n_lag,
+                          int kernel_type, int32_t* nearest, void* weights, void* flow_velocity,
+                          void* velocity_mismatch, void* position_mismatch, void* forcing, int32_t* status_dev,
+                          double* dev_kinematics, sg_ib_binding* out) {
+    SG_REQUIRE(out, SG_ERR_INVALID_ARG, "ib bind: null output");
+    *out = nullptr;
+    SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, SG_ERR_INVALID_ARG, "ib bind: bad dtype");
+    SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "ib bind: dim must be 2 or 3");
+    SG_REQUIRE(n_lag >= 1 && ny >= 1 && nx >= 1 && (dim == 2 || nz >= 1), SG_ERR_INVALID_ARG, "ib bind: bad size");
+    SG_REQUIRE(kernel_type == 0 || kernel_type == 1, SG_ERR_INVALID_ARG, "ib bind: bad kernel type");
+    SG_REQUIRE(dx > 0, SG_ERR_INVALID_ARG, "ib bind: dx must be positive");
+    SG_REQUIRE(nearest && weights && flow_velocity && velocity_mismatch && position_mismatch && forcing &&
+                   status_dev && dev_kinematics,
+               SG_ERR_INVALID_ARG, "ib bind: null argument");
+    auto* b = new sg_ib_binding_s();
+    b->dtype = dtype;
+    b->dim = dim;
+    b->nz = dim == 2 ? 1 : nz;
+    b->ny = ny;
+    b->nx = nx;
+    b->n_lag = n_lag;
+    b->kernel = kernel_type;
+    b->dx = dx;
+    b->shift = shift;
+    b->nearest = nearest;
+    b->weights = weights;
+    b->flow_velocity = flow_velocity;
+    b->vel_mismatch = velocity_mismatch;
+    b->pos_mismatch = position_mismatch;
+    b->lag_forcing = forcing;
+    b->status = status_dev;
+    b->dev_kin = dev_kinematics;
+    const size_t kin_bytes = (size_t)2 * dim * n_lag * sizeof(double);
+    const size_t f_bytes = (size_t)dim * n_lag * (dtype == SG_F32 ? sizeof(float) : sizeof(double));
+    int st = SG_OK;
+    for (int k = 0; k < 2 && st == SG_OK; ++k) {
+        st = cuda_status(cudaMallocHost((void**)&b->kin_host[k], kin_bytes), "ib bind: pinned staging");
+        if (st == SG_OK)
+            st = cuda_status(cudaEventCreateWithFlags(&b->kin_done[k], cudaEventDisableTiming), "ib bind: event");
+    }
+    if (st == SG_OK) st = cuda_status(cudaMallocHost(&b->forcing_host, f_bytes), "ib bind: pinned forcing");
+    if (st == SG_OK)
+        st = cuda_status(cudaEventCreateWithFlags(&b->forcing_done, cudaEventDisableTiming), "ib bind: event");
+    if (st != SG_OK) {
+        ib_binding_free(b);
+        return st;
+    }
+    *out = b;
+    return SG_OK;
+}
+
+extern "C" int sg_ib_binding_buffers(sg_ib_binding b, double** kin_slot0, double** kin_slot1, void** forcing_host) {
+    SG_REQUIRE(b && kin_slot0 && kin_slot1 && forcing_host, SG_ERR_INVALID_ARG, "ib buffers: null argument");
+    *kin_slot0 = b->kin_host[0];
+    *kin_slot1 = b->kin_host[1];
+    *forcing_host = b->forcing_host;
+    return SG_OK;
+}
+
+extern "C" int sg_ib_binding_wait(sg_ib_binding b, int which) {
+    SG_REQUIRE(b && which >= 0 && which <= 2, SG_ERR_INVALID_ARG, "ib wait: bad argument");
+    return cuda_status(cudaEventSynchronize(which < 2 ? b->kin_done[which] : b->forcing_done), "ib wait");
+}
+
+extern "C" int sg_ib_bound_step(sg_ib_binding b, int kin_slot, const void* eul_velocity, void* eul_forcing,
+                                int spread_mode, double stiffness, double damping, int do_xi_step, double xi_dt,
+                                int copy_forcing, void* stream_) {
+    SG_REQUIRE(b && eul_velocity, SG_ERR_INVALID_ARG, "ib bound step: null argument");
+    SG_REQUIRE(kin_slot >= -1 && kin_slot <= 1, SG_ERR_INVALID_ARG, "ib bound step: bad staging slot");
+    SG_REQUIRE(spread_mode >= -1 && spread_mode <= 1, SG_ERR_INVALID_ARG, "ib bound step: bad spread mode");
+    SG_REQUIRE(spread_mode < 0 || eul_forcing, SG_ERR_INVALID_ARG, "ib bound step: no Eulerian forcing");
+    auto stream = (cudaStream_t)stream_;
+    const int64_t nk = (int64_t)b->dim * b->n_lag;
+    if (kin_slot >= 0) {
+        SG_TRY(cuda_status(cudaMemcpyAsync(b->dev_kin, b->kin_host[kin_slot], (size_t)2 * nk * sizeof(double),
+                                           cudaMemcpyHostToDevice, stream),
+                           "ib bound step: kinematics upload"));
+        SG_TRY(cuda_status(cudaEventRecord(b->kin_done[kin_slot], stream), "ib bound step: event"));
+    }
+    SG_TRY(ib_interaction_impl(b->dtype, b->dim, b->nz, b->ny, b->nx, b->dx, b->shift, b->n_lag, b->kernel,
+                               b->dev_kin, b->dev_kin + nk, eul_velocity, b->nearest, b->weights, b->flow_velocity,
+                               b->vel_mismatch, b->pos_mismatch, b->lag_forcing, stiffness, damping, do_xi_step,
+                               xi_dt, nullptr, b->status, stream));
+    if (spread_mode >= 0)
+        SG_TRY(ib_spread_impl(b->dtype, b->dim, b->nz, b->ny, b->nx, b->n_lag, b->nearest, b->weights,
+                              b->lag_forcing, eul_forcing, spread_mode, stream));
+    if (copy_forcing) {
+        const size_t f_bytes = (size_t)nk * (b->dtype == SG_F32 ? sizeof(float) : sizeof(double));
+        SG_TRY(cuda_status(cudaMemcpyAsync(b->forcing_host, b->lag_forcing, f_bytes, cudaMemcpyDeviceToHost, stream),
+                           "ib bound step: forcing copy"));
+        SG_TRY(cuda_status(cudaEventRecord(b->forcing_done, stream), "ib bound step: event"));
+    }
+    return SG_OK;
+}
+
+extern "C" int sg_ib_unbind(sg_ib_binding b) {
+    ib_binding_free(b);
+    return SG_OK;
 }

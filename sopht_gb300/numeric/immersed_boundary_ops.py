@@ -10,6 +10,8 @@ kernel; spreading is a deterministic owner-ordered kernel without atomics.
 
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -80,8 +82,76 @@ class _KinematicsStage:
         return self.pos.dev, self.vel.dev
 
 
+class _IBBinding:
+    """Native binding of one interactor's buffers (``sg_ib_bind``).
+
+    Owns two pinned staging slots for the marker kinematics, used in turn, and
+    a pinned buffer receiving the Lagrangian forcing; ``step`` is one native
+    call (kinematics upload, interaction, spreading, forcing copy)."""
+
+    def __init__(self, vbf, key, eul_velocity):
+        nz, ny, nx = vbf._extent(eul_velocity)
+        dim, n = vbf.grid_dim, vbf.num_lag_nodes
+        self.key = key
+        self.handle = ctypes.c_void_p()
+        with torch.cuda.device(vbf.device):
+            _lib.call("sg_ib_bind", sg_dtype(vbf.real_t), dim, nz, ny, nx, float(vbf.dx),
+                      float(vbf.eul_grid_coord_shift), n, KERNEL_TYPES[vbf.interp_kernel_type],
+                      ptr(vbf.nearest_eul_grid_index_to_lag_grid), ptr(vbf.interp_weights),
+                      ptr(vbf.lag_grid_flow_velocity_field), ptr(vbf._du), ptr(vbf._xi),
+                      ptr(vbf.lag_grid_forcing_field), ptr(vbf._status), ptr(vbf._kin_stage.both.dev),
+                      ctypes.byref(self.handle))
+        self._lib = _lib.load()
+        s0, s1, fh = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.call("sg_ib_binding_buffers", self.handle, ctypes.byref(s0), ctypes.byref(s1), ctypes.byref(fh))
+        dbl = ctypes.POINTER(ctypes.c_double)
+        self.kin = [np.ctypeslib.as_array(ctypes.cast(a.value, dbl), shape=(2, dim, n)) for a in (s0, s1)]
+        ftype = ctypes.c_float if vbf.real_t == np.float32 else ctypes.c_double
+        self.forcing = np.ctypeslib.as_array(ctypes.cast(fh.value, ctypes.POINTER(ftype)), shape=(dim, n))
+        self.slot = 1
+        self.used = [False, False]
+
+    def wait(self, which: int) -> None:
+        st = self._lib.sg_ib_binding_wait(self.handle, which)
+        if st != _lib.SG_OK:
+            _lib.call("sg_ib_binding_wait", self.handle, which)  # raises with the library's message
+
+    def stage(self, position, velocity) -> int:
+        """Write the kinematics into the next staging slot (after its previous upload ran)."""
+        slot = self.slot ^ 1
+        self.slot = slot
+        if self.used[slot]:
+            self.wait(slot)
+        self.used[slot] = True
+        v = self.kin[slot]
+        v[0] = position
+        v[1] = velocity
+        return slot
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._lib.sg_ib_unbind(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
 class VirtualBoundaryForcing:
-    """Feedback F = K xi + C dU between a Lagrangian body and the Eulerian flow."""
+    """Feedback F = K xi + C dU between a Lagrangian body and the Eulerian flow.
+
+    ``time_step(dt)`` (xi += dt * dU) is deferred and folded into the next
+    interaction launch, which applies the same update in the same precision
+    before it reads xi.  Any access to ``lag_grid_position_mismatch_field`` or
+    ``lag_grid_velocity_mismatch_field`` in between first applies the pending
+    update on its own, so every read sees the reference's order of operations.
+    The pending update runs on the stream current at the time it is applied.
+    """
+
+    _pending_xi_dt = None
+    _xi = None
+    _du = None
 
     def __init__(self, virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, grid_dim, dx,
                  num_lag_nodes, real_t, eul_grid_coord_shift=None, interp_kernel_width=None,
@@ -112,8 +182,9 @@ class VirtualBoundaryForcing:
         self.nearest_eul_grid_index_to_lag_grid = torch.zeros((grid_dim, n), dtype=torch.int32, device=dev)
         self.interp_weights = torch.zeros(((2 * interp_kernel_width) ** grid_dim, n), dtype=tdt, device=dev)
         self.lag_grid_flow_velocity_field = torch.zeros((grid_dim, n), dtype=tdt, device=dev)
-        self.lag_grid_position_mismatch_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
-        self.lag_grid_velocity_mismatch_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
+        self._xi = torch.zeros_like(self.lag_grid_flow_velocity_field)
+        self._du = torch.zeros_like(self.lag_grid_flow_velocity_field)
+        self._n_interactions = 0
         self.lag_grid_forcing_field = torch.zeros_like(self.lag_grid_flow_velocity_field)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._kin_stage = _KinematicsStage(grid_dim, n, dev)
@@ -126,6 +197,34 @@ class VirtualBoundaryForcing:
         else:
             self.compute_interaction_forcing = self.compute_interaction_force_on_eul_and_lag_grid
 
+    @property
+    def lag_grid_position_mismatch_field(self) -> torch.Tensor:
+        self._flush_time_step()
+        return self._xi
+
+    @lag_grid_position_mismatch_field.setter
+    def lag_grid_position_mismatch_field(self, value: torch.Tensor) -> None:
+        self._flush_time_step()
+        self._xi = value
+
+    @property
+    def lag_grid_velocity_mismatch_field(self) -> torch.Tensor:
+        self._flush_time_step()
+        return self._du
+
+    @lag_grid_velocity_mismatch_field.setter
+    def lag_grid_velocity_mismatch_field(self, value: torch.Tensor) -> None:
+        self._flush_time_step()
+        self._du = value
+
+    def _flush_time_step(self) -> None:
+        """Apply a deferred ``time_step`` now (its own kernel)."""
+        dt = self._pending_xi_dt
+        if dt is not None:
+            self._pending_xi_dt = None
+            _lib.call("sg_ib_mismatch_step", sg_dtype(self.real_t), self.grid_dim * self.num_lag_nodes,
+                      ptr(self._xi), ptr(self._du), dt, stream_ptr(self.device))
+
     # -- grid extent of a field (component first)
     def _extent(self, field):
         if self.grid_dim == 2:
@@ -137,13 +236,21 @@ class VirtualBoundaryForcing:
     def _interaction(self, eul_velocity, position, body_velocity, xi_step=False, xi_dt=0.0, dev_scalars=None):
         if eul_velocity.dtype != torch_dtype(self.real_t):
             raise ValueError("Eulerian velocity dtype does not match real_t")
+        pending = self._pending_xi_dt
+        if pending is not None:
+            if xi_step or dev_scalars is not None:
+                self._flush_time_step()
+            else:  # the deferred time_step rides on this launch
+                self._pending_xi_dt = None
+                xi_step, xi_dt = True, pending
         pos, vel = self._kin_stage.upload(position, body_velocity)
         nz, ny, nx = self._extent(eul_velocity)
+        self._n_interactions += 1
         _lib.call("sg_ib_interaction", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, float(self.dx),
                   float(self.eul_grid_coord_shift), self.num_lag_nodes, KERNEL_TYPES[self.interp_kernel_type],
                   ptr(pos), ptr(vel), ptr(eul_velocity), ptr(self.nearest_eul_grid_index_to_lag_grid),
                   ptr(self.interp_weights), ptr(self.lag_grid_flow_velocity_field),
-                  ptr(self.lag_grid_velocity_mismatch_field), ptr(self.lag_grid_position_mismatch_field),
+                  ptr(self._du), ptr(self._xi),
                   ptr(self.lag_grid_forcing_field), float(self.virtual_boundary_stiffness_coeff),
                   float(self.virtual_boundary_damping_coeff), int(xi_step), float(xi_dt), dev_scalars,
                   ptr(self._status), stream_ptr(self.device))
@@ -180,8 +287,7 @@ class VirtualBoundaryForcing:
         self._spread(eul_grid_forcing_field, reset=True)
 
     def time_step(self, dt):
-        """VirtualBoundaryForcing.py:276-283: xi += dt * dU."""
-        _lib.call("sg_ib_mismatch_step", sg_dtype(self.real_t), self.grid_dim * self.num_lag_nodes,
-                  ptr(self.lag_grid_position_mismatch_field), ptr(self.lag_grid_velocity_mismatch_field),
-                  float(self.real_t(dt)), stream_ptr(self.device))
+        """VirtualBoundaryForcing.py:276-283: xi += dt * dU (deferred to the next interaction)."""
+        self._flush_time_step()
+        self._pending_xi_dt = float(self.real_t(dt))
         self.time += dt

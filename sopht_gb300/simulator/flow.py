@@ -120,7 +120,9 @@ class _UnboundedNavierStokesBase(FlowSimulator):
             _lib.call("sg_flow_plan_create", self.grid_dim, nz, ny, nx, float(self.x_range), sg_dtype(self.real_t),
                       int(w), host[0] if w > 0 else None, host[1] if w > 0 else None,
                       host[2] if w > 0 else None, self._filter_type, self._filter_order, ctypes.byref(self._plan))
-        self._umax_slot = torch.zeros(1, dtype=torch.float64, device=self.device)
+        self._host_max = ctypes.c_double()
+        self._host_max_ref = ctypes.byref(self._host_max)
+        self._checked_fields = None
 
     @property
     def device_bytes(self) -> int:
@@ -160,10 +162,16 @@ class _UnboundedNavierStokesBase(FlowSimulator):
         return sc
 
     def _step(self, scalars_ptr, dev_scalars):
-        self._check_fields()
         forcing = self.eul_grid_forcing_field if self.with_forcing else None
-        _lib.call("sg_flow_step", self._plan, ptr(self.vorticity_field), ptr(self.velocity_field), ptr(forcing),
-                  ptr(self.stream_func_field), scalars_ptr, dev_scalars, stream_ptr(self.device))
+        w, u, psi = self.vorticity_field, self.velocity_field, self.stream_func_field
+        key = (w, u, psi, forcing, w.data_ptr(), u.data_ptr(), psi.data_ptr())
+        c = self._checked_fields
+        if c is None or any(a is not b for a, b in zip(c[:4], key[:4])) or c[4:] != key[4:]:
+            # dtype, layout and device are checked again only when a field object or its storage changes
+            self._check_fields()
+            self._checked_fields = key
+        _lib.call("sg_flow_step", self._plan, key[4], key[5], ptr(forcing), key[6], scalars_ptr, dev_scalars,
+                  stream_ptr(self.device))
 
     def _flow_time_step(self, dt, free_stream_velocity=None):
         if free_stream_velocity is None:
@@ -174,14 +182,14 @@ class _UnboundedNavierStokesBase(FlowSimulator):
     def compute_stable_timestep(self, dt_prefac: float = 1.0):
         """navier_stokes_flow_simulators.py:212-223 / :501-512 (synchronises).
 
-        The max of sum_d |u_d| is reduced on the GPU; the dt formula of
+        The max of sum_d |u_d| is reduced on the GPU and read back through a
+        pinned word of the plan (one call, one stream drain); the dt formula of
         passive_transport_flow_simulators.py:139-155 is then evaluated on the
         host with the reference's numpy scalar types, so the value is the same.
         """
-        n = int(np.prod(self.grid_size))
-        _lib.call("sg_max_abs_sum", sg_dtype(self.real_t), self.grid_dim, n, ptr(self.velocity_field),
-                  ptr(self._umax_slot), stream_ptr(self.device))
-        umax = self.real_t(self._umax_slot.item())
+        _lib.call("sg_flow_host_max", self._plan, ptr(self.velocity_field), self._host_max_ref,
+                  stream_ptr(self.device))
+        umax = self.real_t(self._host_max.value)
         rt = self.real_t
         tol = 10 * np.finfo(rt).eps
         dt = min(self.cfl * self.dx / (umax + tol),

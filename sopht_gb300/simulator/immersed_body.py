@@ -19,7 +19,9 @@ from abc import abstractmethod
 import numpy as np
 import torch
 
-from ..numeric.immersed_boundary_ops import VirtualBoundaryForcing
+from .. import _lib
+from ..numeric.immersed_boundary_ops import VirtualBoundaryForcing, _IBBinding
+from ..utils import ptr, stream_ptr
 
 logger = logging.getLogger(__name__)
 
@@ -226,6 +228,13 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
                          interp_kernel_type=interp_kernel_type, device=eul_grid_forcing_field.device)
         self._host_forcing = torch.empty(self.lag_grid_forcing_field.shape, dtype=self.lag_grid_forcing_field.dtype,
                                          pin_memory=True)
+        # early copy of the Lagrangian forcing, taken right after the interaction of ``__call__`` once a
+        # caller has read it: a later read waits for that copy only, not for the rest of the step
+        self._snapshot_wanted = False
+        self._snapshot_key = None
+        self._snapshot_src = None
+        self._snapshot_event = torch.cuda.Event()
+        self._binding = None
 
     def compute_interaction_on_lag_grid(self) -> None:
         self.forcing_grid.compute_lag_grid_position_field()
@@ -234,12 +243,60 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
                                                    self.forcing_grid.velocity_field)
 
     def __call__(self) -> None:
-        self.forcing_grid.compute_lag_grid_position_field()
-        self.forcing_grid.compute_lag_grid_velocity_field()
-        self.compute_interaction_forcing(eul_grid_forcing_field=self.eul_grid_forcing_field,
-                                         eul_grid_velocity_field=self.eul_grid_velocity_field,
-                                         lag_grid_position_field=self.forcing_grid.position_field,
-                                         lag_grid_velocity_field=self.forcing_grid.velocity_field)
+        fg = self.forcing_grid
+        fg.compute_lag_grid_position_field()
+        fg.compute_lag_grid_velocity_field()
+        b = self._bound(fg)
+        if b is None:
+            self.compute_interaction_forcing(eul_grid_forcing_field=self.eul_grid_forcing_field,
+                                             eul_grid_velocity_field=self.eul_grid_velocity_field,
+                                             lag_grid_position_field=fg.position_field,
+                                             lag_grid_velocity_field=fg.velocity_field)
+            if self._snapshot_wanted:
+                self._host_forcing.copy_(self.lag_grid_forcing_field, non_blocking=True)
+                if torch.cuda.current_device() == self.device.index:
+                    self._snapshot_event.record()
+                else:  # the copy ran on the forcing field's device
+                    self._snapshot_event.record(torch.cuda.current_stream(self.device))
+                self._snapshot_key = (self._n_interactions, self.lag_grid_forcing_field._version)
+                self._snapshot_src = None
+            return
+        # one native call: kinematics upload, interaction (with a deferred time_step), spreading, and the
+        # early copy of the Lagrangian forcing once a caller reads it
+        slot = b.stage(fg.position_field, fg.velocity_field)
+        pending = self._pending_xi_dt
+        self._pending_xi_dt = None
+        self._n_interactions += 1
+        snap = self._snapshot_wanted
+        _lib.call("sg_ib_bound_step", b.handle, slot, ptr(self.eul_grid_velocity_field),
+                  ptr(self.eul_grid_forcing_field), 1 if self.enable_eul_grid_forcing_reset else 0,
+                  float(self.virtual_boundary_stiffness_coeff), float(self.virtual_boundary_damping_coeff),
+                  0 if pending is None else 1, 0.0 if pending is None else pending, 1 if snap else 0,
+                  stream_ptr(self.device))
+        if snap:
+            self._snapshot_key = (self._n_interactions, self.lag_grid_forcing_field._version)
+            self._snapshot_src = b
+
+    def _bound(self, fg):
+        """The native binding of this interactor's buffers, or None where the generic path applies
+        (kinematics that are not host arrays, an Eulerian field of another dtype or layout)."""
+        if not (isinstance(fg.position_field, np.ndarray) and isinstance(fg.velocity_field, np.ndarray)):
+            return None
+        u, f = self.eul_grid_velocity_field, self.eul_grid_forcing_field
+        key = (self.nearest_eul_grid_index_to_lag_grid, self.interp_weights, self.lag_grid_flow_velocity_field,
+               self._du, self._xi, self.lag_grid_forcing_field, self._status, u, f)
+        b = self._binding
+        if b is not None and all(x is y for x, y in zip(b.key, key)):
+            return b
+        self._binding = None
+        tdt = self.lag_grid_forcing_field.dtype
+        for t in (u, f):
+            if not isinstance(t, torch.Tensor) or t.dtype != tdt or t.device != self.device or not t.is_contiguous():
+                return None
+        if u.shape != f.shape:
+            return None
+        self._binding = b = _IBBinding(self, key, u)
+        return b
 
     def device_call(self, dev_scalars: int) -> None:
         """``time_step(dt)`` then ``__call__()`` with dt read on the GPU (one kernel pair).
@@ -258,9 +315,24 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
         self._kin_stage.upload(self.forcing_grid.position_field, self.forcing_grid.velocity_field)
 
     def lag_grid_forcing_host(self) -> np.ndarray:
-        """The Lagrangian forcing on the host (synchronises)."""
-        self._host_forcing.copy_(self.lag_grid_forcing_field)
-        return self._host_forcing.numpy()
+        """A host copy of the Lagrangian forcing (waits for the GPU work that produces it).
+
+        When the forcing still holds what the last ``__call__`` computed, the
+        pinned copy queued right after that interaction is returned (the wait
+        ends there, not at the end of the flow step queued after it); otherwise
+        the field is copied now."""
+        self._snapshot_wanted = True
+        if self._snapshot_key is not None and self._snapshot_key == (self._n_interactions,
+                                                                     self.lag_grid_forcing_field._version):
+            src = self._snapshot_src
+            if src is not None:
+                src.wait(2)
+                return src.forcing.copy()
+            self._snapshot_event.synchronize()
+        else:
+            self._host_forcing.copy_(self.lag_grid_forcing_field)
+            self._snapshot_key = None
+        return self._host_forcing.numpy().copy()
 
     def compute_flow_forces_and_torques(self) -> None:
         """immersed_body_flow_interaction.py:124-131 (one device->host read)."""
