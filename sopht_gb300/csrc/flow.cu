@@ -106,7 +106,7 @@ int launch_curl2d(const Curl2DParams<T>& p, cudaStream_t stream) {
 
 template <typename T>
 int launch_curl3d(const Curl3DParams<T>& p, int64_t n, cudaStream_t stream) {
-    curl3d_kernel<T><<<ceil_div(n, 256), 256, 0, stream>>>(p);
+    curl3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, stream>>>(p);
     return launch_status("curl3d");
 }
 
@@ -125,7 +125,7 @@ int filter3d(Grid3 G, T* field, int filter_type, int order, T* a, T* b, cudaStre
             for (int it = 0; it < order; ++it) {
                 for (int axis = 0; axis < 3; ++axis) {
                     T* dst = bufs[which];
-                    filter_pass3d_kernel<T><<<blocks, 256, 0, stream>>>(G, src, dst, axis);
+                    filter_pass3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(G, src, dst, axis);
                     src = dst;
                     which ^= 1;
                 }
@@ -139,7 +139,7 @@ int filter3d(Grid3 G, T* field, int filter_type, int order, T* a, T* b, cudaStre
                 int which = 0;
                 for (int it = 0; it < order; ++it) {
                     T* dst = bufs[which];
-                    filter_pass3d_kernel<T><<<blocks, 256, 0, stream>>>(G, src, dst, axis);
+                    filter_pass3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(G, src, dst, axis);
                     src = dst;
                     which ^= 1;
                 }
@@ -238,7 +238,6 @@ template <typename T>
 int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& sc, bool free_stream,
                  cudaStream_t stream) {
     const int64_t n = p->cells();
-    const unsigned blocks = ceil_div(n, 256);
     Grid3 G{p->nz, p->ny, p->nx};
     T* A = (T*)p->scratch_a;
     T* B = (T*)p->scratch_b;
@@ -254,7 +253,7 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         s.out = A;
         s.sc = sc;
         s.mode = 0;
-        forcing_curl3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
+        forcing_curl3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(s);
         SG_TRY(launch_status("forcing_curl3d"));
         w1 = A;
     }
@@ -265,7 +264,7 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         s.b = u;
         s.out = B;
         s.sc = sc;
-        rotational_update3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
+        rotational_update3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(s);
         SG_TRY(launch_status("rotational_update3d"));
     }
     {
@@ -275,7 +274,7 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         s.out = A;
         s.sc = sc;
         s.mode = 0;
-        diffusion3d_kernel<T><<<blocks, 256, 0, stream>>>(s);
+        diffusion3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(s);
         SG_TRY(launch_status("diffusion3d"));
     }
     SG_TRY(filter3d<T>(G, A, p->filter_type, p->filter_order, (T*)p->filt_a, (T*)p->filt_b, stream));

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(FastShape<M, W, E>::NT) fast_flow_load_kernel(
 }
 
 // ---------------------------------------- curl + free stream + max |u| (2D)
+// Non-negative values order like their bit patterns, so an integer atomicMax on the bits is the float max.
 template <typename T>
 __device__ __forceinline__ void atomic_max_nonneg(T* slot, T v);
 template <>
@@ -371,6 +372,24 @@ __device__ __forceinline__ void atomic_max_nonneg<float>(float* slot, float v) {
 template <>
 __device__ __forceinline__ void atomic_max_nonneg<double>(double* slot, double v) {
     atomicMax(reinterpret_cast<unsigned long long*>(slot), (unsigned long long)__double_as_longlong(v));
+}
+
+// The same for grids of many blocks: a value not above the slot's current content cannot change the
+// max and skips the atomic, so after the first blocks most of the grid reads the slot instead of
+// queueing on one address (3D curl: 65 536 blocks at 256^3).  Small grids (under one wave) keep the
+// plain atomic: there the read only lengthens each block's tail.
+template <typename T>
+__device__ __forceinline__ void atomic_max_nonneg_filtered(T* slot, T v);
+template <>
+__device__ __forceinline__ void atomic_max_nonneg_filtered<float>(float* slot, float v) {
+    const int bits = __float_as_int(v);
+    if (bits > *reinterpret_cast<volatile int*>(slot)) atomicMax(reinterpret_cast<int*>(slot), bits);
+}
+template <>
+__device__ __forceinline__ void atomic_max_nonneg_filtered<double>(double* slot, double v) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    if (bits > *reinterpret_cast<volatile unsigned long long*>(slot))
+        atomicMax(reinterpret_cast<unsigned long long*>(slot), bits);
 }
 
 template <typename T>
@@ -441,6 +460,22 @@ struct Grid3 {
     }
 };
 
+// Launch shape of the cell-wise 3D kernels: 32 x 8 threads over (x, y) of one z-plane per block, so a
+// thread's cell comes from its block and thread coordinates (no 64-bit division per thread).
+constexpr int kCell3X = 32, kCell3Y = 8;
+inline dim3 cell3_grid(const Grid3& G) {
+    return dim3((unsigned)((G.nx + kCell3X - 1) / kCell3X), (unsigned)((G.ny + kCell3Y - 1) / kCell3Y),
+                (unsigned)G.nz);
+}
+inline dim3 cell3_block() { return dim3(kCell3X, kCell3Y); }
+__device__ __forceinline__ bool cell3(const Grid3& G, int& x, int& y, int& z, int64_t& g) {
+    x = blockIdx.x * kCell3X + threadIdx.x;
+    y = blockIdx.y * kCell3Y + threadIdx.y;
+    z = blockIdx.z;
+    g = ((int64_t)z * G.ny + y) * G.nx + x;
+    return x < G.nx && y < G.ny;
+}
+
 // out = w + pf * curl_h(v) on [1:-1]^3 (w elsewhere)  — per component as
 // update_vorticity_from_velocity_forcing_3d.py:29-94 writes it.
 template <typename T>
@@ -468,9 +503,9 @@ template <typename T>
 __global__ void __launch_bounds__(256) forcing_curl3d_kernel(Stencil3DParams<T> p) {
     const Grid3 G = p.grid;
     const int64_t n = G.n();
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
-    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    int x, y, z;
+    int64_t g;
+    if (!cell3(G, x, y, z, g)) return;
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
     T w0 = p.a[g], w1 = p.a[n + g], w2 = p.a[2 * n + g];
     if (p.b && G.interior(z, y, x)) {
@@ -501,9 +536,9 @@ template <typename T>
 __global__ void __launch_bounds__(256) rotational_update3d_kernel(Stencil3DParams<T> p) {
     const Grid3 G = p.grid;
     const int64_t n = G.n();
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
-    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    int x, y, z;
+    int64_t g;
+    if (!cell3(G, x, y, z, g)) return;
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
     T w0 = p.a[g], w1 = p.a[n + g], w2 = p.a[2 * n + g];
     if (G.interior(z, y, x)) {
@@ -529,9 +564,9 @@ template <typename T>
 __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) {
     const Grid3 G = p.grid;
     const int64_t n = G.n();
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
-    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    int x, y, z;
+    int64_t g;
+    if (!cell3(G, x, y, z, g)) return;
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
     const T k = p.mode == 0 ? (T)p.sc.diffusion() : p.prefactor;
     const bool in = G.interior(z, y, x);
@@ -552,10 +587,9 @@ __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) 
 // zero ring (laplacian_filter_3d.py:55-73), scalar field.
 template <typename T>
 __global__ void __launch_bounds__(256) filter_pass3d_kernel(Grid3 G, const T* in, T* out, int axis) {
-    const int64_t n = G.n();
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
-    const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    int x, y, z;
+    int64_t g;
+    if (!cell3(G, x, y, z, g)) return;
     const int64_t s = axis == 0 ? 1 : (axis == 1 ? (int64_t)G.nx : (int64_t)G.nx * G.ny);
     T v = T(0);
     if (G.interior(z, y, x)) v = T(0.25) * (-in[g + s] - in[g - s] + T(2) * in[g]);
@@ -591,10 +625,10 @@ template <typename T>
 __global__ void __launch_bounds__(256) curl3d_kernel(Curl3DParams<T> p) {
     const Grid3 G = p.grid;
     const int64_t n = G.n();
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int x, y, z;
+    int64_t g;
     T m = T(0);
-    if (g < n) {
-        const int x = (int)(g % G.nx), y = (int)((g / G.nx) % G.ny), z = (int)(g / ((int64_t)G.nx * G.ny));
+    if (cell3(G, x, y, z, g)) {
         T c[3] = {T(0), T(0), T(0)};
         if (G.interior(z, y, x)) {
             curl3_at(p.psi, g, n, (int64_t)G.nx, (int64_t)G.nx * G.ny, c);
@@ -613,7 +647,7 @@ __global__ void __launch_bounds__(256) curl3d_kernel(Curl3DParams<T> p) {
     }
     if (p.umax) {
         m = block_max(m);
-        if (threadIdx.x == 0) atomic_max_nonneg(p.umax, m);
+        if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg_filtered(p.umax, m);
     }
 }
 

@@ -176,17 +176,15 @@ static int stencil3d_op(int which, int nz, int ny, int nx, const void* a, const 
     p.out = (T*)out;
     p.prefactor = (T)pref;
     p.mode = 1;
-    const int64_t n = (int64_t)nz * ny * nx;
-    const unsigned blocks = ceil_div(n, 256);
-    if (which == 0) forcing_curl3d_kernel<T><<<blocks, 256, 0, s>>>(p);
-    else if (which == 1) diffusion3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+    if (which == 0) forcing_curl3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
+    else if (which == 1) diffusion3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
     else {
         Curl3DParams<T> c{};
         c.grid = p.grid;
         c.psi = (const T*)a;
         c.u = (T*)out;
         c.prefactor = (T)pref;
-        curl3d_kernel<T><<<blocks, 256, 0, s>>>(c);
+        curl3d_kernel<T><<<cell3_grid(c.grid), cell3_block(), 0, s>>>(c);
     }
     return launch_status("stencil3d op");
 }
