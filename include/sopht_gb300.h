@@ -246,6 +246,29 @@ int sg_penalise_3d(int dtype, int nz, int ny, int nx, const void* field_in, void
 int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* field, int filter_type,
                            int filter_order, void* scratch_a, void* scratch_b, void* stream);
 
+/* ------------------------------------------------------ passive transport */
+/* Replaces the 3D conservative ENO3 advection timestep
+ * (stencil_ops_3d/advection_timestep_3d.py:38-96 with advection_flux_3d.py:
+ * 12-233): out = in + flux on [2:-2]^3 (out = in elsewhere), inv_dx = -dt_by_dx,
+ * for `ncomp` components spaced nz*ny*nx apart (all advected by the same
+ * (3, nz, ny, nx) velocity).  in and out must not alias. */
+int sg_advection_eno3_step_3d(int dtype, int nz, int ny, int nx, int ncomp, const void* in,
+                              void* out, const void* velocity, double dt_by_dx, void* stream);
+/* Replaces gen_advection_flux_conservative_eno3_pyst_kernel_3d
+ * (advection_flux_3d.py:12-233): flux += the six face fluxes of a scalar field,
+ * in the reference's pass order, on [2:-2]^3 (in place on `flux`). */
+int sg_advection_eno3_flux_3d(int dtype, int nz, int ny, int nx, const void* field, void* flux,
+                              const void* velocity, double inv_dx, void* stream);
+/* Replaces PassiveTransportFlowSimulator._advection_and_diffusion_time_step
+ * (simulator/flow/passive_transport_flow_simulators.py:104-118): each of the
+ * `ncomp` components of `field` (1 in 2D; 1 or 3 in 3D) is advected by ENO3
+ * with dt_by_dx and then diffused with nu_dt_by_dx2, in place.  `scratch` is
+ * one scalar field of the grid (the simulator's buffer_scalar_field); in 2D
+ * the two operators run as one fused sweep. */
+int sg_passive_transport_step(int dtype, int dim, int nz, int ny, int nx, int ncomp, void* field,
+                              void* scratch, const void* velocity, double dt_by_dx,
+                              double nu_dt_by_dx2, void* stream);
+
 /* ------------------------------------------------------ immersed boundary */
 /* Replaces VirtualBoundaryForcing.compute_interaction_force_on_lag_grid
  * (immersed_boundary_ops/VirtualBoundaryForcing.py:187-230) with the

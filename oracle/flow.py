@@ -156,6 +156,51 @@ class NavierStokes3DOracle:
         self.time += dt
 
 
+class PassiveTransportOracle:
+    """PassiveTransportFlowSimulator (passive_transport_flow_simulators.py:14-136).
+
+    One step is the ENO3 advection step then the diffusion step of the primary
+    field (:104-118); a 3D vector field is advected and diffused component by
+    component.  The stable dt is passive_transport_flow_simulators.py:139-155.
+    """
+
+    def __init__(self, kinematic_viscosity, grid_dim, grid_size, x_range, cfl=0.1, real_t=np.float32,
+                 time=0.0, field_type="scalar"):
+        if field_type not in ("scalar", "vector"):
+            raise ValueError("Invalid field type. Supported values include 'scalar' and 'vector'")
+        if grid_dim == 2 and field_type == "vector":
+            raise ValueError("Passive transport of vector 2D fields not supported yet.")
+        self.nu = kinematic_viscosity
+        self.grid_dim = grid_dim
+        self.grid_size = tuple(grid_size)
+        self.cfl = cfl
+        self.real_t = real_t
+        self.time = time
+        self.field_type = field_type
+        self.dx, self.position_field = position_field(self.grid_size, x_range, real_t)
+        shape = self.grid_size if field_type == "scalar" else (grid_dim, *self.grid_size)
+        self.primary_field = np.zeros(shape, dtype=real_t)
+        self.velocity_field = np.zeros((grid_dim, *self.grid_size), dtype=real_t)
+
+    def compute_stable_timestep(self, dt_prefac=1.0):
+        return stable_timestep(self.velocity_field, self.grid_dim, self.dx, self.cfl, self.nu, self.real_t,
+                               dt_prefac)
+
+    def time_step(self, dt):
+        rt, dx = self.real_t, self.dx
+        dt_by_dx = rt(dt / dx)
+        k = rt(self.nu * dt / dx / dx)
+        if self.grid_dim == 2:
+            st.advection_step_2d(self.primary_field, self.velocity_field, dt_by_dx)
+            st.diffusion_step_2d(self.primary_field, k)
+        else:
+            comps = self.primary_field[None] if self.field_type == "scalar" else self.primary_field
+            for c in range(comps.shape[0]):
+                st.advection_step_3d(comps[c], self.velocity_field, dt_by_dx)
+            st.diffusion_step_3d(comps, k)
+        self.time += dt
+
+
 # ---------------------------------------------------------------------------
 # forcing grids and the interaction wrapper
 # ---------------------------------------------------------------------------

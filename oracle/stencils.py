@@ -200,6 +200,48 @@ def diffusion_step_3d(vector_field, nu_dt_by_dx2):
         vector_field[c] = f + flux
 
 
+def eno3_flux_3d(field, velocity, inv_dx, out=None):
+    """Conservative ENO3 advection flux of a scalar field on [2:-2]^3 (zero elsewhere).
+
+    stencil_ops_3d/advection_flux_3d.py:12-233: six directional passes, each a
+    face flux of ``_eno3_face_flux`` along one axis, accumulated in the order
+    x-front, x-back, y-front, y-back, z-front, z-back into a zeroed buffer.
+    """
+    real_t = field.dtype.type
+    flux = np.zeros_like(field) if out is None else out
+    nz, ny, nx = field.shape
+
+    def sh(a, dz, dy, dx):
+        return a[2 + dz: nz - 2 + dz, 2 + dy: ny - 2 + dy, 2 + dx: nx - 2 + dx]
+
+    acc = None
+    for axis, u in ((2, velocity[0]), (1, velocity[1]), (0, velocity[2])):
+        q = field * u
+
+        def at(a, k, axis=axis):
+            off = [0, 0, 0]
+            off[axis] = k
+            return sh(a, *off)
+
+        front = _eno3_face_flux(at(q, -1), at(q, 0), at(q, 1), at(q, 2), at(u, 0), at(u, 1), real_t)
+        back = _eno3_face_flux(at(q, -2), at(q, -1), at(q, 0), at(q, 1), at(u, -1), at(u, 0), real_t)
+        acc = inv_dx * front if acc is None else acc + inv_dx * front
+        acc = acc - inv_dx * back
+    flux[...] = 0
+    flux[2:-2, 2:-2, 2:-2] = acc
+    return flux
+
+
+def advection_step_3d(field, velocity, dt_by_dx):
+    """Scalar field += ENO3 flux with inv_dx = -dt/dx, in place.
+
+    stencil_ops_3d/advection_timestep_3d.py:38-57 (a vector field is advected
+    component by component with the same velocity, :61-96).
+    """
+    flux = eno3_flux_3d(field, velocity, -dt_by_dx)
+    field[...] = field + flux
+
+
 def divergence_3d(field, inv_dx):
     """0.5*inv_dx * central divergence on [1:-1]^3, zero ring.  divergence_3d.py"""
     div = np.zeros_like(field[0])

@@ -85,6 +85,12 @@ _SIGNATURES = {
                                c_void_p]),
     "sg_laplacian_filter_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                        c_void_p]),
+    "sg_advection_eno3_step_3d": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double,
+                                          c_void_p]),
+    "sg_advection_eno3_flux_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double,
+                                          c_void_p]),
+    "sg_passive_transport_step": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                          c_double, c_double, c_void_p]),
     "sg_ib_interaction": (c_int, [c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int, c_int, c_void_p,
                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_double, c_double, c_int, c_double, c_void_p, c_void_p, c_void_p]),

@@ -496,6 +496,7 @@ template <typename T> struct Stencil3DParams {
     ScalarSrc sc;
     T prefactor;
     int mode;
+    int ncomp;       // components of the diffusion (0 means 3)
 };
 
 // w1 = w + pf curl(f)  (mode 0; f may be null -> copy)
@@ -570,8 +571,9 @@ __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) 
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
     const T k = p.mode == 0 ? (T)p.sc.diffusion() : p.prefactor;
     const bool in = G.interior(z, y, x);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
+    const int nc = p.ncomp ? p.ncomp : 3;
+#pragma unroll 3
+    for (int c = 0; c < nc; ++c) {
         const T* f = p.a + c * n;
         T v = f[g];
         if (in) {
@@ -581,6 +583,53 @@ __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) 
         }
         p.out[c * n + g] = v;
     }
+}
+
+// 3D conservative ENO3 advection of scalar components (advection_flux_3d.py:12-233,
+// advection_timestep_3d.py:38-96).  On [2:-2]^3 the six face fluxes are accumulated in the
+// reference's pass order (x front, x back, y front, y back, z front, z back) onto a start value:
+//   flux mode (add_field = 0): start = base, out = the accumulated flux (the flux kernel adds into
+//     its buffer; base may equal out);
+//   step mode (add_field = 1): start = 0, out = field + flux (the zeroed buffer, then the sum).
+// Outside the interior out = base (flux mode) or field (step mode).  Component c of field / base /
+// out is blockIdx.z / nz; the velocity (3 components) is shared.
+template <typename T> struct Eno3D3Params {
+    Grid3 grid;
+    const T* field;
+    const T* base;
+    T* out;
+    const T* u;      // velocity (3, nz, ny, nx)
+    T inv_dx;
+    int add_field;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) eno3_3d_kernel(Eno3D3Params<T> p) {
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int comp = blockIdx.z / G.nz;
+    const int x = blockIdx.x * kCell3X + threadIdx.x, y = blockIdx.y * kCell3Y + threadIdx.y;
+    const int z = blockIdx.z - comp * G.nz;
+    if (x >= G.nx || y >= G.ny) return;
+    const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
+    const T* f = p.field + comp * n;
+    T acc = p.add_field ? T(0) : p.base[comp * n + g];
+    const bool in = z >= 2 && z <= G.nz - 3 && y >= 2 && y <= G.ny - 3 && x >= 2 && x <= G.nx - 3;
+    if (in) {
+        const int64_t strides[3] = {1, (int64_t)G.nx, (int64_t)G.nx * G.ny};
+#pragma unroll
+        for (int axis = 0; axis < 3; ++axis) {
+            const int64_t s = strides[axis];
+            const T* ua = p.u + axis * n;
+            auto q = [&](int k) { return f[g + k * s] * ua[g + k * s]; };
+            const T um1 = ua[g - s], u0 = ua[g], up1 = ua[g + s];
+            const T front = eno3_face(q(-1), q(0), q(1), q(2), u0, up1);
+            const T back = eno3_face(q(-2), q(-1), q(0), q(1), um1, u0);
+            acc = acc + p.inv_dx * front;
+            acc = acc - p.inv_dx * back;
+        }
+    }
+    p.out[comp * n + g] = p.add_field ? f[g] + acc : acc;
 }
 
 // One 1D Laplacian filter pass g = 0.25 (2 f - f[+s] - f[-s]) on [1:-1]^3,

@@ -261,3 +261,97 @@ extern "C" int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* f
     SG_DTYPE_DISPATCH(dtype, filter3d<float>(G, (float*)field, filter_type, filter_order, (float*)a, (float*)b, s),
                       filter3d<double>(G, (double*)field, filter_type, filter_order, (double*)a, (double*)b, s));
 }
+
+// ------------------------------------------------------------ passive transport
+namespace sg {
+
+template <typename T>
+static int eno3_3d_launch(int nz, int ny, int nx, int ncomp, const void* field, const void* base, void* out,
+                          const void* u, double inv_dx, int add_field, cudaStream_t s) {
+    Eno3D3Params<T> p{};
+    p.grid = Grid3{nz, ny, nx};
+    p.field = (const T*)field;
+    p.base = (const T*)base;
+    p.out = (T*)out;
+    p.u = (const T*)u;
+    p.inv_dx = (T)inv_dx;
+    p.add_field = add_field;
+    dim3 grid = cell3_grid(p.grid);
+    grid.z = (unsigned)nz * (unsigned)ncomp;
+    eno3_3d_kernel<T><<<grid, cell3_block(), 0, s>>>(p);
+    return launch_status("eno3_3d");
+}
+
+template <typename T>
+static int diffusion3d_scalar_launch(int nz, int ny, int nx, const void* in, void* out, double k, cudaStream_t s) {
+    Stencil3DParams<T> p{};
+    p.grid = Grid3{nz, ny, nx};
+    p.a = (const T*)in;
+    p.out = (T*)out;
+    p.prefactor = (T)k;
+    p.mode = 1;
+    p.ncomp = 1;
+    diffusion3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
+    return launch_status("diffusion3d scalar");
+}
+
+// PassiveTransportFlowSimulator._advection_and_diffusion_time_step: advection then diffusion of
+// each component, in place on `field`, through one scalar scratch field.
+template <typename T>
+static int passive_step(int dim, int nz, int ny, int nx, int ncomp, void* field, void* scratch, const void* u,
+                        double dt_by_dx, double k, cudaStream_t s) {
+    if (dim == 2) {
+        // one fused sweep (ENO3 on [2:-2]^2, then diffusion of the advected field on [1:-1]^2)
+        SG_TRY(sweep_op<T>(ny, nx, field, scratch, u, nullptr, 0.0, dt_by_dx, k, SWEEP_ADVECT | SWEEP_DIFFUSE, s));
+        return cuda_status(cudaMemcpyAsync(field, scratch, (size_t)ny * nx * sizeof(T), cudaMemcpyDeviceToDevice, s),
+                           "passive step copy back");
+    }
+    const int64_t n = (int64_t)nz * ny * nx;
+    for (int c = 0; c < ncomp; ++c) {
+        T* fc = (T*)field + c * n;
+        SG_TRY(eno3_3d_launch<T>(nz, ny, nx, 1, fc, nullptr, scratch, u, -dt_by_dx, 1, s));
+        SG_TRY(diffusion3d_scalar_launch<T>(nz, ny, nx, scratch, fc, k, s));
+    }
+    return SG_OK;
+}
+
+}  // namespace sg
+
+extern "C" int sg_advection_eno3_step_3d(int dtype, int nz, int ny, int nx, int ncomp, const void* in, void* out,
+                                         const void* velocity, double dt_by_dx, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, in, out));
+    SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
+    SG_REQUIRE(ncomp >= 1 && (int64_t)nz * ncomp <= 65535, SG_ERR_SHAPE, "eno3 3d: bad component count %d", ncomp);
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, eno3_3d_launch<float>(nz, ny, nx, ncomp, in, nullptr, out, velocity, -dt_by_dx, 1, s),
+                      eno3_3d_launch<double>(nz, ny, nx, ncomp, in, nullptr, out, velocity, -dt_by_dx, 1, s));
+}
+
+extern "C" int sg_advection_eno3_flux_3d(int dtype, int nz, int ny, int nx, const void* field, void* flux,
+                                         const void* velocity, double inv_dx, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, field, flux));
+    SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
+    SG_REQUIRE(nz <= 65535, SG_ERR_SHAPE, "eno3 3d: nz too large");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, eno3_3d_launch<float>(nz, ny, nx, 1, field, flux, flux, velocity, inv_dx, 0, s),
+                      eno3_3d_launch<double>(nz, ny, nx, 1, field, flux, flux, velocity, inv_dx, 0, s));
+}
+
+extern "C" int sg_passive_transport_step(int dtype, int dim, int nz, int ny, int nx, int ncomp, void* field,
+                                         void* scratch, const void* velocity, double dt_by_dx, double nu_dt_by_dx2,
+                                         void* stream) {
+    SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "passive step: dim must be 2 or 3");
+    SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
+    if (dim == 2) {
+        SG_REQUIRE(ncomp == 1, SG_ERR_UNSUPPORTED, "passive step: a 2D field is a scalar");
+        SG_TRY(check2d(ny, nx, field, scratch));
+    } else {
+        SG_TRY(check3d(nz, ny, nx, field, scratch));
+        SG_REQUIRE(ncomp == 1 || ncomp == 3, SG_ERR_INVALID_ARG, "passive step: 1 or 3 components");
+    }
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype,
+                      passive_step<float>(dim, nz, ny, nx, ncomp, field, scratch, velocity, dt_by_dx, nu_dt_by_dx2, s),
+                      passive_step<double>(dim, nz, ny, nx, ncomp, field, scratch, velocity, dt_by_dx, nu_dt_by_dx2,
+                                           s));
+}

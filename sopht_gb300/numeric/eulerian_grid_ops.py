@@ -279,6 +279,45 @@ def gen_diffusion_timestep_euler_forward_pyst_kernel_3d(real_t, num_threads=Fals
     return kernel
 
 
+def gen_advection_flux_conservative_eno3_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False):
+    """advection_flux_3d.py:12-233: advection_flux += the six ENO3 face fluxes of a scalar field."""
+    real_t = normalize_real_t(real_t)
+
+    def kernel(advection_flux, field, velocity, inv_dx):
+        nz, ny, nx = field.shape
+        _lib.call("sg_advection_eno3_flux_3d", sg_dtype(real_t), nz, ny, nx, ptr(field), ptr(advection_flux),
+                  ptr(velocity), float(real_t(inv_dx)), stream_ptr(field.device))
+
+    return kernel
+
+
+def gen_advection_timestep_euler_forward_conservative_eno3_pyst_kernel_3d(
+        real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """advection_timestep_3d.py:12-99: field += ENO3 flux with inv_dx = -dt/dx, scalar or per
+    component of a vector field.  The scalar ``advection_flux`` buffer receives each component's
+    new values before they are copied back."""
+    real_t = normalize_real_t(real_t)
+    if field_type not in ("scalar", "vector"):
+        raise ValueError("Invalid field type")
+
+    def _step(f, buf, velocity, dt_by_dx):
+        nz, ny, nx = f.shape[-3:]
+        ncomp = 1 if f.dim() == 3 else f.shape[0]
+        for c in range(ncomp):
+            src = f if ncomp == 1 else f[c]
+            _lib.call("sg_advection_eno3_step_3d", sg_dtype(real_t), nz, ny, nx, 1, ptr(src), ptr(buf),
+                      ptr(velocity), float(real_t(dt_by_dx)), stream_ptr(f.device))
+            src.copy_(buf)
+
+    if field_type == "scalar":
+        def kernel(field, advection_flux, velocity, dt_by_dx):
+            _step(field, advection_flux, velocity, dt_by_dx)
+    else:
+        def kernel(vector_field, advection_flux, velocity, dt_by_dx):
+            _step(vector_field, advection_flux, velocity, dt_by_dx)
+    return kernel
+
+
 def gen_penalise_field_boundary_pyst_kernel_3d(width, dx, x_grid_field, y_grid_field, z_grid_field, real_t,
                                                num_threads=False, fixed_grid_size=False, field_type="scalar"):
     """penalise_field_boundary_3d.py:13-240 (X, Y then Z pass)."""

@@ -4,6 +4,7 @@ from .adjoint import BodyForceObjective2D, time_integrated_body_force
 from .batch import BatchedFlowSimulator2D
 from .flow import (
     FlowSimulator,
+    PassiveTransportFlowSimulator,
     UnboundedNavierStokesFlowSimulator2D,
     UnboundedNavierStokesFlowSimulator3D,
     create_unbounded_flow_simulator_2d,
@@ -34,6 +35,7 @@ __all__ = [
     "FlowSimulator",
     "ImmersedBodyFlowInteraction",
     "ImmersedBodyForcingGrid",
+    "PassiveTransportFlowSimulator",
     "RigidBodyFlowInteraction",
     "TwoDimensionalCylinderForcingGrid",
     "UnboundedNavierStokesFlowSimulator2D",

@@ -352,3 +352,86 @@ def create_unbounded_flow_simulator_3d(grid_size, x_range, kinematic_viscosity, 
         grid_size=grid_size, x_range=x_range, kinematic_viscosity=kinematic_viscosity, cfl=cfl, real_t=real_t,
         num_threads=num_threads, time=time, with_forcing=with_forcing, filter_vorticity=filter_vorticity,
         poisson_solver_type=poisson_solver_type, **kwargs)
+
+
+def compute_advection_diffusion_stable_timestep(velocity_field, velocity_magnitude_field, grid_dim, dx, cfl,
+                                                kinematic_viscosity, real_t=np.float32):
+    """passive_transport_flow_simulators.py:139-155 (synchronises).
+
+    The max of sum_d |u_d| is reduced by the library's kernel; as in the reference,
+    ``velocity_magnitude_field`` receives sum_d |u_d|."""
+    real_t = normalize_real_t(real_t)
+    torch.sum(torch.abs(velocity_field), dim=0, out=velocity_magnitude_field)
+    slot = torch.zeros(1, dtype=torch.float64, device=velocity_field.device)
+    _lib.call("sg_max_abs_sum", sg_dtype(real_t), grid_dim, int(velocity_field[0].numel()), ptr(velocity_field),
+              ptr(slot), stream_ptr(velocity_field.device))
+    umax = real_t(slot.item())
+    tol = 10 * np.finfo(real_t).eps
+    return min(cfl * dx / (umax + tol), 0.9 * dx**2 / (2 * grid_dim) / kinematic_viscosity + tol)
+
+
+class PassiveTransportFlowSimulator(FlowSimulator):
+    """passive_transport_flow_simulators.py:14-136: advection (ENO3) and diffusion of a passive
+    scalar (2D, 3D) or vector (3D) ``primary_field`` in a given ``velocity_field``.
+
+    One ``time_step`` is one ``sg_passive_transport_step`` call: in 2D one fused sweep, in 3D an
+    advection kernel and a diffusion kernel per component, in place through
+    ``buffer_scalar_field``."""
+
+    def __init__(self, kinematic_viscosity, grid_dim, grid_size, x_range, cfl=0.1, real_t=np.float32,
+                 num_threads=1, time=0.0, field_type: Literal["scalar", "vector"] = "scalar", **kwargs):
+        if field_type not in ["scalar", "vector"]:
+            raise ValueError("Invalid field type. Supported values include 'scalar' and 'vector'")
+        if grid_dim == 2 and field_type == "vector":
+            raise ValueError("Passive transport of vector 2D fields not supported yet.")
+        self.kinematic_viscosity = kinematic_viscosity
+        self.cfl = cfl
+        self.field_type = field_type
+        super().__init__(grid_dim=grid_dim, grid_size=grid_size, x_range=x_range, real_t=real_t,
+                         num_threads=num_threads, time=time, device=kwargs.get("device"))
+
+    def _init_fields(self):
+        if self.field_type == "scalar":
+            self.primary_field = self._zeros(*self.grid_size)
+        else:
+            self.primary_field = self._zeros(self.grid_dim, *self.grid_size)
+        self.velocity_field = self._zeros(self.grid_dim, *self.grid_size)
+        # the reference's shared advection / diffusion flux buffer; here the step's scratch field
+        self.buffer_scalar_field = self._zeros(*self.grid_size)
+        self._max_slot = torch.zeros(1, dtype=torch.float64, device=self.device)
+
+    def _compile_kernels(self):
+        pass
+
+    def _advection_and_diffusion_time_step(self, dt, **kwargs):
+        """passive_transport_flow_simulators.py:104-118."""
+        del kwargs
+        for name in ("primary_field", "velocity_field", "buffer_scalar_field"):
+            t = getattr(self, name)
+            if t.dtype != self._tdtype or not t.is_contiguous() or t.device != self.device:
+                raise ValueError(f"{name} must stay a contiguous {self._tdtype} tensor on {self.device}")
+        dt_by_dx = self.real_t(dt / self.dx)
+        nu_dt_by_dx2 = self.real_t(self.kinematic_viscosity * dt / self.dx / self.dx)
+        if self.grid_dim == 2:
+            nz, (ny, nx) = 1, self.grid_size
+        else:
+            nz, ny, nx = self.grid_size
+        ncomp = 1 if self.field_type == "scalar" else self.grid_dim
+        _lib.call("sg_passive_transport_step", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, ncomp,
+                  ptr(self.primary_field), ptr(self.buffer_scalar_field), ptr(self.velocity_field),
+                  float(dt_by_dx), float(nu_dt_by_dx2), stream_ptr(self.device))
+
+    def _finalise_flow_time_step(self):
+        self._flow_time_step = self._advection_and_diffusion_time_step
+
+    def compute_stable_timestep(self, dt_prefac: float = 1.0):
+        """passive_transport_flow_simulators.py:125-136 (synchronises; the magnitude field is not kept)."""
+        n = int(np.prod(self.grid_size))
+        _lib.call("sg_max_abs_sum", sg_dtype(self.real_t), self.grid_dim, n, ptr(self.velocity_field),
+                  ptr(self._max_slot), stream_ptr(self.device))
+        umax = self.real_t(self._max_slot.item())
+        rt = self.real_t
+        tol = 10 * np.finfo(rt).eps
+        dt = min(self.cfl * self.dx / (umax + tol),
+                 0.9 * self.dx**2 / (2 * self.grid_dim) / self.kinematic_viscosity + tol)
+        return dt * dt_prefac

@@ -3,7 +3,7 @@
 Run in a container that has the reference checkout (read-only) at
 ``/root/reference``::
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference [group ...]]
 
 The reference is imported through the test-only stand-ins in ``ref_shims.py``
 (pystencils kernels evaluated with numpy, pyfftw replaced by scipy.fft, numba's
@@ -427,6 +427,51 @@ def rod_3d(sps, real_t, rec: _Recorder, seed: int) -> None:
         rec.put(f"{name}/lag_forcing_after", inter.lag_grid_forcing_field)
 
 
+def passive(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """3D ENO3 advection (advection_flux_3d.py, advection_timestep_3d.py) and steps of the passive
+    transport simulator (passive_transport_flow_simulators.py:14-155)."""
+    import sopht.numeric.eulerian_grid_ops as spne
+    rng = np.random.default_rng(seed)
+    for tag, shape in (("cube", (10, 10, 10)), ("rect", (8, 10, 12))):
+        field = rng.standard_normal(shape).astype(real_t)
+        vel = rng.standard_normal((3, *shape)).astype(real_t)
+        vec = rng.standard_normal((3, *shape)).astype(real_t)
+        flux_in = rng.standard_normal(shape).astype(real_t)  # the flux kernel accumulates into its buffer
+        rec.put(f"{tag}/field", field)
+        rec.put(f"{tag}/velocity", vel)
+        rec.put(f"{tag}/vector_field", vec)
+        rec.put(f"{tag}/flux_in", flux_in)
+        out = flux_in.copy()
+        spne.gen_advection_flux_conservative_eno3_pyst_kernel_3d(real_t=real_t)(
+            advection_flux=out, field=field, velocity=vel, inv_dx=real_t(0.7))
+        rec.put(f"{tag}/flux_out", out)
+        out = field.copy()
+        spne.gen_advection_timestep_euler_forward_conservative_eno3_pyst_kernel_3d(real_t=real_t)(
+            out, advection_flux=rng.standard_normal(shape).astype(real_t), velocity=vel, dt_by_dx=real_t(0.3))
+        rec.put(f"{tag}/advection_step", out)
+        out = vec.copy()
+        spne.gen_advection_timestep_euler_forward_conservative_eno3_pyst_kernel_3d(
+            real_t=real_t, field_type="vector")(
+            out, advection_flux=np.zeros(shape, real_t), velocity=vel, dt_by_dx=real_t(0.3))
+        rec.put(f"{tag}/advection_step_vector", out)
+    for tag, dim, grid, ftype in (("s2d", 2, (12, 16), "scalar"), ("s3d", 3, (8, 10, 12), "scalar"),
+                                  ("v3d", 3, (8, 8, 10), "vector")):
+        sim = sps.PassiveTransportFlowSimulator(kinematic_viscosity=1e-2, grid_dim=dim, grid_size=grid,
+                                                x_range=1.0, cfl=0.2, real_t=real_t, time=0.5, field_type=ftype)
+        sim.velocity_field[...] = rng.standard_normal(sim.velocity_field.shape).astype(real_t)
+        sim.primary_field[...] = rng.random(sim.primary_field.shape).astype(real_t)
+        rec.put(f"sim_{tag}/velocity", sim.velocity_field)
+        rec.put(f"sim_{tag}/primary_in", sim.primary_field)
+        dts = []
+        for step in range(3):
+            dt = sim.compute_stable_timestep(dt_prefac=0.8)
+            sim.time_step(dt=dt)
+            dts.append(dt)
+            rec.put(f"sim_{tag}/primary_step{step}", sim.primary_field)
+        rec.put(f"sim_{tag}/dt", np.array(dts))
+        rec.put(f"sim_{tag}/time_out", sim.time)
+
+
 GROUPS = {
     "stencils2d": ("spne", stencils_2d, 11),
     "poisson2d": ("spne", poisson_2d, 12),
@@ -437,22 +482,25 @@ GROUPS = {
     "ib": ("spib", ib_ops, 31),
     "cylinder2d": ("sps", cylinder_2d, 32),
     "rod3d": ("sps", rod_3d, 33),
+    "passive": ("sps", passive, 41),
 }
 
 
-def _load_test_restatements(ref_root: str, rel: str) -> dict:
+def _load_test_restatements(ref_root: str, rel: str, ns: dict | None = None) -> dict:
     """Load the numpy restatement functions from one reference test file.
 
     Only top-level ``def``s that are not ``test_*`` are executed, with numpy,
     scipy.fft and the reference's precision helpers in scope; the pytest
-    fixtures and sopht imports of the file are skipped.
+    fixtures and sopht imports of the file are skipped.  Passing the namespace
+    of an earlier file lets this file's restatements call that file's.
     """
     import ast
 
     from scipy.fft import irfftn, rfftn
 
     src = (Path(ref_root) / "tests" / rel).read_text()
-    ns = {"np": np, "rfftn": rfftn, "irfftn": irfftn}
+    if ns is None:
+        ns = {"np": np, "rfftn": rfftn, "irfftn": irfftn}
     for node in ast.parse(src).body:
         if isinstance(node, ast.FunctionDef) and not node.name.startswith("test_"):
             exec(compile(ast.Module([node], []), rel, "exec"), ns)
@@ -525,6 +573,18 @@ def validate_shims(ref_root: str, spne) -> None:
         spne.gen_diffusion_timestep_euler_forward_pyst_kernel_3d(real_t=real_t, field_type="vector")(
             vector_field=out, diffusion_flux=np.zeros_like(w3[0]), nu_dt_by_dx2=real_t(0.1))
         close(out, np.stack([ns["diffusion_timestep_euler_forward_reference"](c, real_t(0.1), real_t) for c in w3]))
+        ns = _load_test_restatements(ref_root, t3 + "test_advection_flux_3d.py")
+        out = np.zeros_like(w3[0])
+        spne.gen_advection_flux_conservative_eno3_pyst_kernel_3d(real_t=real_t)(
+            advection_flux=out, field=w3[0], velocity=g3, inv_dx=real_t(0.1))
+        close(out, ns["advection_flux_conservative_eno3_reference"](w3[0], g3[0], g3[1], g3[2], real_t(0.1),
+                                                                    real_t))
+        ns = _load_test_restatements(ref_root, t3 + "test_advection_timestep_3d.py", ns)
+        out = w3[1].copy()
+        spne.gen_advection_timestep_euler_forward_conservative_eno3_pyst_kernel_3d(real_t=real_t)(
+            out, advection_flux=np.zeros_like(out), velocity=g3, dt_by_dx=real_t(0.02))
+        close(out, ns["advection_timestep_conservative_eno3_euler_forward_reference"](
+            w3[1], g3[0], g3[1], g3[2], real_t(0.2), real_t(0.1), real_t))
         ns = _load_test_restatements(ref_root, t3 + "test_divergence_3d.py")
         out = np.zeros_like(w3[0])
         spne.gen_divergence_pyst_kernel_3d(real_t=real_t)(divergence=out, field=w3, inv_dx=real_t(2.0))
@@ -579,11 +639,14 @@ def validate_shims(ref_root: str, spne) -> None:
     print(f"shim validation: {checked} reference-test restatements agree")
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str = "/root/reference", *groups: str) -> None:
+    """Validate the stand-ins, then write every group's fixtures (or only the named ``groups``)."""
     spne, spib, sps = _import_reference(ref_root)
     validate_shims(ref_root, spne)
     mods = {"spne": spne, "spib": spib, "sps": sps}
     for group, (modname, fn, seed) in GROUPS.items():
+        if groups and group not in groups:
+            continue
         for prec, real_t in PRECISIONS.items():
             rec = _Recorder()
             fn(mods[modname], real_t, rec, seed)

@@ -247,3 +247,50 @@ def test_rod_forcing_grids(precision, name):
     inter.compute_flow_forces_and_torques()
     np.testing.assert_allclose(inter.body_flow_forces, g[f"{name}/body_forces"], rtol=tol, atol=tol)
     np.testing.assert_allclose(inter.body_flow_torques, g[f"{name}/body_torques"], rtol=tol, atol=tol)
+
+
+# ------------------------------------------------------------- passive transport
+
+
+@pytest.mark.parametrize("tag", ["cube", "rect"])
+def test_eno3_advection_3d(precision, tag):
+    """advection_flux_3d.py (accumulating into its buffer) and advection_timestep_3d.py, scalar and vector."""
+    g = load_golden("passive", precision)
+    rt = real_t_of(precision)
+    tol = ref_tol(precision)
+    f, v, vec = g[f"{tag}/field"], g[f"{tag}/velocity"], g[f"{tag}/vector_field"]
+    flux = g[f"{tag}/flux_in"] + st.eno3_flux_3d(f, v, rt(0.7))
+    np.testing.assert_allclose(flux, g[f"{tag}/flux_out"], atol=tol)
+    out = f.copy()
+    st.advection_step_3d(out, v, rt(0.3))
+    np.testing.assert_allclose(out, g[f"{tag}/advection_step"], atol=tol)
+    out = vec.copy()
+    for c in range(3):
+        st.advection_step_3d(out[c], v, rt(0.3))
+    np.testing.assert_allclose(out, g[f"{tag}/advection_step_vector"], atol=tol)
+
+
+@pytest.mark.parametrize("tag,dim,grid,ftype", [("s2d", 2, (12, 16), "scalar"), ("s3d", 3, (8, 10, 12), "scalar"),
+                                                ("v3d", 3, (8, 8, 10), "vector")])
+def test_passive_transport_steps(precision, tag, dim, grid, ftype):
+    """Three steps of PassiveTransportFlowSimulator (stable dt with dt_prefac 0.8, advection, diffusion)."""
+    from oracle.flow import PassiveTransportOracle
+    g = load_golden("passive", precision)
+    rt = real_t_of(precision)
+    sim = PassiveTransportOracle(1e-2, dim, grid, 1.0, cfl=0.2, real_t=rt, time=0.5, field_type=ftype)
+    sim.velocity_field[...] = g[f"sim_{tag}/velocity"]
+    sim.primary_field[...] = g[f"sim_{tag}/primary_in"]
+    for step in range(3):
+        dt = sim.compute_stable_timestep(dt_prefac=0.8)
+        assert dt == g[f"sim_{tag}/dt"][step]
+        sim.time_step(dt)
+        np.testing.assert_allclose(sim.primary_field, g[f"sim_{tag}/primary_step{step}"], atol=ref_tol(precision))
+    assert sim.time == g[f"sim_{tag}/time_out"]
+
+
+def test_passive_transport_rejects_2d_vector():
+    from oracle.flow import PassiveTransportOracle
+    with pytest.raises(ValueError):
+        PassiveTransportOracle(1e-2, 2, (8, 8), 1.0, field_type="vector")
+    with pytest.raises(ValueError):
+        PassiveTransportOracle(1e-2, 3, (8, 8, 8), 1.0, field_type="tensor")
