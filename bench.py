@@ -796,6 +796,240 @@ def run_adjoint(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def point_source(position, centre, nu, mag, t, real_t):
+    """Diffused point source (heat-kernel Gaussian) of the passive-transport example
+    (examples/3d_examples/PointSourceAdvectAndDiffuseCase/point_source_helpers.py)."""
+    r2 = sum((position[d] - centre[d]) ** 2 for d in range(3))
+    return (mag / (4 * real_t(np.pi) * nu * t) ** 1.5 * np.exp(-r2 / (4 * nu * t))).astype(real_t)
+
+
+def _passive_case(grid, real_t, device, nu=1e-3, t0=5.0, centre=(0.3, 0.3, 0.3)):
+    import torch
+
+    from sopht_gb300.simulator import PassiveTransportFlowSimulator
+    sim = PassiveTransportFlowSimulator(kinematic_viscosity=nu, grid_dim=3, grid_size=grid, x_range=1.0,
+                                        real_t=real_t, time=t0, field_type="vector", device=device)
+    mag = 4.0 * np.pi * nu * t0**1.5
+    f0 = point_source(sim.position_field, centre, nu, mag, t0, real_t)
+    for c in range(3):
+        sim.primary_field[c].copy_(torch.from_numpy(f0).to(device))
+    sim.velocity_field.fill_(1.0)
+    return sim, f0, mag
+
+
+def run_passive(args, rank, world):
+    """Passive transport of a vector point source (point_source_advection_diffusion.py): timed at 256^3,
+    where the working set (field, velocity, scratch: 470 MB) exceeds the L2; the example's own 128^3 run
+    from t = 5.0 to 5.4 gives the accuracy figures."""
+    import torch
+
+    from sopht_gb300 import _lib
+    from sopht_gb300.build import build
+    from sopht_gb300.utils import ptr, sg_dtype, stream_ptr
+
+    build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    grid = (256, 256, 256)
+    cells = int(np.prod(grid))
+    sim, _, _ = _passive_case(grid, np.float32, device)
+    dt = sim.compute_stable_timestep()  # the velocity field is uniform and constant: dt is the same every step
+    stream = torch.cuda.Stream(device)
+    seg = min(args.steps, 25)
+    n_seg = max(1, args.steps // seg)
+    steps = seg * n_seg
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        stream.wait_stream(torch.cuda.current_stream())
+        for _ in range(args.warmup):
+            sim.time_step(dt=dt)
+        with torch.cuda.graph(graph, stream=stream):
+            for _ in range(seg):
+                sim.time_step(dt=dt)
+    with torch.cuda.stream(stream):
+        graph.replay()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(n_seg):
+            graph.replay()
+        stop.record(stream)
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t_wall) * 1e3
+    clock_info = clocks.stop()
+    elapsed_ms = start.elapsed_time(stop)
+    if elapsed_ms < 0.5 * wall_ms:
+        raise RuntimeError(f"event time {elapsed_ms:.3f} ms disagrees with wall time {wall_ms:.3f} ms")
+    graph.reset()
+    del graph
+    # the two kernels of one component, timed alone on the launching stream
+    n = cells
+    dt_by_dx = float(np.float32(dt / sim.dx))
+    k = float(np.float32(sim.kinematic_viscosity * dt / sim.dx / sim.dx))
+    reps = 20
+    kern_ms = {}
+    tmp = torch.empty_like(sim.primary_field)
+    with torch.cuda.stream(stream):
+        s = stream_ptr(device)
+        for name in ("eno3_3d", "diffusion3d_3comp"):
+            for r in range(reps + 3):
+                if r == 3:
+                    start.record(stream)
+                if name == "eno3_3d":
+                    _lib.call("sg_advection_eno3_step_3d", sg_dtype(np.float32), *grid, 3, ptr(sim.primary_field),
+                              ptr(tmp), ptr(sim.velocity_field), dt_by_dx, s)
+                else:
+                    _lib.call("sg_diffusion_step_3d", sg_dtype(np.float32), *grid, ptr(sim.primary_field),
+                              ptr(tmp), k, s)
+            stop.record(stream)
+            torch.cuda.synchronize()
+            kern_ms[name] = start.elapsed_time(stop) / reps
+    del tmp
+    # end to end through the public API: host stable dt (one D2H read of the max) and the step call
+    sim_e, _, _ = _passive_case(grid, np.float32, device)
+    for _ in range(args.warmup):
+        sim_e.time_step(dt=sim_e.compute_stable_timestep())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim_e.time_step(dt=sim_e.compute_stable_timestep())
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    del sim_e
+    # accuracy: the example's 128^3 run to t = 5.4 in FP32 and FP64 on the GPU, errors against the translated
+    # point source as the example prints them; FP64 GPU steps against the FP64 oracle from the same state
+    acc = {}
+    small = (128, 128, 128)
+    finals = {}
+    for real_t in (() if args.skip_accuracy else (np.float32, np.float64)):
+        s_sim, _, mag = _passive_case(small, real_t, device)
+        n_steps = 0
+        while s_sim.time < 5.4:
+            s_sim.time_step(dt=s_sim.compute_stable_timestep())
+            n_steps += 1
+        t_end = float(s_sim.time)
+        shift = 1.0 * (t_end - 5.0)
+        exact = point_source(s_sim.position_field, (0.3 + shift,) * 3, 1e-3, mag, 5.0, real_t)
+        w = s_sim.primary_field.cpu().numpy()
+        err = np.fabs(w - exact[None])
+        finals[real_t] = w.astype(np.float64)
+        acc["fp32" if real_t == np.float32 else "fp64"] = {
+            "steps": n_steps, "t_end": t_end, "l2_error": float(np.linalg.norm(err) * float(s_sim.dx) ** 1.5),
+            "linf_error": float(err.max())}
+    if finals:
+        acc["fp32_vs_fp64_rel_l2"] = float(np.linalg.norm(finals[np.float32] - finals[np.float64])
+                                           / np.linalg.norm(finals[np.float64]))
+    cpu = None
+    if not args.skip_cpu:
+        from oracle.flow import PassiveTransportOracle
+        g_sim, f0, _ = _passive_case(small, np.float64, device)
+        ora = PassiveTransportOracle(1e-3, 3, small, 1.0, real_t=np.float64, time=5.0, field_type="vector")
+        ora.primary_field[...] = f0[None]
+        ora.velocity_field[...] = 1.0
+        for _ in range(3):
+            d = ora.compute_stable_timestep()
+            assert g_sim.compute_stable_timestep() == d
+            ora.time_step(d)
+            g_sim.time_step(dt=d)
+        gw = g_sim.primary_field.cpu().numpy()
+        acc["fp64_gpu_vs_fp64_oracle_rel_l2_3_steps_128cube"] = float(np.linalg.norm(gw - ora.primary_field)
+                                                                     / np.linalg.norm(ora.primary_field))
+        # CPU baseline: the oracle (fp32) on the same 256^3 workload, a bounded sample
+        c_ora = PassiveTransportOracle(1e-3, 3, grid, 1.0, real_t=np.float32, time=5.0, field_type="vector")
+        c_ora.velocity_field[...] = 1.0
+        c_ora.primary_field[...] = point_source(c_ora.position_field, (0.3,) * 3, 1e-3,
+                                                4.0 * np.pi * 1e-3 * 5.0**1.5, 5.0, np.float32)[None]
+        c_ora.time_step(c_ora.compute_stable_timestep())
+        nc, tc = 0, time.perf_counter()
+        while True:
+            c_ora.time_step(c_ora.compute_stable_timestep())
+            nc += 1
+            el = time.perf_counter() - tc
+            if el >= args.cpu_seconds:
+                break
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+        cpu = {"value": round(nc / el, 4), "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": f"{nc} steps of the same 256^3 vector workload after 1 warm-up step ({el:.1f} s), "
+                         "numpy, fp32"}
+    if rank != 0:
+        return
+    peaks = load_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    eno3_bytes = 36 * cells  # three components: field 12 + velocity 12 read, 12 written per cell
+    out = {
+        "metric": "passive-transport steps/s (vector point source, ENO3 advection + diffusion)",
+        "value": round(world * steps / (elapsed_ms * 1e-3), 2), "unit": "steps/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": round(elapsed_ms / steps, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "gcell_updates_per_s": round(world * cells * steps / (elapsed_ms * 1e-3) / 1e9, 3),
+        "config": {"workload": "3D 256^3 fp32 passive transport of a vector point source (nu 1e-3, uniform "
+                               "velocity 1 on every axis, x_range 1), the example's 128^3 case for accuracy",
+                   "grid": list(grid), "field_type": "vector", "dt_rule": "compute_stable_timestep, CFL 0.1",
+                   "l2": "no flush: the working set (470 MB) exceeds the 126 MB L2"},
+        "step_bytes_per_cell": {"design": 60, "compulsory": 36,
+                                "note": "ENO3 reads the 3 components and the velocity and writes a 3-component "
+                                        "scratch (36 B), diffusion reads it and writes the field (24 B)"},
+        "step_roofline": {"achieved_GB_s": round(60 * cells * steps / (elapsed_ms * 1e-3) / 1e9, 1),
+                          "frac": round(60 * cells * steps / (elapsed_ms * 1e-3) / 1e9 / peak, 3)},
+        "roofline": {"bound": "hbm", "kernel": "eno3_3d", "achieved": round(eno3_bytes / (kern_ms["eno3_3d"] * 1e-3)
+                                                                             / 1e9, 1),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(eno3_bytes / (kern_ms["eno3_3d"] * 1e-3) / 1e9 / peak, 3),
+                     "traffic": traffic_from_profiles("pointsource256", "eno3_3d"),
+                     "algorithmic_bytes_per_launch": eno3_bytes,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
+        "kernels_ms": {k: round(v, 5) for k, v in kern_ms.items()},
+        "kernels_note": "eno3_3d: the 3-component launch of the step (36 B/cell); diffusion3d_3comp: the "
+                        "3-component diffusion of the step (24 B/cell)",
+        "e2e": {"value": round(world * steps / e2e_s, 2), "unit": "steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 8,
+                "note": "public API per step: compute_stable_timestep (max reduction, 8-byte read) and time_step"},
+        "gpu_launches": steps * 2,
+        "cpu_baseline": cpu,
+        "accuracy": acc,
+        "clocks": clock_info,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_passive_reference(args, rank, world):
+    """The reference's passive-transport algorithm on the host cores (the numpy oracle), same 256^3 workload."""
+    if rank != 0:
+        return
+    from oracle.flow import PassiveTransportOracle
+    grid = (256, 256, 256)
+    ora = PassiveTransportOracle(1e-3, 3, grid, 1.0, real_t=np.float32, time=5.0, field_type="vector")
+    ora.velocity_field[...] = 1.0
+    ora.primary_field[...] = point_source(ora.position_field, (0.3,) * 3, 1e-3, 4.0 * np.pi * 1e-3 * 5.0**1.5, 5.0,
+                                          np.float32)[None]
+    ora.time_step(ora.compute_stable_timestep())
+    budget = max(10.0, min(180.0, float(args.cpu_seconds) * 4))
+    n, t0 = 0, time.perf_counter()
+    while True:
+        ora.time_step(ora.compute_stable_timestep())
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget or n >= args.steps:
+            break
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    v = round(n / el, 4)
+    out = {"impl": "reference", "metric": "passive-transport steps/s (vector point source, ENO3 advection + "
+                                          "diffusion)",
+           "value": v, "unit": "steps/s", "n_gpus": world, "steps": n, "warmup": 1, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "ms_per_step": round(1e3 / v, 2),
+           "config": {"workload": "3D 256^3 fp32 passive transport of a vector point source", "grid": list(grid)},
+           "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
+                            "sample": f"{n} steps after 1 warm-up step ({el:.1f} s), numpy, fp32"},
+           "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
 def accuracy_checkpoints(wl, device, checkpoints, cpu_oracle=False):
     """Relative L2 of the fp32 GPU path against the same path in FP64 on the GPU (and, in 2D, the FP64
     CPU oracle) at the checkpoint steps.  All runs take the FP64 GPU run's dt sequence, so the errors
@@ -941,7 +1175,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="rod128",
-                    choices=["rod128", "cylinder2d", "carpet256", "batch64", "adjoint2d"])
+                    choices=["rod128", "cylinder2d", "carpet256", "batch64", "adjoint2d", "pointsource256"])
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-cpu-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -955,6 +1189,12 @@ def main():
         return
     if args.workload == "adjoint2d":
         run_adjoint(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
+        return
+    if args.workload == "pointsource256":
+        if args.impl == "reference":
+            run_passive_reference(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
+        else:
+            run_passive(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
         return
     wl = make_workload(args.workload)
     world = int(os.environ.get("WORLD_SIZE", "1"))

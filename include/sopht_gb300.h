@@ -251,7 +251,8 @@ int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* field, int f
  * (stencil_ops_3d/advection_timestep_3d.py:38-96 with advection_flux_3d.py:
  * 12-233): out = in + flux on [2:-2]^3 (out = in elsewhere), inv_dx = -dt_by_dx,
  * for `ncomp` components spaced nz*ny*nx apart (all advected by the same
- * (3, nz, ny, nx) velocity).  in and out must not alias. */
+ * (3, nz, ny, nx) velocity; with ncomp = 3 one thread advects all three,
+ * loading the velocity once).  in and out must not alias. */
 int sg_advection_eno3_step_3d(int dtype, int nz, int ny, int nx, int ncomp, const void* in,
                               void* out, const void* velocity, double dt_by_dx, void* stream);
 /* Replaces gen_advection_flux_conservative_eno3_pyst_kernel_3d
@@ -262,9 +263,10 @@ int sg_advection_eno3_flux_3d(int dtype, int nz, int ny, int nx, const void* fie
 /* Replaces PassiveTransportFlowSimulator._advection_and_diffusion_time_step
  * (simulator/flow/passive_transport_flow_simulators.py:104-118): each of the
  * `ncomp` components of `field` (1 in 2D; 1 or 3 in 3D) is advected by ENO3
- * with dt_by_dx and then diffused with nu_dt_by_dx2, in place.  `scratch` is
- * one scalar field of the grid (the simulator's buffer_scalar_field); in 2D
- * the two operators run as one fused sweep. */
+ * with dt_by_dx and then diffused with nu_dt_by_dx2, in place.  `scratch`
+ * holds ncomp fields of the grid (a scalar field: the simulator's
+ * buffer_scalar_field).  2D: one fused sweep; 3D: one advection launch and
+ * one diffusion launch for all components. */
 int sg_passive_transport_step(int dtype, int dim, int nz, int ny, int nx, int ncomp, void* field,
                               void* scratch, const void* velocity, double dt_by_dx,
                               double nu_dt_by_dx2, void* stream);

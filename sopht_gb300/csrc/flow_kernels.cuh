@@ -585,14 +585,17 @@ __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) 
     }
 }
 
-// 3D conservative ENO3 advection of scalar components (advection_flux_3d.py:12-233,
-// advection_timestep_3d.py:38-96).  On [2:-2]^3 the six face fluxes are accumulated in the
-// reference's pass order (x front, x back, y front, y back, z front, z back) onto a start value:
+// 3D conservative ENO3 advection (advection_flux_3d.py:12-233, advection_timestep_3d.py:38-96).
+// On [2:-2]^3 the six face fluxes are accumulated in the reference's pass order (x front, x back,
+// y front, y back, z front, z back) onto a start value:
 //   flux mode (add_field = 0): start = base, out = the accumulated flux (the flux kernel adds into
 //     its buffer; base may equal out);
 //   step mode (add_field = 1): start = 0, out = field + flux (the zeroed buffer, then the sum).
-// Outside the interior out = base (flux mode) or field (step mode).  Component c of field / base /
-// out is blockIdx.z / nz; the velocity (3 components) is shared.
+// Outside the interior out = base (flux mode) or field (step mode).  The velocity (3 components) is
+// shared by every advected component.  NC = 3: one thread advects all three components of a vector
+// field (the velocity and the upwind choices are loaded once); NC = 1: one component per thread, the
+// component being blockIdx.z / nz.  Neighbours are addressed from per-thread base pointers with
+// 32-bit strides (nz, ny, nx < 2^31 / (nx ny) is checked by the launcher).
 template <typename T> struct Eno3D3Params {
     Grid3 grid;
     const T* field;
@@ -603,33 +606,44 @@ template <typename T> struct Eno3D3Params {
     int add_field;
 };
 
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) eno3_3d_kernel(Eno3D3Params<T> p) {
     const Grid3 G = p.grid;
     const int64_t n = G.n();
-    const int comp = blockIdx.z / G.nz;
+    const int comp0 = NC == 1 ? (int)(blockIdx.z / G.nz) : 0;
     const int x = blockIdx.x * kCell3X + threadIdx.x, y = blockIdx.y * kCell3Y + threadIdx.y;
-    const int z = blockIdx.z - comp * G.nz;
+    const int z = blockIdx.z - comp0 * G.nz;
     if (x >= G.nx || y >= G.ny) return;
     const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
-    const T* f = p.field + comp * n;
-    T acc = p.add_field ? T(0) : p.base[comp * n + g];
+    const T* f[NC];
+    T acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        f[c] = p.field + (int64_t)(comp0 + c) * n + g;
+        acc[c] = p.add_field ? T(0) : p.base[(int64_t)(comp0 + c) * n + g];
+    }
     const bool in = z >= 2 && z <= G.nz - 3 && y >= 2 && y <= G.ny - 3 && x >= 2 && x <= G.nx - 3;
     if (in) {
-        const int64_t strides[3] = {1, (int64_t)G.nx, (int64_t)G.nx * G.ny};
+        const int strides[3] = {1, G.nx, G.nx * G.ny};
 #pragma unroll
         for (int axis = 0; axis < 3; ++axis) {
-            const int64_t s = strides[axis];
-            const T* ua = p.u + axis * n;
-            auto q = [&](int k) { return f[g + k * s] * ua[g + k * s]; };
-            const T um1 = ua[g - s], u0 = ua[g], up1 = ua[g + s];
-            const T front = eno3_face(q(-1), q(0), q(1), q(2), u0, up1);
-            const T back = eno3_face(q(-2), q(-1), q(0), q(1), um1, u0);
-            acc = acc + p.inv_dx * front;
-            acc = acc - p.inv_dx * back;
+            const int s = strides[axis];
+            const T* ua = p.u + axis * n + g;
+            const T um2 = ua[-2 * s], um1 = ua[-s], u0 = ua[0], up1 = ua[s], up2 = ua[2 * s];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const T* fc = f[c];
+                const T qm2 = fc[-2 * s] * um2, qm1 = fc[-s] * um1, q0 = fc[0] * u0;
+                const T qp1 = fc[s] * up1, qp2 = fc[2 * s] * up2;
+                const T front = eno3_face(qm1, q0, qp1, qp2, u0, up1);
+                const T back = eno3_face(qm2, qm1, q0, qp1, um1, u0);
+                acc[c] = acc[c] + p.inv_dx * front;
+                acc[c] = acc[c] - p.inv_dx * back;
+            }
         }
     }
-    p.out[comp * n + g] = p.add_field ? f[g] + acc : acc;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) p.out[(int64_t)(comp0 + c) * n + g] = p.add_field ? f[c][0] + acc[c] : acc[c];
 }
 
 // One 1D Laplacian filter pass g = 0.25 (2 f - f[+s] - f[-s]) on [1:-1]^3,

@@ -265,9 +265,11 @@ extern "C" int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* f
 // ------------------------------------------------------------ passive transport
 namespace sg {
 
+// ncomp components; vector_threads: one thread per cell advects all three (ncomp must be 3)
 template <typename T>
 static int eno3_3d_launch(int nz, int ny, int nx, int ncomp, const void* field, const void* base, void* out,
-                          const void* u, double inv_dx, int add_field, cudaStream_t s) {
+                          const void* u, double inv_dx, int add_field, bool vector_threads, cudaStream_t s) {
+    SG_REQUIRE((int64_t)nx * ny <= (int64_t)1 << 29, SG_ERR_SHAPE, "eno3 3d: plane of %d x %d too large", ny, nx);
     Eno3D3Params<T> p{};
     p.grid = Grid3{nz, ny, nx};
     p.field = (const T*)field;
@@ -277,26 +279,32 @@ static int eno3_3d_launch(int nz, int ny, int nx, int ncomp, const void* field, 
     p.inv_dx = (T)inv_dx;
     p.add_field = add_field;
     dim3 grid = cell3_grid(p.grid);
-    grid.z = (unsigned)nz * (unsigned)ncomp;
-    eno3_3d_kernel<T><<<grid, cell3_block(), 0, s>>>(p);
+    if (vector_threads) {
+        SG_REQUIRE(ncomp == 3, SG_ERR_INVALID_ARG, "eno3 3d: vector threads need 3 components");
+        eno3_3d_kernel<T, 3><<<grid, cell3_block(), 0, s>>>(p);
+    } else {
+        grid.z = (unsigned)nz * (unsigned)ncomp;
+        eno3_3d_kernel<T, 1><<<grid, cell3_block(), 0, s>>>(p);
+    }
     return launch_status("eno3_3d");
 }
 
 template <typename T>
-static int diffusion3d_scalar_launch(int nz, int ny, int nx, const void* in, void* out, double k, cudaStream_t s) {
+static int diffusion3d_comps_launch(int nz, int ny, int nx, int ncomp, const void* in, void* out, double k,
+                                    cudaStream_t s) {
     Stencil3DParams<T> p{};
     p.grid = Grid3{nz, ny, nx};
     p.a = (const T*)in;
     p.out = (T*)out;
     p.prefactor = (T)k;
     p.mode = 1;
-    p.ncomp = 1;
+    p.ncomp = ncomp;
     diffusion3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
-    return launch_status("diffusion3d scalar");
+    return launch_status("diffusion3d");
 }
 
 // PassiveTransportFlowSimulator._advection_and_diffusion_time_step: advection then diffusion of
-// each component, in place on `field`, through one scalar scratch field.
+// every component, in place on `field`, through a scratch field of the same components.
 template <typename T>
 static int passive_step(int dim, int nz, int ny, int nx, int ncomp, void* field, void* scratch, const void* u,
                         double dt_by_dx, double k, cudaStream_t s) {
@@ -306,13 +314,8 @@ static int passive_step(int dim, int nz, int ny, int nx, int ncomp, void* field,
         return cuda_status(cudaMemcpyAsync(field, scratch, (size_t)ny * nx * sizeof(T), cudaMemcpyDeviceToDevice, s),
                            "passive step copy back");
     }
-    const int64_t n = (int64_t)nz * ny * nx;
-    for (int c = 0; c < ncomp; ++c) {
-        T* fc = (T*)field + c * n;
-        SG_TRY(eno3_3d_launch<T>(nz, ny, nx, 1, fc, nullptr, scratch, u, -dt_by_dx, 1, s));
-        SG_TRY(diffusion3d_scalar_launch<T>(nz, ny, nx, scratch, fc, k, s));
-    }
-    return SG_OK;
+    SG_TRY(eno3_3d_launch<T>(nz, ny, nx, ncomp, field, nullptr, scratch, u, -dt_by_dx, 1, ncomp == 3, s));
+    return diffusion3d_comps_launch<T>(nz, ny, nx, ncomp, scratch, field, k, s);
 }
 
 }  // namespace sg
@@ -323,8 +326,10 @@ extern "C" int sg_advection_eno3_step_3d(int dtype, int nz, int ny, int nx, int 
     SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
     SG_REQUIRE(ncomp >= 1 && (int64_t)nz * ncomp <= 65535, SG_ERR_SHAPE, "eno3 3d: bad component count %d", ncomp);
     auto s = (cudaStream_t)stream;
-    SG_DTYPE_DISPATCH(dtype, eno3_3d_launch<float>(nz, ny, nx, ncomp, in, nullptr, out, velocity, -dt_by_dx, 1, s),
-                      eno3_3d_launch<double>(nz, ny, nx, ncomp, in, nullptr, out, velocity, -dt_by_dx, 1, s));
+    SG_DTYPE_DISPATCH(dtype,
+                      eno3_3d_launch<float>(nz, ny, nx, ncomp, in, nullptr, out, velocity, -dt_by_dx, 1, ncomp == 3, s),
+                      eno3_3d_launch<double>(nz, ny, nx, ncomp, in, nullptr, out, velocity, -dt_by_dx, 1, ncomp == 3,
+                                             s));
 }
 
 extern "C" int sg_advection_eno3_flux_3d(int dtype, int nz, int ny, int nx, const void* field, void* flux,
@@ -333,8 +338,8 @@ extern "C" int sg_advection_eno3_flux_3d(int dtype, int nz, int ny, int nx, cons
     SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
     SG_REQUIRE(nz <= 65535, SG_ERR_SHAPE, "eno3 3d: nz too large");
     auto s = (cudaStream_t)stream;
-    SG_DTYPE_DISPATCH(dtype, eno3_3d_launch<float>(nz, ny, nx, 1, field, flux, flux, velocity, inv_dx, 0, s),
-                      eno3_3d_launch<double>(nz, ny, nx, 1, field, flux, flux, velocity, inv_dx, 0, s));
+    SG_DTYPE_DISPATCH(dtype, eno3_3d_launch<float>(nz, ny, nx, 1, field, flux, flux, velocity, inv_dx, 0, false, s),
+                      eno3_3d_launch<double>(nz, ny, nx, 1, field, flux, flux, velocity, inv_dx, 0, false, s));
 }
 
 extern "C" int sg_passive_transport_step(int dtype, int dim, int nz, int ny, int nx, int ncomp, void* field,

@@ -374,9 +374,10 @@ class PassiveTransportFlowSimulator(FlowSimulator):
     """passive_transport_flow_simulators.py:14-136: advection (ENO3) and diffusion of a passive
     scalar (2D, 3D) or vector (3D) ``primary_field`` in a given ``velocity_field``.
 
-    One ``time_step`` is one ``sg_passive_transport_step`` call: in 2D one fused sweep, in 3D an
-    advection kernel and a diffusion kernel per component, in place through
-    ``buffer_scalar_field``."""
+    One ``time_step`` is one ``sg_passive_transport_step`` call, in place: in 2D one fused sweep
+    through ``buffer_scalar_field``; in 3D one advection kernel (a vector field's three components
+    per thread) into a scratch field and one diffusion kernel back (the scratch of a vector field is
+    a private three-component buffer)."""
 
     def __init__(self, kinematic_viscosity, grid_dim, grid_size, x_range, cfl=0.1, real_t=np.float32,
                  num_threads=1, time=0.0, field_type: Literal["scalar", "vector"] = "scalar", **kwargs):
@@ -398,6 +399,7 @@ class PassiveTransportFlowSimulator(FlowSimulator):
         self.velocity_field = self._zeros(self.grid_dim, *self.grid_size)
         # the reference's shared advection / diffusion flux buffer; here the step's scratch field
         self.buffer_scalar_field = self._zeros(*self.grid_size)
+        self._vector_scratch = self._zeros(self.grid_dim, *self.grid_size) if self.field_type == "vector" else None
         self._max_slot = torch.zeros(1, dtype=torch.float64, device=self.device)
 
     def _compile_kernels(self):
@@ -417,8 +419,9 @@ class PassiveTransportFlowSimulator(FlowSimulator):
         else:
             nz, ny, nx = self.grid_size
         ncomp = 1 if self.field_type == "scalar" else self.grid_dim
+        scratch = self.buffer_scalar_field if ncomp == 1 else self._vector_scratch
         _lib.call("sg_passive_transport_step", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, ncomp,
-                  ptr(self.primary_field), ptr(self.buffer_scalar_field), ptr(self.velocity_field),
+                  ptr(self.primary_field), ptr(scratch), ptr(self.velocity_field),
                   float(dt_by_dx), float(nu_dt_by_dx2), stream_ptr(self.device))
 
     def _finalise_flow_time_step(self):

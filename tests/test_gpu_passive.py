@@ -161,3 +161,21 @@ def test_passive_simulator_argument_errors():
     sim.primary_field = sim.primary_field.double()
     with pytest.raises(ValueError):
         sim.time_step(dt=1e-3)
+
+
+@pytest.mark.parametrize("rt", [np.float32, np.float64])
+def test_vector_threads_equal_per_component_launches(rt):
+    """ncomp = 3 (one thread advects all three components) against three single-component launches."""
+    from sopht_gb300 import _lib
+    from sopht_gb300.utils import ptr, sg_dtype, stream_ptr
+    rng = np.random.default_rng(8)
+    grid = (20, 36, 44)
+    f = dev(rng.standard_normal((3, *grid)).astype(rt))
+    u = dev(rng.standard_normal((3, *grid)).astype(rt))
+    out3 = torch.empty_like(f)
+    out1 = torch.empty_like(f)
+    s = stream_ptr(f.device)
+    _lib.call("sg_advection_eno3_step_3d", sg_dtype(rt), *grid, 3, ptr(f), ptr(out3), ptr(u), 0.05, s)
+    for c in range(3):
+        _lib.call("sg_advection_eno3_step_3d", sg_dtype(rt), *grid, 1, ptr(f[c]), ptr(out1[c]), ptr(u), 0.05, s)
+    np.testing.assert_array_equal(host(out3), host(out1))
