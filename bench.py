@@ -345,9 +345,7 @@ def run_gpu(args, wl: Workload, rank, world):
     if elapsed_ms < 0.5 * wall_ms:
         raise RuntimeError(f"event time {elapsed_ms:.3f} ms disagrees with wall time {wall_ms:.3f} ms")
     if world > 1:
-        t = torch.tensor([elapsed_ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+        elapsed_ms = max_over_ranks(elapsed_ms, device)
         torch.distributed.barrier()
     with torch.cuda.stream(stream):
         graph_inst.replay()
@@ -378,9 +376,7 @@ def run_gpu(args, wl: Workload, rank, world):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:
-        t = torch.tensor([e2e_s], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, device)
     n_lag = sum(inter.num_lag_nodes for inter in inters_e)
     h2d = 2 * wl.dim * n_lag * 8
     d2h = wl.dim * n_lag * 4 + 8
@@ -1073,6 +1069,17 @@ def accuracy_checkpoints(wl, device, checkpoints, cpu_oracle=False):
             out["checkpoints"].append(row)
     del runs
     return out
+
+
+def max_over_ranks(value, device=None):
+    """The largest of every rank's ``value`` (a replica's time: the job ends with the slowest); the
+    value itself when no process group is running."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 def load_peaks():

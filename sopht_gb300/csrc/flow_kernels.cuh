@@ -44,12 +44,14 @@ template <typename T> struct Sweep2DParams {
     T* tape_w2;   // optional: w2 (after advection)
 };
 
+// advection_flux_2d.py:35-47: left-biased when u_0 > -u_{+1}.  The two fused multiply-adds are
+// written out, so every kernel that uses the face (and every launch shape of one kernel) rounds it
+// the same way whatever the compiler's contraction choices around the call.
 template <typename T>
 __device__ __forceinline__ T eno3_face(T qm1, T q0, T qp1, T qp2, T u0, T up1) {
     const T third = T(1.0 / 3.0), five6 = T(5.0 / 6.0), sixth = T(1.0 / 6.0);
-    // advection_flux_2d.py:35-47: left-biased when u_0 > -u_{+1}
-    if (u0 > -up1) return third * qp1 + five6 * q0 - sixth * qm1;
-    return third * q0 + five6 * qp1 - sixth * qp2;
+    if (u0 > -up1) return fma(-sixth, qm1, fma(five6, q0, third * qp1));
+    return fma(-sixth, qp2, fma(five6, qp1, third * q0));
 }
 
 template <typename T, int TX, int TY>
@@ -595,7 +597,7 @@ __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) 
 // shared by every advected component.  NC = 3: one thread advects all three components of a vector
 // field (the velocity and the upwind choices are loaded once); NC = 1: one component per thread, the
 // component being blockIdx.z / nz.  Neighbours are addressed from per-thread base pointers with
-// 32-bit strides (nz, ny, nx < 2^31 / (nx ny) is checked by the launcher).
+// 32-bit strides (the launcher checks that two planes fit).
 template <typename T> struct Eno3D3Params {
     Grid3 grid;
     const T* field;
@@ -637,8 +639,8 @@ __global__ void __launch_bounds__(256) eno3_3d_kernel(Eno3D3Params<T> p) {
                 const T qp1 = fc[s] * up1, qp2 = fc[2 * s] * up2;
                 const T front = eno3_face(qm1, q0, qp1, qp2, u0, up1);
                 const T back = eno3_face(qm2, qm1, q0, qp1, um1, u0);
-                acc[c] = acc[c] + p.inv_dx * front;
-                acc[c] = acc[c] - p.inv_dx * back;
+                acc[c] = fma(p.inv_dx, front, acc[c]);
+                acc[c] = fma(-p.inv_dx, back, acc[c]);
             }
         }
     }

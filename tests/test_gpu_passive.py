@@ -179,3 +179,32 @@ def test_vector_threads_equal_per_component_launches(rt):
     for c in range(3):
         _lib.call("sg_advection_eno3_step_3d", sg_dtype(rt), *grid, 1, ptr(f[c]), ptr(out1[c]), ptr(u), 0.05, s)
     np.testing.assert_array_equal(host(out3), host(out1))
+
+
+@pytest.mark.parametrize("grid", [(83, 256, 256), (163, 256, 256)])
+def test_large_grids_vs_oracle(grid):
+    """Large grids with odd plane counts: the vector step and the scalar flux form in FP64 against the
+    oracle, and the planes outside the interior copied unchanged."""
+    from oracle import stencils as st
+    from sopht_gb300 import _lib
+    from sopht_gb300.utils import ptr, sg_dtype, stream_ptr
+    rt = np.float64
+    rng = np.random.default_rng(grid[0])
+    f = rng.standard_normal((3, *grid)).astype(rt)
+    u = rng.standard_normal((3, *grid)).astype(rt)
+    fd, ud = dev(f), dev(u)
+    out = torch.empty_like(fd)
+    s = stream_ptr(fd.device)
+    _lib.call("sg_advection_eno3_step_3d", sg_dtype(rt), *grid, 3, ptr(fd), ptr(out), ptr(ud), 0.05, s)
+    got = host(out)
+    for c in range(3):
+        ref = f[c].copy()
+        st.advection_step_3d(ref, u, rt(0.05))
+        assert rel_l2(got[c], ref) < 1e-13
+        np.testing.assert_array_equal(got[c][:2], f[c][:2])  # planes outside the interior are copied
+        np.testing.assert_array_equal(got[c][-2:], f[c][-2:])
+    base = rng.standard_normal(grid).astype(rt)
+    flux = dev(base)
+    _lib.call("sg_advection_eno3_flux_3d", sg_dtype(rt), *grid, ptr(fd[1]), ptr(flux), ptr(ud), 0.7, s)
+    ref = base + st.eno3_flux_3d(f[1], u, rt(0.7))
+    assert rel_l2(host(flux), ref) < 1e-13
