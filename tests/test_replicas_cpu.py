@@ -40,7 +40,7 @@ def _max_worker(rank, world, port, out):
 
 def test_max_over_ranks_gloo():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_max_worker, args=(2, port, out), nprocs=2, join=True)
         assert dict(out) == {0: 2.5, 1: 2.5}
