@@ -171,7 +171,13 @@ def make_workload(name: str) -> Workload:
 
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms around a timed region.
+
+    ``start`` returns once the first sample has been written, so the region that follows is
+    sampled from its beginning; ``stop`` keeps the samples whose timestamps fall between the
+    two calls (all of them if none do or the timestamps cannot be read)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -179,16 +185,51 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"sg_clocks_{os.getpid()}.csv"
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while time.time() < deadline and self.proc.poll() is None:
+            if self.path.exists() and self.path.stat().st_size > 0:
+                break
+            time.sleep(0.01)
+        self.t0 = time.time()
+
+    @staticmethod
+    def parse(lines, t0=None, t1=None):
+        """Median SM clock, max clock and throttle reasons of the sample lines (CSV of FIELDS)."""
+        import datetime
+        rows = []
+        for line in lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                sm, smax = float(parts[2]), float(parts[3])
+            except ValueError:
+                continue
+            try:
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                ts = None
+            rows.append((ts, sm, smax, parts[6:10]))
+        inside = [r for r in rows if t0 is not None and r[0] is not None and t0 <= r[0] <= t1]
+        use = inside if inside else rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in use for n, flag in zip(names, r[3], strict=False) if flag.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[1] for r in use])) if use else None,
+                "sm_max_mhz": max(r[2] for r in use) if use else None,
+                "samples": len(use), "samples_in_timed_region": len(inside), "reasons": reasons}
 
     def stop(self):
+        self.t1 = time.time()
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -196,23 +237,9 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.path.read_text().splitlines():
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for name, flag in zip(names, parts[5:9], strict=False):
-                if flag.lower() == "active":
-                    reasons.add(name)
+        out = self.parse(self.path.read_text().splitlines(), self.t0, self.t1)
         self.path.unlink(missing_ok=True)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+        return out
 
 
 # ---------------------------------------------------------------- GPU arm
