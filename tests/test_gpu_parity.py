@@ -445,3 +445,32 @@ def test_rod_coupling_vs_reference(precision, name):
     inter.compute_flow_forces_and_torques()
     np.testing.assert_allclose(inter.body_flow_forces, g[f"{name}/body_forces"], rtol=tol, atol=tol)
     np.testing.assert_allclose(inter.body_flow_torques, g[f"{name}/body_torques"], rtol=tol, atol=tol)
+
+
+@pytest.mark.parametrize("dim,grid,steps", [(3, (128, 128, 128), 2), (2, (512, 1024), 5)])
+def test_full_size_steps_vs_oracle(precision, dim, grid, steps):
+    """Forced steps at the benchmark sizes: the 128^3 rod-flow grid (256^3 doubled FFT, radix-16
+    line passes) and the largest batched 2D grid (1024-point rows) against the oracle."""
+    import sopht_gb300.simulator as sps
+    from oracle.flow import NavierStokes2DOracle, NavierStokes3DOracle
+    rt = real_t_of(precision)
+    rng = np.random.default_rng(29)
+    kw = dict(grid_size=grid, x_range=1.0, kinematic_viscosity=3e-3, real_t=rt, with_forcing=True,
+              with_free_stream_flow=True)
+    w0 = (1e-2 * rng.standard_normal((grid if dim == 2 else (3, *grid)))).astype(rt)
+    fs = np.array([1.0, 0.0, 0.0][:dim])
+    f0 = (0.1 * rng.standard_normal((dim, *grid))).astype(rt)
+    Sim = sps.UnboundedNavierStokesFlowSimulator2D if dim == 2 else sps.UnboundedNavierStokesFlowSimulator3D
+    Ora = NavierStokes2DOracle if dim == 2 else NavierStokes3DOracle
+    sim, ora = Sim(**kw), Ora(**kw)
+    sim.vorticity_field.copy_(dev(w0))
+    ora.vorticity_field[...] = w0
+    for _ in range(steps):
+        sim.eul_grid_forcing_field.copy_(dev(f0))
+        ora.eul_grid_forcing_field[...] = f0
+        dt = ora.compute_stable_timestep()  # both driven by the same dt sequence
+        sim.time_step(dt=dt, free_stream_velocity=fs)
+        ora.time_step(dt, fs)
+    bound = 1e-5 if rt == np.float32 else 1e-12
+    assert rel_l2(host(sim.vorticity_field), ora.vorticity_field) < bound
+    assert rel_l2(host(sim.velocity_field), ora.velocity_field) < bound
