@@ -54,7 +54,7 @@ def test_max_over_ranks_without_group():
 
 @pytest.mark.timeout(300)
 def test_reference_arm_under_torchrun_prints_one_line():
-    """``--impl reference`` launched as the driver launches N > 1: rank 0 times the CPU path and prints
+    """``--impl reference`` launched by torchrun with two ranks: rank 0 times the CPU path and prints
     the only JSON line; the other rank exits 0 without work."""
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
