@@ -239,3 +239,46 @@ def test_bound_interactor_call_is_bitwise_the_generic_path(rt):
     a()
     assert a._binding is not old
     np.testing.assert_array_equal(a.lag_grid_forcing_host(), host(a.lag_grid_forcing_field))
+
+
+def test_bound_call_reports_markers_outside_the_grid():
+    """The one-call interactor path shares the status word: a body moved off the grid is reported,
+    and after the report a body back inside runs clean."""
+    sim, inter = _cylinder_case(np.float32)
+    inter()
+    inter.check_markers_in_domain()  # inside: no error
+    assert inter._binding is not None
+    inter.forcing_grid.cylinder.position_collection[1, 0] = 0.02  # the support now crosses y = 0
+    inter()
+    with pytest.raises(ValueError, match="outside"):
+        inter.check_markers_in_domain()
+    inter.forcing_grid.cylinder.position_collection[1, 0] = 0.125
+    inter()
+    inter.check_markers_in_domain()
+
+
+def test_graph_cache_gives_up_on_moving_fields_and_stays_exact():
+    """Fields replaced before every step: after a few captures the plan stops capturing and launches
+    directly, and every step still equals the direct-launch step bitwise."""
+    import sopht_gb300.simulator as sps
+    grid = (40, 72)
+    kw = dict(grid_size=grid, x_range=1.0, kinematic_viscosity=1e-3, real_t=np.float32, with_forcing=True,
+              with_free_stream_flow=True)
+    a, b = sps.UnboundedNavierStokesFlowSimulator2D(**kw), sps.UnboundedNavierStokesFlowSimulator2D(**kw)
+    rng = np.random.default_rng(4)
+    w0 = torch.from_numpy(rng.standard_normal(grid).astype(np.float32)).cuda()
+    a.vorticity_field.copy_(w0)
+    b.vorticity_field.copy_(w0)
+    keep = []
+    for step in range(12):
+        for s in (a, b):  # a new stream-function tensor every step (kept alive: new addresses)
+            s.stream_func_field = torch.zeros_like(s.stream_func_field)
+            keep.append(s.stream_func_field)
+        dt = a.compute_stable_timestep()
+        a.time_step(dt=dt, free_stream_velocity=np.array([1.0, 0.0]))
+        events = _arm_direct(b)
+        b.time_step(dt=dt, free_stream_velocity=np.array([1.0, 0.0]))
+        torch.cuda.synchronize()
+        del events
+        np.testing.assert_array_equal(host(a.vorticity_field), host(b.vorticity_field))
+        np.testing.assert_array_equal(host(a.velocity_field), host(b.velocity_field))
