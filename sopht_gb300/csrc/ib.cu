@@ -31,7 +31,7 @@ static int ib_interaction_impl(int dtype, int dim, int nz, int ny, int nx, doubl
                                const void* eul_velocity, int32_t* nearest, void* weights, void* flow_velocity,
                                void* velocity_mismatch, void* position_mismatch, void* forcing, double stiffness,
                                double damping, int do_xi_step, double xi_dt, const sg_step_scalars* dev_scalars,
-                               int32_t* status_dev, cudaStream_t stream) {
+                               int32_t* status_dev, cudaStream_t stream, const IBDynArgs* dyn = nullptr) {
     SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "ib interaction: dim must be 2 or 3");
     SG_REQUIRE(n_lag >= 1, SG_ERR_INVALID_ARG, "ib interaction: n_lag must be >= 1");
     SG_REQUIRE(kernel_type == 0 || kernel_type == 1, SG_ERR_INVALID_ARG, "ib interaction: bad kernel type");
@@ -44,14 +44,14 @@ static int ib_interaction_impl(int dtype, int dim, int nz, int ny, int nx, doubl
         IBParams<float> p{dim, nz, ny, nx, n_lag, kernel_type, dx, shift, position, body_velocity,
                           (const float*)eul_velocity, nearest, (float*)weights, (float*)flow_velocity,
                           (float*)velocity_mismatch, (float*)position_mismatch, (float*)forcing,
-                          stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev};
+                          stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev, dyn};
         ib_interaction_launch<float>(p, stream);
     } else {
         SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "ib interaction: bad dtype");
         IBParams<double> p{dim, nz, ny, nx, n_lag, kernel_type, dx, shift, position, body_velocity,
                            (const double*)eul_velocity, nearest, (double*)weights, (double*)flow_velocity,
                            (double*)velocity_mismatch, (double*)position_mismatch, (double*)forcing,
-                           stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev};
+                           stiffness, damping, do_xi_step, xi_dt, dev_scalars, status_dev, dyn};
         ib_interaction_launch<double>(p, stream);
     }
     return launch_status("ib_interaction");
@@ -147,10 +147,26 @@ struct sg_ib_binding_s {
     cudaEvent_t kin_done[2] = {nullptr, nullptr};
     void* forcing_host = nullptr;       // pinned (dim, n_lag) of the field type
     cudaEvent_t forcing_done = nullptr;
+    // graphs of the per-call work, one per (staging slot, spread mode, forcing copy, Eulerian fields),
+    // captured on first use; the per-call scalars come from `dyn`
+    IBDynArgs* dyn = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        int slot = 0, spread_mode = 0, copy = 0;
+        const void* u = nullptr;
+        void* f = nullptr;
+    } graphs[8];
+    int n_graphs = 0, builds = 0;
+    bool graphs_off = false;
 };
 
 static void ib_binding_free(sg_ib_binding_s* b) {
     if (!b) return;
+    for (int k = 0; k < b->n_graphs; ++k)
+        if (b->graphs[k].exec) cudaGraphExecDestroy(b->graphs[k].exec);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    cudaFree(b->dyn);
     for (int k = 0; k < 2; ++k) {
         if (b->kin_done[k]) cudaEventDestroy(b->kin_done[k]);
         cudaFreeHost(b->kin_host[k]);
@@ -203,6 +219,7 @@ extern "C" int sg_ib_bind(int dtype, int dim, int nz, int ny, int nx, double dx,
     if (st == SG_OK) st = cuda_status(cudaMallocHost(&b->forcing_host, f_bytes), "ib bind: pinned forcing");
     if (st == SG_OK)
         st = cuda_status(cudaEventCreateWithFlags(&b->forcing_done, cudaEventDisableTiming), "ib bind: event");
+    if (st == SG_OK) st = cuda_status(cudaMalloc((void**)&b->dyn, sizeof(IBDynArgs)), "ib bind: argument block");
     if (st != SG_OK) {
         ib_binding_free(b);
         return st;
@@ -224,6 +241,83 @@ extern "C" int sg_ib_binding_wait(sg_ib_binding b, int which) {
     return cuda_status(cudaEventSynchronize(which < 2 ? b->kin_done[which] : b->forcing_done), "ib wait");
 }
 
+// The per-call work of a bound interactor on `stream`.  dyn: the interaction reads K, C and the xi
+// step from the binding's device block (a graph being recorded); capturing: the event records
+// become nodes of the graph being captured.
+static int ib_bound_work(sg_ib_binding_s* b, int kin_slot, const void* eul_velocity, void* eul_forcing,
+                         int spread_mode, double stiffness, double damping, int do_xi_step, double xi_dt,
+                         int copy_forcing, bool dyn, bool capturing, cudaStream_t stream) {
+    const int64_t nk = (int64_t)b->dim * b->n_lag;
+    const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (kin_slot >= 0) {
+        SG_TRY(cuda_status(cudaMemcpyAsync(b->dev_kin, b->kin_host[kin_slot], (size_t)2 * nk * sizeof(double),
+                                           cudaMemcpyHostToDevice, stream),
+                           "ib bound step: kinematics upload"));
+        SG_TRY(cuda_status(cudaEventRecordWithFlags(b->kin_done[kin_slot], stream, rec), "ib bound step: event"));
+    }
+    SG_TRY(ib_interaction_impl(b->dtype, b->dim, b->nz, b->ny, b->nx, b->dx, b->shift, b->n_lag, b->kernel,
+                               b->dev_kin, b->dev_kin + nk, eul_velocity, b->nearest, b->weights, b->flow_velocity,
+                               b->vel_mismatch, b->pos_mismatch, b->lag_forcing, stiffness, damping, do_xi_step,
+                               xi_dt, nullptr, b->status, stream, dyn ? b->dyn : nullptr));
+    if (spread_mode >= 0)
+        SG_TRY(ib_spread_impl(b->dtype, b->dim, b->nz, b->ny, b->nx, b->n_lag, b->nearest, b->weights,
+                              b->lag_forcing, eul_forcing, spread_mode, stream));
+    if (copy_forcing) {
+        const size_t f_bytes = (size_t)nk * (b->dtype == SG_F32 ? sizeof(float) : sizeof(double));
+        SG_TRY(cuda_status(cudaMemcpyAsync(b->forcing_host, b->lag_forcing, f_bytes, cudaMemcpyDeviceToHost, stream),
+                           "ib bound step: forcing copy"));
+        SG_TRY(cuda_status(cudaEventRecordWithFlags(b->forcing_done, stream, rec), "ib bound step: event"));
+    }
+    return SG_OK;
+}
+
+__global__ void set_ib_dyn_kernel(IBDynArgs v, IBDynArgs* dst) { *dst = v; }
+
+static void ib_graphs_off(sg_ib_binding_s* b) {
+    cudaGetLastError();  // a failed capture leaves no sticky error: direct launches follow
+    b->graphs_off = true;
+}
+
+// The captured graph of one call variant, captured now if it is new; null when graphs are off.
+static cudaGraphExec_t ib_bound_graph(sg_ib_binding_s* b, int kin_slot, const void* u, void* f, int spread_mode,
+                                      int copy_forcing) {
+    if (b->graphs_off) return nullptr;
+    for (int k = 0; k < b->n_graphs; ++k) {
+        const auto& e = b->graphs[k];
+        if (e.slot == kin_slot && e.spread_mode == spread_mode && e.copy == copy_forcing && e.u == u && e.f == f)
+            return e.exec;
+    }
+    if (b->builds >= 16) {  // fields that keep moving: direct launches from now on
+        ib_graphs_off(b);
+        return nullptr;
+    }
+    ++b->builds;
+    if (!b->capture_stream && cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        b->capture_stream = nullptr;
+        ib_graphs_off(b);
+        return nullptr;
+    }
+    if (cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        ib_graphs_off(b);
+        return nullptr;
+    }
+    const int st = ib_bound_work(b, kin_slot, u, f, spread_mode, 0.0, 0.0, 0, 0.0, copy_forcing, true, true,
+                                 b->capture_stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->capture_stream, &g);
+    cudaGraphExec_t exec = nullptr;
+    if (st != SG_OK || e != cudaSuccess || !g || cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        ib_graphs_off(b);
+        return nullptr;
+    }
+    cudaGraphDestroy(g);
+    const int k = b->n_graphs < 8 ? b->n_graphs++ : b->builds % 8;
+    if (b->graphs[k].exec) cudaGraphExecDestroy(b->graphs[k].exec);
+    b->graphs[k] = sg_ib_binding_s::Graph{exec, kin_slot, spread_mode, copy_forcing, u, f};
+    return exec;
+}
+
 extern "C" int sg_ib_bound_step(sg_ib_binding b, int kin_slot, const void* eul_velocity, void* eul_forcing,
                                 int spread_mode, double stiffness, double damping, int do_xi_step, double xi_dt,
                                 int copy_forcing, void* stream_) {
@@ -232,27 +326,23 @@ extern "C" int sg_ib_bound_step(sg_ib_binding b, int kin_slot, const void* eul_v
     SG_REQUIRE(spread_mode >= -1 && spread_mode <= 1, SG_ERR_INVALID_ARG, "ib bound step: bad spread mode");
     SG_REQUIRE(spread_mode < 0 || eul_forcing, SG_ERR_INVALID_ARG, "ib bound step: no Eulerian forcing");
     auto stream = (cudaStream_t)stream_;
-    const int64_t nk = (int64_t)b->dim * b->n_lag;
-    if (kin_slot >= 0) {
-        SG_TRY(cuda_status(cudaMemcpyAsync(b->dev_kin, b->kin_host[kin_slot], (size_t)2 * nk * sizeof(double),
-                                           cudaMemcpyHostToDevice, stream),
-                           "ib bound step: kinematics upload"));
-        SG_TRY(cuda_status(cudaEventRecord(b->kin_done[kin_slot], stream), "ib bound step: event"));
+    copy_forcing = copy_forcing ? 1 : 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        cs = cudaStreamCaptureStatusActive;  // unknown: take the direct path, events as graph nodes
     }
-    SG_TRY(ib_interaction_impl(b->dtype, b->dim, b->nz, b->ny, b->nx, b->dx, b->shift, b->n_lag, b->kernel,
-                               b->dev_kin, b->dev_kin + nk, eul_velocity, b->nearest, b->weights, b->flow_velocity,
-                               b->vel_mismatch, b->pos_mismatch, b->lag_forcing, stiffness, damping, do_xi_step,
-                               xi_dt, nullptr, b->status, stream));
-    if (spread_mode >= 0)
-        SG_TRY(ib_spread_impl(b->dtype, b->dim, b->nz, b->ny, b->nx, b->n_lag, b->nearest, b->weights,
-                              b->lag_forcing, eul_forcing, spread_mode, stream));
-    if (copy_forcing) {
-        const size_t f_bytes = (size_t)nk * (b->dtype == SG_F32 ? sizeof(float) : sizeof(double));
-        SG_TRY(cuda_status(cudaMemcpyAsync(b->forcing_host, b->lag_forcing, f_bytes, cudaMemcpyDeviceToHost, stream),
-                           "ib bound step: forcing copy"));
-        SG_TRY(cuda_status(cudaEventRecord(b->forcing_done, stream), "ib bound step: event"));
+    if (cs == cudaStreamCaptureStatusNone) {
+        // one replay of the captured call: 2 launches instead of 4 to 6
+        const cudaGraphExec_t g = ib_bound_graph(b, kin_slot, eul_velocity, eul_forcing, spread_mode, copy_forcing);
+        if (g) {
+            set_ib_dyn_kernel<<<1, 1, 0, stream>>>(IBDynArgs{stiffness, damping, do_xi_step, xi_dt}, b->dyn);
+            SG_TRY(launch_status("ib bound step arguments"));
+            return cuda_status(cudaGraphLaunch(g, stream), "ib bound step graph launch");
+        }
     }
-    return SG_OK;
+    return ib_bound_work(b, kin_slot, eul_velocity, eul_forcing, spread_mode, stiffness, damping, do_xi_step, xi_dt,
+                         copy_forcing, false, cs != cudaStreamCaptureStatusNone, stream);
 }
 
 extern "C" int sg_ib_unbind(sg_ib_binding b) {

@@ -39,6 +39,14 @@ template <typename T> __device__ __forceinline__ T peskin_phi(T a) {
     return v;
 }
 
+// Per-call scalars of a bound interactor read from device memory, so that one captured graph
+// serves every call (written by a one-thread kernel before each replay).
+struct IBDynArgs {
+    double K, C;
+    int xi_step;
+    double xi_dt;
+};
+
 template <typename T> struct IBParams {
     int dim, nz, ny, nx, n_lag, kernel;
     double dx, shift;
@@ -56,6 +64,7 @@ template <typename T> struct IBParams {
     double xi_dt;
     const sg_step_scalars* dev;
     int32_t* status;
+    const IBDynArgs* dyn;  // when not null, K, C, xi_step and xi_dt come from here
 };
 
 // Marker i is handled by one whole warp.  Lane 4 d + k (d < DIM, k < 4)
@@ -91,8 +100,9 @@ __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i)
     }
     if ((lane & 3) == 0 && (lane >> 2) < DIM) p.nearest[(lane >> 2) * n + i] = my_near;
     // optional VirtualBoundaryForcing.time_step: xi += dt * dU (previous dU)
-    if (p.xi_step && lane < DIM) {
-        const T dt = (T)(p.dev ? p.dev->dt : p.xi_dt);
+    const int xi_step = p.dyn ? p.dyn->xi_step : p.xi_step;
+    if (xi_step && lane < DIM) {
+        const T dt = (T)(p.dev ? p.dev->dt : (p.dyn ? p.dyn->xi_dt : p.xi_dt));
         p.pos_mismatch[lane * n + i] = p.pos_mismatch[lane * n + i] + dt * p.vel_mismatch[lane * n + i];
     }
     if (!inside) {
@@ -146,7 +156,8 @@ __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i)
         p.flow_vel[d * n + i] = U;
         const T dU = (T)((double)U - p.body_vel[d * n + i]);
         p.vel_mismatch[d * n + i] = dU;
-        p.forcing[d * n + i] = (T)(p.K * (double)p.pos_mismatch[d * n + i] + p.C * (double)dU);
+        const double K = p.dyn ? p.dyn->K : p.K, C = p.dyn ? p.dyn->C : p.C;
+        p.forcing[d * n + i] = (T)(K * (double)p.pos_mismatch[d * n + i] + C * (double)dU);
     }
 }
 
