@@ -327,7 +327,11 @@ int sg_ib_binding_wait(sg_ib_binding binding, int which);
  * kinematics buffer; then sg_ib_interaction on it (xi step as there, host dt
  * only); then, when spread_mode >= 0, sg_ib_spread with reset = spread_mode;
  * then, when copy_forcing != 0, copy the Lagrangian forcing to the pinned
- * forcing buffer (completion: sg_ib_binding_wait(binding, 2)). */
+ * forcing buffer (completion: sg_ib_binding_wait(binding, 2)).  Outside stream
+ * capture the work is a graph captured on first use of each (kin_slot,
+ * spread_mode, copy_forcing, eul_velocity, eul_forcing) and replayed, with the
+ * per-call scalars written to a binding-owned device block just before; the
+ * results are those of direct launches. */
 int sg_ib_bound_step(sg_ib_binding binding, int kin_slot, const void* eul_velocity,
                      void* eul_forcing, int spread_mode, double stiffness, double damping,
                      int do_xi_step, double xi_dt, int copy_forcing, void* stream);
