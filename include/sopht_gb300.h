@@ -336,6 +336,18 @@ int sg_ib_bound_step(sg_ib_binding binding, int kin_slot, const void* eul_veloci
                      void* eul_forcing, int spread_mode, double stiffness, double damping,
                      int do_xi_step, double xi_dt, int copy_forcing, void* stream);
 int sg_ib_unbind(sg_ib_binding binding);
+/* Host-side (no GPU work) CosseratRodElementCentricForcingGrid kinematics
+ * (simulator/immersed_body/cosserat_rod/cosserat_rod_forcing_grids.py:82-130):
+ * element centres and mass-weighted element velocities of a rod with
+ * n_elems + 1 nodes (node arrays of 3 rows of n_elems + 1 float64, rows
+ * `*_row_stride` elements apart; mass (n_elems + 1) contiguous),
+ * in numpy's operation order without fused multiply-adds, written to the
+ * grid's (grid_dim, n_elems) position and velocity arrays and, when `staging`
+ * is not NULL, to a staging slot of sg_ib_binding_buffers. */
+int sg_rod_element_kinematics(int grid_dim, int n_elems, const double* node_position,
+                              int64_t position_row_stride, const double* node_velocity,
+                              int64_t velocity_row_stride, const double* mass,
+                              double* position_out, double* velocity_out, double* staging);
 
 /* ------------------------------------------------------------- adjoints */
 /* Transposes of the 2D step's operators and of the virtual-boundary

@@ -104,6 +104,8 @@ _SIGNATURES = {
     "sg_ib_bound_step": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_double, c_double, c_int, c_double,
                                  c_int, c_void_p]),
     "sg_ib_unbind": (c_int, [c_void_p]),
+    "sg_rod_element_kinematics": (c_int, [c_int, c_int, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p,
+                                          c_void_p, c_void_p]),
     # adjoints
     "sg_adj_partials_count_2d": (c_int64, [c_int, c_int]),
     "sg_sum_partials": (c_int, [c_int64, c_void_p, c_void_p, c_void_p]),

@@ -349,3 +349,39 @@ extern "C" int sg_ib_unbind(sg_ib_binding b) {
     ib_binding_free(b);
     return SG_OK;
 }
+
+// ------------------------------------------------------------ host-side forcing-grid kinematics
+// CosseratRodElementCentricForcingGrid (cosserat_rod_forcing_grids.py:82-130) on the host:
+// element centres (x_i + x_{i+1}) / 2 and the mass-weighted element velocities of pyelastica's
+// _node_to_element_velocity, (m_{i+1} v_{i+1} + m_i v_i) / (m_{i+1} + m_i), with the operations in
+// numpy's order and without fused multiply-adds, written to the grid's position/velocity arrays and,
+// when given, to a (2, grid_dim, n_elems) staging slot of sg_ib_binding_buffers.  Node-array rows
+// may be strided (views into a larger block of rods).
+extern "C" int sg_rod_element_kinematics(int grid_dim, int n_elems, const double* node_position,
+                                         int64_t position_row_stride, const double* node_velocity,
+                                         int64_t velocity_row_stride, const double* mass, double* position_out,
+                                         double* velocity_out, double* staging) {
+    SG_REQUIRE(grid_dim == 2 || grid_dim == 3, SG_ERR_INVALID_ARG, "rod kinematics: dim must be 2 or 3");
+    SG_REQUIRE(n_elems >= 1, SG_ERR_INVALID_ARG, "rod kinematics: n_elems must be >= 1");
+    SG_REQUIRE(node_position && node_velocity && mass && position_out && velocity_out, SG_ERR_INVALID_ARG,
+               "rod kinematics: null argument");
+    SG_REQUIRE(position_row_stride >= n_elems + 1 && velocity_row_stride >= n_elems + 1, SG_ERR_INVALID_ARG,
+               "rod kinematics: row stride shorter than a row");
+    for (int d = 0; d < grid_dim; ++d) {
+        const double* p = node_position + (int64_t)d * position_row_stride;
+        const double* v = node_velocity + (int64_t)d * velocity_row_stride;
+        for (int e = 0; e < n_elems; ++e) {
+            const double x = (p[e + 1] + p[e]) / 2.0;
+            const double a = mass[e + 1] * v[e + 1];
+            const double b = mass[e] * v[e];
+            const double u = (a + b) / (mass[e + 1] + mass[e]);
+            position_out[(int64_t)d * n_elems + e] = x;
+            velocity_out[(int64_t)d * n_elems + e] = u;
+            if (staging) {
+                staging[(int64_t)d * n_elems + e] = x;
+                staging[(int64_t)(grid_dim + d) * n_elems + e] = u;
+            }
+        }
+    }
+    return SG_OK;
+}

@@ -106,6 +106,7 @@ class _IBBinding:
         _lib.call("sg_ib_binding_buffers", self.handle, ctypes.byref(s0), ctypes.byref(s1), ctypes.byref(fh))
         dbl = ctypes.POINTER(ctypes.c_double)
         self.kin = [np.ctypeslib.as_array(ctypes.cast(a.value, dbl), shape=(2, dim, n)) for a in (s0, s1)]
+        self.kin_ptr = [s0.value, s1.value]
         ftype = ctypes.c_float if vbf.real_t == np.float32 else ctypes.c_double
         self.forcing = np.ctypeslib.as_array(ctypes.cast(fh.value, ctypes.POINTER(ftype)), shape=(dim, n))
         self.slot = 1
@@ -116,13 +117,18 @@ class _IBBinding:
         if st != _lib.SG_OK:
             _lib.call("sg_ib_binding_wait", self.handle, which)  # raises with the library's message
 
-    def stage(self, position, velocity) -> int:
-        """Write the kinematics into the next staging slot (after its previous upload ran)."""
+    def next_slot(self) -> int:
+        """The next staging slot, once its previous upload has run."""
         slot = self.slot ^ 1
         self.slot = slot
         if self.used[slot]:
             self.wait(slot)
         self.used[slot] = True
+        return slot
+
+    def stage(self, position, velocity) -> int:
+        """Write the kinematics into the next staging slot (after its previous upload ran)."""
+        slot = self.next_slot()
         v = self.kin[slot]
         v[0] = position
         v[1] = velocity

@@ -235,6 +235,7 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
         self._snapshot_src = None
         self._snapshot_event = torch.cuda.Event()
         self._binding = None
+        self._rod_args_cache = None
 
     def compute_interaction_on_lag_grid(self) -> None:
         self.forcing_grid.compute_lag_grid_position_field()
@@ -244,9 +245,11 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
 
     def __call__(self) -> None:
         fg = self.forcing_grid
-        fg.compute_lag_grid_position_field()
-        fg.compute_lag_grid_velocity_field()
         b = self._bound(fg)
+        rod = self._rod_kinematics_args(fg) if b is not None else None
+        if rod is None:
+            fg.compute_lag_grid_position_field()
+            fg.compute_lag_grid_velocity_field()
         if b is None:
             self.compute_interaction_forcing(eul_grid_forcing_field=self.eul_grid_forcing_field,
                                              eul_grid_velocity_field=self.eul_grid_velocity_field,
@@ -263,7 +266,11 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
             return
         # one native call: kinematics upload, interaction (with a deferred time_step), spreading, and the
         # early copy of the Lagrangian forcing once a caller reads it
-        slot = b.stage(fg.position_field, fg.velocity_field)
+        if rod is None:
+            slot = b.stage(fg.position_field, fg.velocity_field)
+        else:  # the grid's kinematics computed natively, into its arrays and the staging slot at once
+            slot = b.next_slot()
+            _lib.call("sg_rod_element_kinematics", *rod, b.kin_ptr[slot])
         pending = self._pending_xi_dt
         self._pending_xi_dt = None
         self._n_interactions += 1
@@ -276,6 +283,35 @@ class ImmersedBodyFlowInteraction(VirtualBoundaryForcing):
         if snap:
             self._snapshot_key = (self._n_interactions, self.lag_grid_forcing_field._version)
             self._snapshot_src = b
+
+    def _rod_kinematics_args(self, fg):
+        """Arguments of ``sg_rod_element_kinematics`` for an element-centric rod grid (exactly that
+        class, so overridden kinematics keep running), or None where numpy computes them.  Cached by
+        array identity: pyelastica updates the rod arrays in place."""
+        if type(fg) is not CosseratRodElementCentricForcingGrid:
+            return None
+        rod = fg.cosserat_rod
+        arrays = (rod.position_collection, rod.velocity_collection, rod.mass, fg.position_field, fg.velocity_field)
+        c = self._rod_args_cache
+        if c is not None and all(x is y for x, y in zip(c[0], arrays)):
+            return c[1]
+        self._rod_args_cache = None
+        p, v, m, po, vo = arrays
+        n = fg.num_lag_nodes
+        dim = fg.grid_dim
+        if not all(isinstance(a, np.ndarray) and a.dtype == np.float64 for a in arrays):
+            return None
+        if (p.shape != (3, n + 1) or v.shape != (3, n + 1) or m.shape != (n + 1,) or po.shape != (dim, n)
+                or vo.shape != (dim, n)):
+            return None
+        if not (p.strides[1] == 8 and v.strides[1] == 8 and p.strides[0] % 8 == 0 and v.strides[0] % 8 == 0
+                and p.strides[0] >= 8 * (n + 1) and v.strides[0] >= 8 * (n + 1)
+                and m.flags.c_contiguous and po.flags.c_contiguous and vo.flags.c_contiguous):
+            return None
+        args = (dim, n, p.ctypes.data, p.strides[0] // 8, v.ctypes.data, v.strides[0] // 8, m.ctypes.data,
+                po.ctypes.data, vo.ctypes.data)
+        self._rod_args_cache = (arrays, args)
+        return args
 
     def _bound(self, fg):
         """The native binding of this interactor's buffers, or None where the generic path applies

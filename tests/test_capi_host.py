@@ -151,3 +151,33 @@ def test_ghat_is_real_and_symmetric():
     gh = np.fft.rfftn(g)
     assert np.abs(gh.imag).max() < 1e-12 * np.abs(gh.real).max()
     np.testing.assert_allclose(gh.real[1:6], gh.real[-1:-6:-1], rtol=1e-12, atol=1e-14)
+
+
+def test_rod_element_kinematics_matches_numpy(lib):
+    """The host-side element-centric rod kinematics against the grid's numpy formulas, bitwise, for
+    contiguous node arrays and for rows strided inside a larger block; the staging slot gets both."""
+    from sopht_gb300.simulator.immersed_body import _node_to_element_velocity
+    rng = np.random.default_rng(6)
+    n = 37
+    block = rng.standard_normal((3, 3 * (n + 1)))
+    cases = [(rng.standard_normal((3, n + 1)), rng.standard_normal((3, n + 1))),
+             (block[:, n + 1: 2 * (n + 1)], block[:, 2 * (n + 1):])]
+    mass = rng.random(n + 1) + 0.5
+    for pos, vel in cases:
+        for dim in (2, 3):
+            po = np.empty((dim, n))
+            vo = np.empty((dim, n))
+            stage = np.full((2, dim, n), np.nan)
+            st_ = lib.sg_rod_element_kinematics(dim, n, pos.ctypes.data, pos.strides[0] // 8, vel.ctypes.data,
+                                                vel.strides[0] // 8, mass.ctypes.data, po.ctypes.data,
+                                                vo.ctypes.data, stage.ctypes.data)
+            assert st_ == 0
+            ref_p = (pos[:dim, 1:] + pos[:dim, :-1]) / 2.0
+            ref_v = _node_to_element_velocity(mass, vel)[:dim]
+            np.testing.assert_array_equal(po, ref_p)
+            np.testing.assert_array_equal(vo, ref_v)
+            np.testing.assert_array_equal(stage[0], ref_p)
+            np.testing.assert_array_equal(stage[1], ref_v)
+    bad = lib.sg_rod_element_kinematics(3, n, cases[0][0].ctypes.data, n, cases[0][1].ctypes.data, n + 1,
+                                        mass.ctypes.data, po.ctypes.data, vo.ctypes.data, None)
+    assert bad == 1  # a row stride shorter than a row is rejected

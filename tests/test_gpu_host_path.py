@@ -282,3 +282,56 @@ def test_graph_cache_gives_up_on_moving_fields_and_stays_exact():
         del events
         np.testing.assert_array_equal(host(a.vorticity_field), host(b.vorticity_field))
         np.testing.assert_array_equal(host(a.velocity_field), host(b.velocity_field))
+
+
+class _MovingRod:
+    """A rod with the attributes the forcing grids read (pyelastica layout)."""
+
+    def __init__(self, n, rng):
+        s = np.linspace(0.0, 0.3, n + 1)
+        self.position_collection = np.stack([0.5 + 0.0 * s, 0.5 + 0.05 * np.sin(3 * s), 0.35 + s])
+        self.velocity_collection = 0.1 * rng.standard_normal((3, n + 1))
+        self.mass = 0.5 + rng.random(n + 1)
+        self.director_collection = np.tile(np.eye(3)[:, :, None], (1, 1, n))
+        self.n_elems = n
+        self.lengths = np.linalg.norm(np.diff(self.position_collection, axis=1), axis=0)
+
+
+def test_native_rod_kinematics_path_is_bitwise_the_numpy_path():
+    """An element-centric rod interactor computes its marker kinematics natively; a subclass of the
+    grid (the numpy path) gives bitwise the same grid arrays, forcing and flow over moving steps."""
+    import sopht_gb300.simulator as sps
+
+    class _NumpyGrid(sps.CosseratRodElementCentricForcingGrid):
+        pass
+
+    grid = (32, 32, 32)
+    sims, inters = [], []
+    for cls in (sps.CosseratRodElementCentricForcingGrid, _NumpyGrid):
+        sim = sps.UnboundedNavierStokesFlowSimulator3D(grid_size=grid, x_range=1.0, kinematic_viscosity=3e-3,
+                                                       real_t=np.float32, with_forcing=True,
+                                                       with_free_stream_flow=True)
+        rod = _MovingRod(24, np.random.default_rng(2))
+        inter = sps.CosseratRodFlowInteraction(
+            cosserat_rod=rod, eul_grid_forcing_field=sim.eul_grid_forcing_field,
+            eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=-2e4,
+            virtual_boundary_damping_coeff=-1e2, dx=sim.dx, grid_dim=3, real_t=np.float32, forcing_grid_cls=cls)
+        sims.append(sim)
+        inters.append(inter)
+    fs = np.array([1.0, 0.0, 0.0])
+    for step in range(4):
+        for inter in inters:  # move the rods in place, as pyelastica does
+            rod = inter.forcing_grid.cosserat_rod
+            rod.position_collection[0] += 1e-3 * (step + 1)
+            rod.velocity_collection[1] = 0.05 * step
+        dt = sims[0].compute_stable_timestep()
+        for sim, inter in zip(sims, inters, strict=True):
+            inter.time_step(dt=dt)
+            inter()
+            sim.time_step(dt=dt, free_stream_velocity=fs)
+        assert inters[0]._rod_args_cache is not None and inters[1]._rod_args_cache is None
+        a, b = inters
+        np.testing.assert_array_equal(a.forcing_grid.position_field, b.forcing_grid.position_field)
+        np.testing.assert_array_equal(a.forcing_grid.velocity_field, b.forcing_grid.velocity_field)
+        np.testing.assert_array_equal(a.lag_grid_forcing_host(), b.lag_grid_forcing_host())
+        np.testing.assert_array_equal(host(sims[0].vorticity_field), host(sims[1].vorticity_field))
