@@ -14,6 +14,15 @@ Workloads (``--workload``, one GPU each; the default is the headline one):
   carpet256  3D 256^3, fp32, a 4 x 4 carpet of 16 clamped rods (100 elements,
              length 0.2, radius 0.005) standing on the plane z0 = 6 dx, one
              interactor per rod, U = 1 along x, Re = 500 on the rod length.
+  batch64    64 2D cylinder flows of uneven sizes (128x256 to 512x1024) and
+             Reynolds numbers advanced by the batched persistent launches, against
+             the same 64 instances run one after another.
+  adjoint2d  the cylinder flow's drag integrated over 200 frozen-dt steps and its
+             gradient with respect to the marker wall velocities and the viscosity
+             (adjoint step time against the forward step, finite differences, the
+             oracle's FP64 adjoint).
+  pointsource256  passive transport (ENO3 advection + diffusion) of a vector point
+             source at 256^3, with the reference example's 128^3 run for accuracy.
 
 One step is: stable dt, every interactor's time_step + interaction +
 spreading, then the flow time step.  Rods and the cylinder stay on the host
