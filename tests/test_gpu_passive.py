@@ -208,3 +208,20 @@ def test_large_grids_vs_oracle(grid):
     _lib.call("sg_advection_eno3_flux_3d", sg_dtype(rt), *grid, ptr(fd[1]), ptr(flux), ptr(ud), 0.7, s)
     ref = base + st.eno3_flux_3d(f[1], u, rt(0.7))
     assert rel_l2(host(flux), ref) < 1e-13
+
+
+@pytest.mark.parametrize("rt", [np.float32, np.float64])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_module_stable_timestep_function(rt, dim):
+    """compute_advection_diffusion_stable_timestep (passive_transport_flow_simulators.py:139-155): the dt
+    equals the oracle's, and the magnitude field holds sum_d |u_d|."""
+    from oracle.flow import stable_timestep
+    from sopht_gb300.simulator.flow import compute_advection_diffusion_stable_timestep
+    rng = np.random.default_rng(dim)
+    grid = (24, 40) if dim == 2 else (12, 16, 20)
+    u = rng.standard_normal((dim, *grid)).astype(rt)
+    mag = torch.zeros(grid, dtype=torch.float32 if rt == np.float32 else torch.float64, device="cuda")
+    dx = rt(1.0 / grid[-1])
+    dt = compute_advection_diffusion_stable_timestep(dev(u), mag, dim, dx, 0.1, 1e-3, real_t=rt)
+    assert dt == stable_timestep(u, dim, dx, 0.1, 1e-3, rt)
+    np.testing.assert_allclose(host(mag), np.sum(np.fabs(u), axis=0), rtol=1e-6 if rt == np.float32 else 1e-14)
