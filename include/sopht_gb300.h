@@ -246,6 +246,32 @@ int sg_penalise_3d(int dtype, int nz, int ny, int nx, const void* field_in, void
 int sg_laplacian_filter_3d(int dtype, int nz, int ny, int nx, void* field, int filter_type,
                            int filter_order, void* scratch_a, void* scratch_b, void* stream);
 
+/* ------------------------------------- elementwise and flux-form operators */
+/* The lower-level factories of stencil_ops_{2,3}d/elementwise_ops_{2,3}d.py on
+ * n contiguous values: op 0 set (out = alpha), 1 add a fixed value
+ * (out = a + alpha), 2 copy (out = a), 3 sum (out = a + b), 4 saxpby
+ * (out = alpha a + beta b), 5 complex product of n interleaved complex values
+ * (re = ar br - ai bi, im = ar bi + ai br).  alpha and beta are rounded to the
+ * field type first, as pystencils passes them. */
+int sg_elementwise(int dtype, int op, int64_t n, const void* a, const void* b, void* out,
+                   double alpha, double beta, void* stream);
+/* gen_set_fixed_val_at_boundaries_pyst_kernel_{2,3}d (elementwise_ops_2d.py:
+ * 193-253, elementwise_ops_3d.py:200-268): every cell within `width` of a face
+ * of the grid set to `value` (dim 2 ignores nz). */
+int sg_set_boundary_zone(int dtype, int dim, int nz, int ny, int nx, int width, void* field,
+                         double value, void* stream);
+/* gen_diffusion_flux_pyst_kernel_{2,3}d (diffusion_flux_2d.py:13-72,
+ * diffusion_flux_3d.py:14-115): flux = k lap(field) on [1:-1] in the
+ * reference's term order; with reset_ghost_zone the ring is set to 0, without
+ * it the ring is left unchanged.  field and flux must not alias. */
+int sg_diffusion_flux(int dtype, int dim, int nz, int ny, int nx, const void* field, void* flux,
+                      double k, int reset_ghost_zone, void* stream);
+/* gen_advection_flux_conservative_eno3_pyst_kernel_2d (advection_flux_2d.py:
+ * 12-165): flux += the four ENO3 face fluxes of a 2D scalar field on [2:-2]^2 in
+ * the reference's pass order (in place on `flux`). */
+int sg_advection_eno3_flux_2d(int dtype, int ny, int nx, const void* field, void* flux,
+                              const void* velocity, double inv_dx, void* stream);
+
 /* ------------------------------------------------------ passive transport */
 /* Replaces the 3D conservative ENO3 advection timestep
  * (stencil_ops_3d/advection_timestep_3d.py:38-96 with advection_flux_3d.py:

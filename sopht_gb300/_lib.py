@@ -85,6 +85,10 @@ _SIGNATURES = {
                                c_void_p]),
     "sg_laplacian_filter_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                        c_void_p]),
+    "sg_elementwise": (c_int, [c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_double, c_void_p]),
+    "sg_set_boundary_zone": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_double, c_void_p]),
+    "sg_diffusion_flux": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_int, c_void_p]),
+    "sg_advection_eno3_flux_2d": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p]),
     "sg_advection_eno3_step_3d": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double,
                                           c_void_p]),
     "sg_advection_eno3_flux_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double,

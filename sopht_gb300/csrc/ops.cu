@@ -360,3 +360,158 @@ extern "C" int sg_passive_transport_step(int dtype, int dim, int nz, int ny, int
                       passive_step<double>(dim, nz, ny, nx, ncomp, field, scratch, velocity, dt_by_dx, nu_dt_by_dx2,
                                            s));
 }
+
+// ------------------------------------------------------ elementwise and flux-form operators
+// The lower-level factories of elementwise_ops_{2,3}d.py, diffusion_flux_{2,3}d.py and
+// advection_flux_2d.py, each one launch over contiguous arrays.
+namespace sg {
+
+enum { EW_SET = 0, EW_ADD_FIXED = 1, EW_COPY = 2, EW_SUM = 3, EW_SAXPBY = 4, EW_COMPLEX_PRODUCT = 5 };
+
+template <typename T>
+__global__ void __launch_bounds__(256) elementwise_kernel(int op, int64_t n, const T* a, const T* b, T* out, T alpha,
+                                                          T beta) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    switch (op) {
+        case EW_SET: out[i] = alpha; break;
+        case EW_ADD_FIXED: out[i] = a[i] + alpha; break;
+        case EW_COPY: out[i] = a[i]; break;
+        case EW_SUM: out[i] = a[i] + b[i]; break;
+        case EW_SAXPBY: out[i] = alpha * a[i] + beta * b[i]; break;
+        default: {  // n interleaved complex values (real, imaginary)
+            const T ar = a[2 * i], ai = a[2 * i + 1], br = b[2 * i], bi = b[2 * i + 1];
+            out[2 * i] = ar * br - ai * bi;
+            out[2 * i + 1] = ar * bi + ai * br;
+        }
+    }
+}
+
+// cells within `width` of any face of the grid (2D: nz = 1, no z faces) set to `value`
+template <typename T>
+__global__ void __launch_bounds__(256) boundary_zone_kernel(int dim, int nz, int ny, int nx, int width, T* f, T value) {
+    const int x = blockIdx.x * kCell3X + threadIdx.x, y = blockIdx.y * kCell3Y + threadIdx.y, z = blockIdx.z;
+    if (x >= nx || y >= ny) return;
+    bool edge = x < width || x >= nx - width || y < width || y >= ny - width;
+    if (dim == 3) edge = edge || z < width || z >= nz - width;
+    if (edge) f[((int64_t)z * ny + y) * nx + x] = value;
+}
+
+// flux = k lap(field) on the interior [1:-1]; the ring is set to 0 when reset, else left as it is
+template <typename T>
+__global__ void __launch_bounds__(256) diffusion_flux_kernel(int dim, int nz, int ny, int nx, const T* f, T* flux, T k,
+                                                             int reset) {
+    const int x = blockIdx.x * kCell3X + threadIdx.x, y = blockIdx.y * kCell3Y + threadIdx.y, z = blockIdx.z;
+    if (x >= nx || y >= ny) return;
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    const int64_t g = (int64_t)z * sz + (int64_t)y * nx + x;
+    const bool in = x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2 && (dim == 2 || (z >= 1 && z <= nz - 2));
+    if (in) {
+        if (dim == 2) {
+            // diffusion_flux_2d.py:36-38 term order: y+1, y-1, x+1, x-1
+            flux[g] = k * (f[g + sy] + f[g - sy] + f[g + 1] + f[g - 1] - T(4) * f[g]);
+        } else {
+            // diffusion_flux_3d.py:34-43 term order: z+1, z-1, y+1, y-1, x+1, x-1
+            flux[g] = k * (f[g + sz] + f[g - sz] + f[g + sy] + f[g - sy] + f[g + 1] + f[g - 1] - T(6) * f[g]);
+        }
+    } else if (reset) {
+        flux[g] = T(0);
+    }
+}
+
+// flux += the four ENO3 face fluxes of a 2D scalar field on [2:-2]^2, in the passes' order
+// (advection_flux_2d.py:28-128: x front, x back, y front, y back)
+template <typename T>
+__global__ void __launch_bounds__(256) eno3_2d_flux_kernel(int ny, int nx, const T* f, const T* u, T* flux, T inv_dx) {
+    const int x = blockIdx.x * kCell3X + threadIdx.x, y = blockIdx.y * kCell3Y + threadIdx.y;
+    if (x < 2 || y < 2 || x > nx - 3 || y > ny - 3) return;
+    const int64_t n = (int64_t)ny * nx;
+    const int64_t g = (int64_t)y * nx + x;
+    T acc = flux[g];
+#pragma unroll
+    for (int axis = 0; axis < 2; ++axis) {
+        const int64_t s = axis == 0 ? 1 : nx;
+        const T* ua = u + axis * n;
+        auto q = [&](int k) { return f[g + k * s] * ua[g + k * s]; };
+        const T front = eno3_face(q(-1), q(0), q(1), q(2), ua[g], ua[g + s]);
+        const T back = eno3_face(q(-2), q(-1), q(0), q(1), ua[g - s], ua[g]);
+        acc = fma(inv_dx, front, acc);
+        acc = fma(-inv_dx, back, acc);
+    }
+    flux[g] = acc;
+}
+
+template <typename T>
+static int elementwise_op(int op, int64_t n, const void* a, const void* b, void* out, double alpha, double beta,
+                          cudaStream_t s) {
+    if (n == 0) return SG_OK;
+    elementwise_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(op, n, (const T*)a, (const T*)b, (T*)out, (T)alpha,
+                                                           (T)beta);
+    return launch_status("elementwise");
+}
+
+}  // namespace sg
+
+extern "C" int sg_elementwise(int dtype, int op, int64_t n, const void* a, const void* b, void* out, double alpha,
+                              double beta, void* stream) {
+    SG_REQUIRE(op >= EW_SET && op <= EW_COMPLEX_PRODUCT, SG_ERR_INVALID_ARG, "elementwise: bad op %d", op);
+    SG_REQUIRE(n >= 0 && out, SG_ERR_INVALID_ARG, "elementwise: bad argument");
+    SG_REQUIRE(op == EW_SET || a, SG_ERR_INVALID_ARG, "elementwise: null input");
+    SG_REQUIRE((op != EW_SUM && op != EW_SAXPBY && op != EW_COMPLEX_PRODUCT) || b, SG_ERR_INVALID_ARG,
+               "elementwise: null second input");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, elementwise_op<float>(op, n, a, b, out, alpha, beta, s),
+                      elementwise_op<double>(op, n, a, b, out, alpha, beta, s));
+}
+
+extern "C" int sg_set_boundary_zone(int dtype, int dim, int nz, int ny, int nx, int width, void* field, double value,
+                                    void* stream) {
+    SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "boundary zone: dim must be 2 or 3");
+    SG_REQUIRE(field && width > 0, SG_ERR_INVALID_ARG, "boundary zone: bad argument");
+    if (dim == 2) nz = 1;
+    SG_REQUIRE(nz >= 1 && ny >= 1 && nx >= 1, SG_ERR_SHAPE, "boundary zone: bad extent");
+    auto s = (cudaStream_t)stream;
+    const dim3 grid = cell3_grid(Grid3{nz, ny, nx});
+    if (dtype == SG_F32)
+        boundary_zone_kernel<float><<<grid, cell3_block(), 0, s>>>(dim, nz, ny, nx, width, (float*)field, (float)value);
+    else {
+        SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "boundary zone: bad dtype");
+        boundary_zone_kernel<double><<<grid, cell3_block(), 0, s>>>(dim, nz, ny, nx, width, (double*)field, value);
+    }
+    return launch_status("boundary zone");
+}
+
+extern "C" int sg_diffusion_flux(int dtype, int dim, int nz, int ny, int nx, const void* field, void* flux, double k,
+                                 int reset_ghost_zone, void* stream) {
+    SG_REQUIRE(dim == 2 || dim == 3, SG_ERR_INVALID_ARG, "diffusion flux: dim must be 2 or 3");
+    if (dim == 2) nz = 1;
+    SG_TRY(check3d(nz, ny, nx, field, flux));
+    auto s = (cudaStream_t)stream;
+    const dim3 grid = cell3_grid(Grid3{nz, ny, nx});
+    if (dtype == SG_F32)
+        diffusion_flux_kernel<float><<<grid, cell3_block(), 0, s>>>(dim, nz, ny, nx, (const float*)field, (float*)flux,
+                                                                    (float)k, reset_ghost_zone);
+    else {
+        SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "diffusion flux: bad dtype");
+        diffusion_flux_kernel<double><<<grid, cell3_block(), 0, s>>>(dim, nz, ny, nx, (const double*)field,
+                                                                     (double*)flux, k, reset_ghost_zone);
+    }
+    return launch_status("diffusion flux");
+}
+
+extern "C" int sg_advection_eno3_flux_2d(int dtype, int ny, int nx, const void* field, void* flux, const void* velocity,
+                                         double inv_dx, void* stream) {
+    SG_TRY(check2d(ny, nx, field, flux));
+    SG_REQUIRE(velocity, SG_ERR_INVALID_ARG, "null velocity");
+    auto s = (cudaStream_t)stream;
+    const dim3 grid = cell3_grid(Grid3{1, ny, nx});
+    if (dtype == SG_F32)
+        eno3_2d_flux_kernel<float><<<grid, cell3_block(), 0, s>>>(ny, nx, (const float*)field, (const float*)velocity,
+                                                                  (float*)flux, (float)inv_dx);
+    else {
+        SG_REQUIRE(dtype == SG_F64, SG_ERR_INVALID_ARG, "eno3 2d flux: bad dtype");
+        eno3_2d_flux_kernel<double><<<grid, cell3_block(), 0, s>>>(ny, nx, (const double*)field,
+                                                                   (const double*)velocity, (double*)flux, inv_dx);
+    }
+    return launch_status("eno3 2d flux");
+}

@@ -414,3 +414,249 @@ def gen_divergence_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=Fal
                   float(real_t(inv_dx)), stream_ptr(field.device))
 
     return kernel
+
+
+# ------------------------------------------------- elementwise and flux-form factories
+# stencil_ops_{2,3}d/elementwise_ops_{2,3}d.py, diffusion_flux_{2,3}d.py, advection_flux_2d.py.
+# Each callable is one launch over C-contiguous CUDA tensors of real_t (a vector field's
+# components are handled in the same launch unless they take different values).
+
+_EW_SET, _EW_ADD_FIXED, _EW_COPY, _EW_SUM, _EW_SAXPBY, _EW_COMPLEX_PRODUCT = range(6)
+
+
+def _contig(*tensors):
+    for t in tensors:
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous()):
+            raise ValueError("field arguments must be C-contiguous CUDA tensors")
+
+
+def _ew(real_t, op, n, a, b, out, alpha=0.0, beta=0.0, device=None):
+    _lib.call("sg_elementwise", sg_dtype(real_t), op, int(n), ptr(a), ptr(b), ptr(out), float(alpha), float(beta),
+              stream_ptr(device))
+
+
+def _check_field_type(field_type):
+    if field_type not in ("scalar", "vector"):
+        raise ValueError("Invalid field type")
+
+
+def _gen_elementwise_sum(real_t, field_type="scalar"):
+    real_t = normalize_real_t(real_t)
+    _check_field_type(field_type)
+
+    def kernel(sum_field, field_1, field_2):
+        _contig(sum_field, field_1, field_2)
+        _ew(real_t, _EW_SUM, sum_field.numel(), field_1, field_2, sum_field, device=sum_field.device)
+
+    return kernel
+
+
+def _gen_set_fixed_val(real_t, field_type="scalar"):
+    real_t = normalize_real_t(real_t)
+    _check_field_type(field_type)
+    if field_type == "scalar":
+        def kernel(field, fixed_val):
+            _contig(field)
+            _ew(real_t, _EW_SET, field.numel(), None, None, field, real_t(fixed_val), device=field.device)
+    else:
+        def kernel(vector_field, fixed_vals):
+            _contig(vector_field)
+            for c in range(vector_field.shape[0]):
+                _ew(real_t, _EW_SET, vector_field[c].numel(), None, None, vector_field[c], real_t(fixed_vals[c]),
+                    device=vector_field.device)
+    return kernel
+
+
+def _gen_elementwise_copy(real_t):
+    real_t = normalize_real_t(real_t)
+
+    def kernel(field, rhs_field):
+        _contig(field, rhs_field)
+        _ew(real_t, _EW_COPY, field.numel(), rhs_field, None, field, device=field.device)
+
+    return kernel
+
+
+def _gen_elementwise_complex_product(real_t):
+    real_t = normalize_real_t(real_t)
+
+    def kernel(product_field, field_1, field_2):
+        _contig(product_field, field_1, field_2)
+        if not (product_field.is_complex() and field_1.is_complex() and field_2.is_complex()):
+            raise ValueError("complex product: the fields must be complex tensors")
+        _ew(real_t, _EW_COMPLEX_PRODUCT, product_field.numel(), field_1, field_2, product_field,
+            device=product_field.device)
+
+    return kernel
+
+
+def _gen_set_fixed_val_at_boundaries(real_t, width, dim, field_type="scalar"):
+    real_t = normalize_real_t(real_t)
+    if not isinstance(width, (int, np.integer)) or isinstance(width, bool) or width <= 0:
+        raise ValueError("Invalid width for boundary zone, must be a positive integer")
+    _check_field_type(field_type)
+
+    def _one(f, val):
+        ext = f.shape[-dim:]
+        nz, ny, nx = (1, *ext) if dim == 2 else ext
+        _lib.call("sg_set_boundary_zone", sg_dtype(real_t), dim, nz, ny, nx, int(width), ptr(f),
+                  float(real_t(val)), stream_ptr(f.device))
+
+    if field_type == "scalar":
+        def kernel(field, fixed_val):
+            _contig(field)
+            _one(field, fixed_val)
+    else:
+        def kernel(vector_field, fixed_vals):
+            _contig(vector_field)
+            for c in range(vector_field.shape[0]):
+                _one(vector_field[c], fixed_vals[c])
+    return kernel
+
+
+def _gen_add_fixed_val(real_t, field_type="scalar"):
+    real_t = normalize_real_t(real_t)
+    _check_field_type(field_type)
+    if field_type == "scalar":
+        def kernel(sum_field, field, fixed_val):
+            _contig(sum_field, field)
+            _ew(real_t, _EW_ADD_FIXED, field.numel(), field, None, sum_field, real_t(fixed_val), device=field.device)
+    else:
+        def kernel(sum_field, vector_field, fixed_vals):
+            _contig(sum_field, vector_field)
+            for c in range(vector_field.shape[0]):
+                _ew(real_t, _EW_ADD_FIXED, vector_field[c].numel(), vector_field[c], None, sum_field[c],
+                    real_t(fixed_vals[c]), device=vector_field.device)
+    return kernel
+
+
+def _gen_elementwise_saxpby(real_t, field_type="scalar"):
+    real_t = normalize_real_t(real_t)
+    _check_field_type(field_type)
+
+    def kernel(sum_field, field_1, field_2, field_1_prefac, field_2_prefac):
+        _contig(sum_field, field_1, field_2)
+        _ew(real_t, _EW_SAXPBY, sum_field.numel(), field_1, field_2, sum_field, real_t(field_1_prefac),
+            real_t(field_2_prefac), device=sum_field.device)
+
+    return kernel
+
+
+def gen_elementwise_sum_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_2d.py:13-57: sum_field = field_1 + field_2."""
+    return _gen_elementwise_sum(real_t, field_type)
+
+
+def gen_elementwise_sum_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_3d.py:13-57."""
+    return _gen_elementwise_sum(real_t, field_type)
+
+
+def gen_set_fixed_val_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_2d.py:60-114: field = fixed_val (per component for a vector field)."""
+    return _gen_set_fixed_val(real_t, field_type)
+
+
+def gen_set_fixed_val_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_3d.py:60-119."""
+    return _gen_set_fixed_val(real_t, field_type)
+
+
+def gen_elementwise_copy_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False):
+    """elementwise_ops_2d.py:117-138: field = rhs_field."""
+    return _gen_elementwise_copy(real_t)
+
+
+def gen_elementwise_copy_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False):
+    """elementwise_ops_3d.py:122-143."""
+    return _gen_elementwise_copy(real_t)
+
+
+def gen_elementwise_complex_product_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False):
+    """elementwise_ops_2d.py:141-190: product_field = field_1 * field_2 (complex tensors)."""
+    return _gen_elementwise_complex_product(real_t)
+
+
+def gen_elementwise_complex_product_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False):
+    """elementwise_ops_3d.py:146-197."""
+    return _gen_elementwise_complex_product(real_t)
+
+
+def gen_set_fixed_val_at_boundaries_pyst_kernel_2d(real_t, width, num_threads=False, field_type="scalar"):
+    """elementwise_ops_2d.py:193-253: the band of `width` cells along every edge set to fixed_val."""
+    return _gen_set_fixed_val_at_boundaries(real_t, width, 2, field_type)
+
+
+def gen_set_fixed_val_at_boundaries_pyst_kernel_3d(real_t, width, num_threads=False, field_type="scalar"):
+    """elementwise_ops_3d.py:200-268."""
+    return _gen_set_fixed_val_at_boundaries(real_t, width, 3, field_type)
+
+
+def gen_add_fixed_val_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_2d.py:256-313: sum_field = field + fixed_val (per component for a vector field)."""
+    return _gen_add_fixed_val(real_t, field_type)
+
+
+def gen_add_fixed_val_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_3d.py:271-334."""
+    return _gen_add_fixed_val(real_t, field_type)
+
+
+def gen_elementwise_saxpby_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_2d.py:316-370: sum_field = field_1_prefac field_1 + field_2_prefac field_2."""
+    return _gen_elementwise_saxpby(real_t, field_type)
+
+
+def gen_elementwise_saxpby_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar"):
+    """elementwise_ops_3d.py:337-387."""
+    return _gen_elementwise_saxpby(real_t, field_type)
+
+
+def gen_diffusion_flux_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False, reset_ghost_zone=True):
+    """diffusion_flux_2d.py:13-72: diffusion_flux = prefactor lap(field) on [1:-1]^2 (ring zeroed when
+    reset_ghost_zone, else left unchanged)."""
+    real_t = normalize_real_t(real_t)
+
+    def kernel(diffusion_flux, field, prefactor):
+        _contig(diffusion_flux, field)
+        ny, nx = field.shape
+        _lib.call("sg_diffusion_flux", sg_dtype(real_t), 2, 1, ny, nx, ptr(field), ptr(diffusion_flux),
+                  float(real_t(prefactor)), int(bool(reset_ghost_zone)), stream_ptr(field.device))
+
+    return kernel
+
+
+def gen_diffusion_flux_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False, field_type="scalar",
+                                      reset_ghost_zone=True):
+    """diffusion_flux_3d.py:14-115: scalar, or per component of a vector field."""
+    real_t = normalize_real_t(real_t)
+    _check_field_type(field_type)
+
+    def _one(flux, f, prefactor):
+        nz, ny, nx = f.shape
+        _lib.call("sg_diffusion_flux", sg_dtype(real_t), 3, nz, ny, nx, ptr(f), ptr(flux),
+                  float(real_t(prefactor)), int(bool(reset_ghost_zone)), stream_ptr(f.device))
+
+    if field_type == "scalar":
+        def kernel(diffusion_flux, field, prefactor):
+            _contig(diffusion_flux, field)
+            _one(diffusion_flux, field, prefactor)
+    else:
+        def kernel(vector_field_diffusion_flux, vector_field, prefactor):
+            _contig(vector_field_diffusion_flux, vector_field)
+            for c in range(vector_field.shape[0]):
+                _one(vector_field_diffusion_flux[c], vector_field[c], prefactor)
+    return kernel
+
+
+def gen_advection_flux_conservative_eno3_pyst_kernel_2d(real_t, num_threads=False, fixed_grid_size=False):
+    """advection_flux_2d.py:12-165: advection_flux += the four ENO3 face fluxes (in place)."""
+    real_t = normalize_real_t(real_t)
+
+    def kernel(advection_flux, field, velocity, inv_dx):
+        _contig(advection_flux, field, velocity)
+        ny, nx = field.shape
+        _lib.call("sg_advection_eno3_flux_2d", sg_dtype(real_t), ny, nx, ptr(field), ptr(advection_flux),
+                  ptr(velocity), float(real_t(inv_dx)), stream_ptr(field.device))
+
+    return kernel
