@@ -472,6 +472,149 @@ def passive(sps, real_t, rec: _Recorder, seed: int) -> None:
         rec.put(f"sim_{tag}/time_out", sim.time)
 
 
+def _random_directors(rng) -> np.ndarray:
+    """Rows d1, d2, d3 of a random proper rotation, shaped (3, 3, 1)."""
+    q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    if np.linalg.det(q) < 0:
+        q[2] *= -1.0
+    return q.reshape(3, 3, 1)
+
+
+class _FakeRigid3D:
+    """Moving 3D rigid body with the attributes the reference forcing grids read."""
+
+    def __init__(self, rng, radius: float, length: float = 0.0) -> None:
+        self.position_collection = (0.5 + 0.01 * rng.standard_normal(3)).reshape(3, 1)
+        self.director_collection = _random_directors(rng)
+        self.velocity_collection = 0.1 * rng.standard_normal((3, 1))
+        self.omega_collection = rng.standard_normal((3, 1))
+        self.radius = radius
+        self.length = length
+
+
+class _FakeTaperedRod(_FakeRod):
+    """``_FakeRod`` with a tapered radius, unit tangents and angular velocities."""
+
+    def __init__(self, rng, n_elems: int, taper: float) -> None:
+        super().__init__(rng, n_elems)
+        self.radius = 0.02 * np.linspace(1.0, 1.0 / taper, n_elems)
+        diff = np.diff(self.position_collection, axis=1)
+        self.tangents = diff / np.linalg.norm(diff, axis=0)
+        self.omega_collection = rng.standard_normal((3, n_elems))
+        self.director_collection = np.concatenate(
+            [_random_directors(rng) for _ in range(n_elems)], axis=2)
+
+
+def _record_grid(rec: _Recorder, tag: str, grid, rng, n_forces: int, n_torques: int, extra=()) -> None:
+    rec.put(f"{tag}/num_lag_nodes", grid.num_lag_nodes)
+    rec.put(f"{tag}/position", grid.position_field)
+    rec.put(f"{tag}/velocity", grid.velocity_field)
+    rec.put(f"{tag}/spacing", grid.get_maximum_lagrangian_grid_spacing())
+    for name in extra:
+        value = getattr(grid, name)
+        if isinstance(value, list):
+            for i, v in enumerate(value):
+                rec.put(f"{tag}/{name}/{i}", v)
+        else:
+            rec.put(f"{tag}/{name}", value)
+    f = rng.standard_normal(grid.position_field.shape)
+    forces, torques = np.zeros((3, n_forces)), np.zeros((3, n_torques))
+    grid.transfer_forcing_from_grid_to_body(body_flow_forces=forces, body_flow_torques=torques,
+                                            lag_grid_forcing_field=f)
+    rec.put(f"{tag}/lag_forcing_in", f)
+    rec.put(f"{tag}/body_forces", forces)
+    rec.put(f"{tag}/body_torques", torques)
+
+
+def forcing_grids(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """The 3D rigid-body grids (rigid_body_forcing_grids.py:108-349), the plane body
+    (derived_rigid_bodies.py:12-63), the rod edge and surface grids
+    (cosserat_rod_forcing_grids.py:134-589), and two 3D interactions using them."""
+    rng = np.random.default_rng(seed)
+    bodies = {}
+    for tag, cls, make, kw in (
+            ("sphere16", sps.SphereForcingGrid, lambda: _FakeRigid3D(rng, 0.15),
+             {"num_forcing_points_along_equator": 16}),
+            ("sphere7", sps.SphereForcingGrid, lambda: _FakeRigid3D(rng, 0.1),
+             {"num_forcing_points_along_equator": 7}),
+            ("open_cylinder", sps.OpenEndCircularCylinderForcingGrid, lambda: _FakeRigid3D(rng, 0.1, 0.4),
+             {"num_forcing_points_along_length": 8}),
+            ("plane", sps.RectangularPlaneForcingGrid,
+             lambda: sps.RectangularPlane(origin=np.array([0.5, 0.4, 0.6]), plane_normal=np.array([0.2, 0.1, 1.0]),
+                                          plane_tangent_along_length=np.array([1.0, 0.0, -0.2]),
+                                          plane_length=0.4, plane_breadth=0.25),
+             {"num_forcing_points_along_length": 10})):
+        body = make()
+        if tag == "plane":
+            rec.put("plane/directors_as_built", body.director_collection)
+            body.velocity_collection[...] = 0.1 * rng.standard_normal((3, 1))
+            body.omega_collection[...] = rng.standard_normal((3, 1))
+        grid = cls(grid_dim=3, rigid_body=body, **kw)
+        # the grid follows the body: move it and recompute
+        body.position_collection += 0.01
+        body.velocity_collection *= -1.5
+        grid.compute_lag_grid_position_field()
+        grid.compute_lag_grid_velocity_field()
+        bodies[tag] = body
+        rec.put(f"{tag}/body_position", body.position_collection)
+        rec.put(f"{tag}/body_directors", body.director_collection)
+        rec.put(f"{tag}/body_velocity", body.velocity_collection)
+        rec.put(f"{tag}/body_omega", body.omega_collection)
+        rec.put(f"{tag}/body_radius", getattr(body, "radius", 0.0))
+        rec.put(f"{tag}/body_length", getattr(body, "length", 0.0))
+        _record_grid(rec, tag, grid, rng, 1, 1)
+    rod_cases = (("edge", 2, 10, 2.0, {}),
+                 ("surface_cap", 3, 8, 3.0, {"surface_grid_density_for_largest_element": 12, "with_cap": True}),
+                 ("surface_nocap", 3, 8, 5.0, {"surface_grid_density_for_largest_element": 8, "with_cap": False}),
+                 ("surface_one", 3, 1, 1.0, {"surface_grid_density_for_largest_element": 16, "with_cap": True}))
+    for tag, dim, n_elems, taper, kw in rod_cases:
+        rod = _FakeTaperedRod(rng, n_elems, taper)
+        if tag == "edge":
+            grid = sps.CosseratRodEdgeForcingGrid(grid_dim=dim, cosserat_rod=rod)
+            extra = ("moment_arm",)
+        else:
+            grid = sps.CosseratRodSurfaceForcingGrid(grid_dim=dim, cosserat_rod=rod, **kw)
+            extra = ("surface_grid_points", "start_idx", "end_idx", "grid_point_radius_ratio",
+                     "local_frame_surface_points", "moment_arm", "surface_point_rotation_angle_list")
+        for name in ("position_collection", "velocity_collection", "omega_collection", "director_collection",
+                     "mass", "radius", "lengths", "tangents"):
+            rec.put(f"{tag}/rod_{name}", getattr(rod, name))
+        _record_grid(rec, tag, grid, rng, n_elems + 1, n_elems, extra)
+    # 3D interactions through the grids (immersed_body_flow_interaction.py:15-141)
+    grid_shape = (16, 16, 16)
+    dx = real_t(1.0 / 16)
+    eul_vel = rng.standard_normal((3, *grid_shape)).astype(real_t)
+    rec.put("eul_velocity", eul_vel)
+    sphere = _FakeRigid3D(rng, 0.2)
+    rod = _FakeTaperedRod(rng, 6, 2.0)
+    rod.radius = 0.06 * np.linspace(1.0, 0.5, 6)
+    for tag, make in (
+            ("sphere_inter", lambda force: sps.RigidBodyFlowInteraction(
+                rigid_body=sphere, eul_grid_forcing_field=force, eul_grid_velocity_field=eul_vel,
+                virtual_boundary_stiffness_coeff=-2e4, virtual_boundary_damping_coeff=-1e2, dx=dx, grid_dim=3,
+                real_t=real_t, forcing_grid_cls=sps.SphereForcingGrid, num_forcing_points_along_equator=20)),
+            ("surface_inter", lambda force: sps.CosseratRodFlowInteraction(
+                cosserat_rod=rod, eul_grid_forcing_field=force, eul_grid_velocity_field=eul_vel,
+                virtual_boundary_stiffness_coeff=-2e4, virtual_boundary_damping_coeff=-1e2, dx=dx, grid_dim=3,
+                real_t=real_t, forcing_grid_cls=sps.CosseratRodSurfaceForcingGrid,
+                surface_grid_density_for_largest_element=6, with_cap=True))):
+        force = np.zeros((3, *grid_shape), dtype=real_t)
+        inter = make(force)
+        inter.time_step(dt=1e-3)
+        inter()
+        rec.put(f"{tag}/eul_forcing_out", force)
+        rec.put(f"{tag}/lag_forcing", inter.lag_grid_forcing_field)
+        inter.compute_flow_forces_and_torques()
+        rec.put(f"{tag}/body_forces", inter.body_flow_forces)
+        rec.put(f"{tag}/body_torques", inter.body_flow_torques)
+    for name in ("position_collection", "velocity_collection", "omega_collection", "director_collection"):
+        rec.put(f"sphere_inter/body_{name}", getattr(sphere, name))
+        rec.put(f"surface_inter/rod_{name}", getattr(rod, name))
+    for name in ("mass", "radius", "lengths", "tangents"):
+        rec.put(f"surface_inter/rod_{name}", getattr(rod, name))
+    rec.put("sphere_inter/body_radius", sphere.radius)
+
+
 GROUPS = {
     "stencils2d": ("spne", stencils_2d, 11),
     "poisson2d": ("spne", poisson_2d, 12),
@@ -483,6 +626,7 @@ GROUPS = {
     "cylinder2d": ("sps", cylinder_2d, 32),
     "rod3d": ("sps", rod_3d, 33),
     "passive": ("sps", passive, 41),
+    "grids": ("sps", forcing_grids, 42),
 }
 
 
