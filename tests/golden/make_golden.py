@@ -613,6 +613,33 @@ def forcing_grids(sps, real_t, rec: _Recorder, seed: int) -> None:
     for name in ("mass", "radius", "lengths", "tangents"):
         rec.put(f"surface_inter/rod_{name}", getattr(rod, name))
     rec.put("sphere_inter/body_radius", sphere.radius)
+    # a 2D interaction through the edge grid: a tapered rod lying in the XY plane
+    grid_2d = (32, 48)
+    dx = real_t(1.0 / 48)
+    eul_vel_2d = rng.standard_normal((2, *grid_2d)).astype(real_t)
+    rod = _FakeTaperedRod(rng, 12, 2.0)
+    s = np.linspace(0.0, 0.4, 13)
+    rod.position_collection = np.stack([0.3 + s, 0.33 + 0.02 * np.sin(9 * s), 0.0 * s])
+    diff = np.diff(rod.position_collection, axis=1)
+    rod.lengths = np.linalg.norm(diff, axis=0)
+    rod.tangents = diff / rod.lengths
+    rod.radius = 0.03 * np.linspace(1.0, 0.5, 12)
+    force = np.zeros((2, *grid_2d), dtype=real_t)
+    inter = sps.CosseratRodFlowInteraction(
+        cosserat_rod=rod, eul_grid_forcing_field=force, eul_grid_velocity_field=eul_vel_2d,
+        virtual_boundary_stiffness_coeff=-5e4, virtual_boundary_damping_coeff=-20.0, dx=dx, grid_dim=2,
+        real_t=real_t, forcing_grid_cls=sps.CosseratRodEdgeForcingGrid)
+    inter.time_step(dt=1e-3)
+    inter()
+    rec.put("edge_inter/eul_velocity", eul_vel_2d)
+    rec.put("edge_inter/eul_forcing_out", force)
+    rec.put("edge_inter/lag_forcing", inter.lag_grid_forcing_field)
+    inter.compute_flow_forces_and_torques()
+    rec.put("edge_inter/body_forces", inter.body_flow_forces)
+    rec.put("edge_inter/body_torques", inter.body_flow_torques)
+    for name in ("position_collection", "velocity_collection", "omega_collection", "director_collection",
+                 "mass", "radius", "lengths", "tangents"):
+        rec.put(f"edge_inter/rod_{name}", getattr(rod, name))
 
 
 GROUPS = {
