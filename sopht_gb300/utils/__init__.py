@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _lib
+from .. import _lib
 
 
 def get_real_t(precision: str = "single") -> type:
@@ -106,3 +106,7 @@ def as_device(x, dtype: torch.dtype, device: torch.device, out: torch.Tensor | N
         return src.to(device=device, non_blocking=True).contiguous()
     out.copy_(src, non_blocking=True)
     return out
+
+
+from .io import IO, CosseratRodIO, EulerianFieldIO  # noqa: E402
+from .restart_sim import restart_simulation  # noqa: E402

@@ -642,6 +642,71 @@ def forcing_grids(sps, real_t, rec: _Recorder, seed: int) -> None:
         rec.put(f"edge_inter/rod_{name}", getattr(rod, name))
 
 
+def field_io(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """The HDF5 + XDMF field IO (sopht/utils/io.py:13-694) through the in-memory h5py
+    stand-in: the saved tree (datasets, attributes) and the XDMF text of three cases."""
+    import os
+    import tempfile
+
+    import memory_h5
+    import sopht.utils.io as ref_io
+    ref_io.h5py = memory_h5
+    rng = np.random.default_rng(seed)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:
+        os.chdir(tmp)
+        try:
+            # 3D: scalar and vector Eulerian fields, a named and an unnamed (connected) Lagrangian grid
+            grid = np.array([8, 10, 12])
+            io = ref_io.IO(dim=3, real_dtype=real_t)
+            origin, dx = np.array([0.1, 0.2, 0.3]), np.array([0.05, 0.05, 0.05])
+            io.define_eulerian_grid(origin=origin, dx=dx, grid_size=grid)
+            eul = {"vorticity_mag": rng.standard_normal(tuple(grid)).astype(real_t),
+                   "velocity": rng.standard_normal((3, *grid)).astype(real_t)}
+            io.add_as_eulerian_fields_for_io(**eul)
+            lag = {"sphere_grid": rng.standard_normal((3, 20)), "radius_field": rng.standard_normal(20),
+                   "forcing": rng.standard_normal((3, 20)), "rod_grid": rng.standard_normal((3, 7)),
+                   "rod_velocity": rng.standard_normal((3, 7))}
+            io.add_as_lagrangian_fields_for_io(lagrangian_grid=lag["sphere_grid"], lagrangian_grid_name="sphere",
+                                               radius_field=lag["radius_field"], forcing=lag["forcing"])
+            io.add_as_lagrangian_fields_for_io(lagrangian_grid=lag["rod_grid"], lagrangian_grid_connect=True,
+                                               rod_velocity=lag["rod_velocity"])
+            io.save(h5_file_name="sopht_0003.h5", time=0.125)
+            for k, v in {**eul, **lag}.items():
+                rec.put(f"eul3d/in/{k}", v)
+            for k, v in memory_h5.dump("sopht_0003.h5").items():
+                rec.put(f"eul3d/h5/{k}", v)
+            for name in ("eulerian", "sphere", "Lagrangian_grid_0"):
+                rec.put(f"eul3d/xmf/{name}", Path(f"sopht_0003_{name}.xmf").read_text())
+            # 2D, from a simulator-style position field
+            ny, nx = 6, 10
+            h = 1.0 / nx
+            axes = [np.linspace(h / 2, n * h - h / 2, n).astype(real_t) for n in (ny, nx)]
+            position = np.flipud(np.array(np.meshgrid(*axes, indexing="ij")))
+            fields = {"vorticity": rng.standard_normal((ny, nx)).astype(real_t),
+                      "velocity": rng.standard_normal((2, ny, nx)).astype(real_t)}
+            io = ref_io.EulerianFieldIO(position_field=position, eulerian_fields_dict=fields)
+            io.save(h5_file_name="flow_0001.h5", time=2.5)
+            rec.put("eul2d/in/position", position)
+            for k, v in fields.items():
+                rec.put(f"eul2d/in/{k}", v)
+            for k, v in memory_h5.dump("flow_0001.h5").items():
+                rec.put(f"eul2d/h5/{k}", v)
+            rec.put("eul2d/xmf/eulerian", Path("flow_0001_eulerian.xmf").read_text())
+            # a rod
+            rod = _FakeTaperedRod(rng, 9, 2.0)
+            io = ref_io.CosseratRodIO(cosserat_rod=rod, dim=3, real_dtype=real_t)
+            rod.position_collection += 0.01  # save reads the rod as it is then
+            io.save(h5_file_name="rod_0007.h5", time=1.0)
+            rec.put("rod/in/position_collection", rod.position_collection)
+            rec.put("rod/in/radius", rod.radius)
+            for k, v in memory_h5.dump("rod_0007.h5").items():
+                rec.put(f"rod/h5/{k}", v)
+            rec.put("rod/xmf/rod", Path("rod_0007_rod.xmf").read_text())
+        finally:
+            os.chdir(cwd)
+
+
 GROUPS = {
     "stencils2d": ("spne", stencils_2d, 11),
     "poisson2d": ("spne", poisson_2d, 12),
@@ -654,6 +719,7 @@ GROUPS = {
     "rod3d": ("sps", rod_3d, 33),
     "passive": ("sps", passive, 41),
     "grids": ("sps", forcing_grids, 42),
+    "io": ("sps", field_io, 43),
 }
 
 
