@@ -406,6 +406,9 @@ def test_cylinder_coupled_steps_vs_reference(precision):
         assert rel_l2(host(sim.vorticity_field), g[f"step{step}/vorticity"]) < bound
         assert rel_l2(host(sim.velocity_field), g[f"step{step}/velocity"]) < bound
         assert rel_l2(host(inter.lag_grid_forcing_field), g[f"step{step}/lag_forcing"]) < bound
+        assert rel_l2(host(inter.lag_grid_position_mismatch_field), g[f"step{step}/position_mismatch"]) < bound
+    # immersed_body_flow_interaction.py:133-141
+    assert inter.get_grid_deviation_error_l2_norm() == pytest.approx(float(g["grid_deviation"]), rel=bound)
     inter.compute_flow_forces_and_torques()
     scale = np.abs(g["body_forces"]).max()
     atol = scale * (1e-5 if rt == np.float32 else 1e-11)
