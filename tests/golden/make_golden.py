@@ -642,6 +642,49 @@ def forcing_grids(sps, real_t, rec: _Recorder, seed: int) -> None:
         rec.put(f"edge_inter/rod_{name}", getattr(rod, name))
 
 
+def forcing_grids_random(sps, real_t, rec: _Recorder, seed: int) -> None:
+    """Randomised cases of every 3D rigid-body and tapered-rod forcing grid: sizes, marker
+    counts, tapers, cap flags and body states drawn at random (including one-element rods,
+    one-point rings and densities below 3), with the reference's geometry, kinematics and
+    force/torque transfer for a random forcing."""
+    rng = np.random.default_rng(seed)
+    body_names = ("position_collection", "director_collection", "velocity_collection", "omega_collection")
+    rod_names = ("position_collection", "velocity_collection", "omega_collection", "director_collection",
+                 "mass", "radius", "lengths", "tangents")
+    for i in range(12):
+        radius, length, breadth = rng.uniform(0.01, 0.3), rng.uniform(0.05, 1.0), rng.uniform(0.05, 1.0)
+        for kind, cls, key, hi in (("sphere", sps.SphereForcingGrid, "num_forcing_points_along_equator", 40),
+                                   ("open_cylinder", sps.OpenEndCircularCylinderForcingGrid,
+                                    "num_forcing_points_along_length", 24),
+                                   ("plane", sps.RectangularPlaneForcingGrid, "num_forcing_points_along_length", 24)):
+            body = _FakeRigid3D(rng, radius, length)
+            body.breadth = breadth
+            count = int(rng.integers(1, hi))
+            grid = cls(grid_dim=3, rigid_body=body, **{key: count})
+            tag = f"{kind}/{i}"
+            for name in body_names:
+                rec.put(f"{tag}/body_{name}", getattr(body, name))
+            rec.put(f"{tag}/params", [radius, length, breadth, count])
+            _record_grid(rec, tag, grid, rng, 1, 1)
+        n_elems, taper = int(rng.integers(1, 13)), float(rng.uniform(1.0, 12.0))
+        rod = _FakeTaperedRod(rng, n_elems, taper)
+        grid = sps.CosseratRodEdgeForcingGrid(grid_dim=2, cosserat_rod=rod)
+        for name in rod_names:
+            rec.put(f"edge/{i}/rod_{name}", getattr(rod, name))
+        _record_grid(rec, f"edge/{i}", grid, rng, n_elems + 1, n_elems)
+        for kind, scale in (("surface", 1.0), ("surface_wide", 20.0)):  # wide: caps with several rings
+            rod = _FakeTaperedRod(rng, n_elems, taper)
+            rod.radius = rod.radius * scale
+            density, cap = int(rng.integers(1, 24)), bool(rng.integers(0, 2))
+            grid = sps.CosseratRodSurfaceForcingGrid(grid_dim=3, cosserat_rod=rod,
+                                                     surface_grid_density_for_largest_element=density, with_cap=cap)
+            tag = f"{kind}/{i}"
+            for name in rod_names:
+                rec.put(f"{tag}/rod_{name}", getattr(rod, name))
+            rec.put(f"{tag}/params", [density, int(cap)])
+            _record_grid(rec, tag, grid, rng, n_elems + 1, n_elems, ("surface_grid_points",))
+
+
 def field_io(sps, real_t, rec: _Recorder, seed: int) -> None:
     """The HDF5 + XDMF field IO (sopht/utils/io.py:13-694) through the in-memory h5py
     stand-in: the saved tree (datasets, attributes) and the XDMF text of three cases."""
@@ -720,7 +763,9 @@ GROUPS = {
     "passive": ("sps", passive, 41),
     "grids": ("sps", forcing_grids, 42),
     "io": ("sps", field_io, 43),
+    "gridsrandom": ("sps", forcing_grids_random, 44),
 }
+HOST_ONLY = {"gridsrandom"}
 
 
 def _load_test_restatements(ref_root: str, rel: str, ns: dict | None = None) -> dict:
@@ -885,6 +930,8 @@ def main(ref_root: str = "/root/reference", *groups: str) -> None:
         if groups and group not in groups:
             continue
         for prec, real_t in PRECISIONS.items():
+            if group in HOST_ONLY and prec != "double":
+                continue  # float64 host geometry: one file serves both precisions
             rec = _Recorder()
             fn(mods[modname], real_t, rec, seed)
             out = HERE / f"golden_{group}_{prec}.npz"

@@ -248,3 +248,41 @@ def test_interaction_through_grids_vs_reference(precision, tag):
     inter.compute_flow_forces_and_torques()
     np.testing.assert_allclose(inter.body_flow_forces, gg[f"{tag}/body_forces"], rtol=tol, atol=tol)
     np.testing.assert_allclose(inter.body_flow_torques, gg[f"{tag}/body_torques"], rtol=tol, atol=tol)
+
+
+# ------------------------------------------------------- randomised cases
+
+
+@pytest.fixture(scope="module")
+def gr():
+    return load_golden("gridsrandom", "double")
+
+
+@pytest.mark.parametrize("kind", ["sphere", "open_cylinder", "plane"])
+@pytest.mark.parametrize("i", range(12))
+def test_rigid_grids_random_cases_vs_reference(gr, kind, i):
+    tag = f"{kind}/{i}"
+    radius, length, breadth, count = gr[f"{tag}/params"]
+    body = types.SimpleNamespace(**{n: gr[f"{tag}/body_{n}"].copy() for n in
+                                    ("position_collection", "director_collection", "velocity_collection",
+                                     "omega_collection")}, radius=radius, length=length, breadth=breadth)
+    cls, key = {"sphere": (sps.SphereForcingGrid, "num_forcing_points_along_equator"),
+                "open_cylinder": (sps.OpenEndCircularCylinderForcingGrid, "num_forcing_points_along_length"),
+                "plane": (sps.RectangularPlaneForcingGrid, "num_forcing_points_along_length")}[kind]
+    _check_grid(gr, tag, cls(grid_dim=3, rigid_body=body, **{key: int(count)}), 1, 1)
+
+
+@pytest.mark.parametrize("kind", ["edge", "surface", "surface_wide"])
+@pytest.mark.parametrize("i", range(12))
+def test_rod_grids_random_cases_vs_reference(gr, kind, i):
+    tag = f"{kind}/{i}"
+    rod = _rod(gr, tag)
+    if kind == "edge":
+        grid = sps.CosseratRodEdgeForcingGrid(grid_dim=2, cosserat_rod=rod)
+    else:
+        density, cap = gr[f"{tag}/params"]
+        grid = sps.CosseratRodSurfaceForcingGrid(grid_dim=3, cosserat_rod=rod,
+                                                 surface_grid_density_for_largest_element=int(density),
+                                                 with_cap=bool(cap))
+        np.testing.assert_array_equal(grid.surface_grid_points, gr[f"{tag}/surface_grid_points"])
+    _check_grid(gr, tag, grid, rod.n_elems + 1, rod.n_elems)
