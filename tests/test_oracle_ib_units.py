@@ -5,8 +5,8 @@ markers on grid nodes give their node index and offsets k dx (k = -1..2);
 interpolating a field of ones with weights 0..4^dim - 1 gives their sum times
 dx^dim; spreading 2 with unit weights puts n_lag * 2 * 4^dim on the grid;
 with offsets 0 along x and dx along the other axes both delta kernels weigh
-every support cell the same, 2 (0.25/dx)^dim (a factor 2 along x, 1 along the others).  Tolerance: 1e3 eps
-absolute, as in the reference.
+every support cell the same, 2 (0.25/dx)^dim (a factor 2 along x, 1 along the
+others).  Tolerance: 1e3 eps, as in the reference.
 """
 
 from __future__ import annotations
