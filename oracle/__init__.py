@@ -13,7 +13,10 @@ never imports it and has no CPU fallback.
 
 Parity pinning: the oracle is checked against golden fixtures produced by
 running the reference package itself (``tests/golden/make_golden.py``) and
-against the known-answer cases of the reference's own tests.
+against the known-answer cases of the reference's own tests.  ``rod`` (the
+discrete Cosserat rod model pyelastica implements, for a future batched rod
+integrator) is the exception: pyelastica is not installed, so its parity is
+unpinned and it is pinned to analytic solutions and conservation laws instead.
 
 Precision: every routine takes ``real_t`` (``np.float32`` or ``np.float64``) and
 follows the reference's numpy type promotion (weak Python scalars, float64
