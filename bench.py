@@ -972,8 +972,11 @@ def run_passive(args, rank, world):
         gw = g_sim.primary_field.cpu().numpy()
         acc["fp64_gpu_vs_fp64_oracle_rel_l2_3_steps_128cube"] = float(np.linalg.norm(gw - ora.primary_field)
                                                                      / np.linalg.norm(ora.primary_field))
-        # CPU baseline: the oracle (fp32) on the same 256^3 workload, a bounded sample
-        c_ora = PassiveTransportOracle(1e-3, 3, grid, 1.0, real_t=np.float32, time=5.0, field_type="vector")
+        # CPU baseline: the oracle (fp32, sweeps on z-slabs across the cores) on the same 256^3 workload,
+        # a bounded sample
+        from oracle.threaded import ThreadedPassiveTransportOracle
+        c_ora = ThreadedPassiveTransportOracle(1e-3, 3, grid, 1.0, real_t=np.float32, time=5.0,
+                                               field_type="vector")
         c_ora.velocity_field[...] = 1.0
         c_ora.primary_field[...] = point_source(c_ora.position_field, (0.3,) * 3, 1e-3,
                                                 4.0 * np.pi * 1e-3 * 5.0**1.5, 5.0, np.float32)[None]
@@ -988,7 +991,7 @@ def run_passive(args, rank, world):
         cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
         cpu = {"value": round(nc / el, 4), "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": f"{nc} steps of the same 256^3 vector workload after 1 warm-up step ({el:.1f} s), "
-                         "numpy, fp32"}
+                         "numpy sweeps on z-slabs across all cores, fp32"}
     if rank != 0:
         return
     peaks = load_peaks()
@@ -1034,9 +1037,9 @@ def run_passive_reference(args, rank, world):
     """The reference's passive-transport algorithm on the host cores (the numpy oracle), same 256^3 workload."""
     if rank != 0:
         return
-    from oracle.flow import PassiveTransportOracle
+    from oracle.threaded import ThreadedPassiveTransportOracle
     grid = (256, 256, 256)
-    ora = PassiveTransportOracle(1e-3, 3, grid, 1.0, real_t=np.float32, time=5.0, field_type="vector")
+    ora = ThreadedPassiveTransportOracle(1e-3, 3, grid, 1.0, real_t=np.float32, time=5.0, field_type="vector")
     ora.velocity_field[...] = 1.0
     ora.primary_field[...] = point_source(ora.position_field, (0.3,) * 3, 1e-3, 4.0 * np.pi * 1e-3 * 5.0**1.5, 5.0,
                                           np.float32)[None]
@@ -1057,7 +1060,8 @@ def run_passive_reference(args, rank, world):
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "ms_per_step": round(1e3 / v, 2),
            "config": {"workload": "3D 256^3 fp32 passive transport of a vector point source", "grid": list(grid)},
            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
-                            "sample": f"{n} steps after 1 warm-up step ({el:.1f} s), numpy, fp32"},
+                            "sample": f"{n} steps after 1 warm-up step ({el:.1f} s), numpy sweeps on "
+                                      "z-slabs across all cores, fp32"},
            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -1147,11 +1151,12 @@ def make_cpu_case(wl: Workload, real_t=np.float32):
         CircularCylinderOracle,
         ImmersedBodyInteractionOracle,
         NavierStokes2DOracle,
-        NavierStokes3DOracle,
         RodElementCentricGridOracle,
     )
+    from oracle.threaded import ThreadedNavierStokes3DOracle
     rt = real_t
-    Sim = NavierStokes2DOracle if wl.dim == 2 else NavierStokes3DOracle
+    # 3D: every sweep on z-slabs across the host cores, bitwise the serial oracle
+    Sim = NavierStokes2DOracle if wl.dim == 2 else ThreadedNavierStokes3DOracle
     sim = Sim(wl.grid, wl.x_range, wl.nu, cfl=wl.cfl, real_t=rt, with_forcing=True, with_free_stream_flow=True)
     sim.vorticity_field[...] = wl.initial_vorticity(rt)
     inters = []
@@ -1190,7 +1195,8 @@ def run_cpu_sample(wl, seconds, max_steps=None):
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     return {"value": round(n / el, 4), "unit": "flow steps/s", "cores": cores, "kind": "port",
             "sample": f"{n} coupled steps of the same workload ({wl.name}) after 1 warm-up step ({el:.1f} s), "
-                      "numpy + scipy.fft with workers = all cores, fp32"}
+                      + ("numpy sweeps on z-slabs across all cores, " if wl.dim == 3 else "numpy sweeps, ")
+                      + "scipy.fft with workers = all cores, fp32"}
 
 
 def run_reference(args, wl, rank, world):
