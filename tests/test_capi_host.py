@@ -63,6 +63,28 @@ def test_argument_validation_without_gpu(lib):
     assert lib.sg_ib_spread(0, 5, 1, 8, 8, 3, None, None, None, None, 0, None) == 1
 
 
+def test_argument_validation_of_the_operator_entries(lib):
+    """Each call fails a check that precedes every launch (the pointers are never dereferenced)."""
+    a, b, c = 16, 32, 48  # distinct non-null placeholders
+    assert lib.sg_elementwise(0, 9, 8, None, None, None, 0.0, 0.0, None) == 1  # unknown op
+    assert lib.sg_elementwise(0, 3, 8, a, None, c, 0.0, 0.0, None) == 1  # sum without a second input
+    assert lib.sg_elementwise(0, 2, -1, a, None, c, 0.0, 0.0, None) == 1  # negative count
+    assert lib.sg_set_boundary_zone(0, 4, 1, 8, 8, 1, None, 0.0, None) == 1  # dim
+    assert lib.sg_set_boundary_zone(0, 3, 8, 8, 8, 0, a, 0.0, None) == 1  # width 0
+    assert lib.sg_set_boundary_zone(0, 3, 0, 8, 8, 1, a, 0.0, None) == 2  # empty extent
+    assert lib.sg_set_boundary_zone(7, 3, 8, 8, 8, 1, a, 0.0, None) == 1  # dtype
+    assert lib.sg_diffusion_flux(0, 5, 8, 8, 8, a, b, 0.1, 1, None) == 1  # dim
+    assert lib.sg_diffusion_flux(7, 3, 8, 8, 8, a, b, 0.1, 1, None) == 1  # dtype
+    assert lib.sg_diffusion_flux(0, 3, 8, 8, 8, a, a, 0.1, 1, None) == 1  # aliasing
+    assert lib.sg_advection_eno3_flux_2d(0, 8, 8, a, b, None, 0.1, None) == 1  # no velocity
+    assert lib.sg_advection_eno3_flux_3d(0, 8, 8, 8, a, b, None, 0.1, None) == 1
+    assert lib.sg_advection_eno3_step_3d(0, 8, 8, 8, 0, a, b, c, 0.1, None) == 2  # no components
+    assert lib.sg_passive_transport_step(0, 2, 1, 8, 8, 3, a, b, c, 0.1, 0.1, None) == 4  # 2D vector
+    assert lib.sg_passive_transport_step(0, 3, 8, 8, 8, 2, a, b, c, 0.1, 0.1, None) == 1  # 2 components
+    assert lib.sg_passive_transport_step(0, 4, 8, 8, 8, 1, a, b, c, 0.1, 0.1, None) == 1  # dim
+    assert b"dim" in lib.sg_last_error()
+
+
 def _clamped_penalise(field, width, cx, cy, cz=None):
     """Penalisation as the fused kernels do it: gather from the clamped index, times factors."""
     def clamp(i, n):
