@@ -48,6 +48,11 @@ class ThreadedNavierStokes3DOracle(NavierStokes3DOracle):
     def _run(self, fn, ranges):
         return list(self._pool.map(fn, ranges))
 
+    def __del__(self):
+        pool = getattr(self, "_pool", None)
+        if pool is not None:
+            pool.shutdown(wait=False)
+
     # ------------------------------------------------------------ sweeps
 
     def _forcing_curl(self, w, f, prefactor):
@@ -156,6 +161,11 @@ class ThreadedPassiveTransportOracle(PassiveTransportOracle):
 
     def _run(self, fn, ranges):
         return list(self._pool.map(fn, ranges))
+
+    def __del__(self):
+        pool = getattr(self, "_pool", None)
+        if pool is not None:
+            pool.shutdown(wait=False)
 
     def _advect(self, field, inv_dx):
         u = self.velocity_field
