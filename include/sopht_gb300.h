@@ -462,6 +462,47 @@ int sg_ib_interp_adj(int dtype, int dim, int nz, int ny, int nx, int n_lag,
 int sg_lag_weighted_sum(int dtype, int dim, int n_lag, const void* lag_field,
                         const double* weights3, double* acc, void* stream);
 
+/* ------------------------------------------------------------ Cosserat rods
+ * A batch of rods with the same element count n, every array FP64 on the
+ * device and C-ordered with the rod index first: nodes (n_rods, 3, n+1),
+ * elements (n_rods, 3, n) or (n_rods, 3, 3, n) for matrices, Voronoi regions
+ * (n_rods, 3, n-1) or (n_rods, 3, 3, n-1).  Directors are rows d1, d2, d3 (a
+ * lab vector v has local components Q v); omega and external_torques are in
+ * the local frame.  This is the layout of pyelastica's CosseratRod
+ * (elastica/rod/cosserat_rod.py), which SophT couples through
+ * cosserat_rod_flow_interaction.py:9-58 and flow_forces.py:12-25. */
+typedef struct sg_rod_batch {
+    int n_rods, n_elems;
+    double* position;                     /* (n_rods, 3, n+1) */
+    double* velocity;                     /* (n_rods, 3, n+1) */
+    double* directors;                    /* (n_rods, 3, 3, n) */
+    double* omega;                        /* (n_rods, 3, n)   */
+    const double* mass;                   /* (n_rods, n+1)    */
+    const double* rest_lengths;           /* (n_rods, n)      */
+    const double* rest_voronoi_lengths;   /* (n_rods, n-1)    */
+    const double* shear_matrix;           /* (n_rods, 3, 3, n)   */
+    const double* bend_matrix;            /* (n_rods, 3, 3, n-1) */
+    const double* mass_second_moment;     /* (n_rods, 3, 3, n)   */
+    const double* inv_mass_second_moment; /* (n_rods, 3, 3, n)   */
+    const double* rest_sigma;             /* (n_rods, 3, n)   */
+    const double* rest_kappa;             /* (n_rods, 3, n-1) */
+    const double* external_forces;        /* (n_rods, 3, n+1) */
+    const double* external_torques;       /* (n_rods, 3, n)   */
+    const int* clamped;                   /* (n_rods) 1 = node 0 and element 0's directors fixed, or NULL */
+    const double* clamp_position;         /* (n_rods, 3)      */
+    const double* clamp_directors;        /* (n_rods, 3, 3)   */
+} sg_rod_batch;
+
+/* n_substeps position-Verlet steps of dt for every rod of the batch, in one
+ * launch (one CTA per rod): the discrete Cosserat model of Gazzola et al.
+ * (2018) that pyelastica's PositionVerlet stepper integrates
+ * (flow_past_rod_case.py:231-250 runs it rod_time_steps times per flow step).
+ * External loads stay fixed over the call; damping_rate > 0 multiplies
+ * velocities and angular velocities by exp(-damping_rate dt) each sub-step.
+ * 1 <= n_elems <= 1024.  The batch struct is read on the host. */
+int sg_rod_batch_step(const sg_rod_batch* batch, int n_substeps, double dt, double damping_rate,
+                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif

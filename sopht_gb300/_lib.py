@@ -49,6 +49,15 @@ class Batch2DMember(ctypes.Structure):
     ]
 
 
+class RodBatch(ctypes.Structure):
+    """Mirror of ``sg_rod_batch`` (device array pointers; read on the host)."""
+
+    _fields_ = [("n_rods", c_int), ("n_elems", c_int)] + [(name, c_void_p) for name in (
+        "position", "velocity", "directors", "omega", "mass", "rest_lengths", "rest_voronoi_lengths",
+        "shear_matrix", "bend_matrix", "mass_second_moment", "inv_mass_second_moment", "rest_sigma", "rest_kappa",
+        "external_forces", "external_torques", "clamped", "clamp_position", "clamp_directors")]
+
+
 _SIGNATURES = {
     "sg_last_error": (c_char_p, []),
     "sg_version": (c_int, []),
@@ -131,6 +140,7 @@ _SIGNATURES = {
     "sg_ib_interp_adj": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
     "sg_lag_weighted_sum": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_rod_batch_step": (c_int, [POINTER(RodBatch), c_int, c_double, c_double, c_void_p]),
     "sg_batch2d_create": (c_int, [c_int, POINTER(Batch2DMember), POINTER(c_void_p)]),
     "sg_batch2d_set_tuning": (c_int, [c_void_p, c_int, c_int, c_int]),
     "sg_batch2d_step": (c_int, [c_void_p, c_void_p]),

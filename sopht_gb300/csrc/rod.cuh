@@ -1,0 +1,281 @@
+// Discrete Cosserat rod dynamics, one position-Verlet sub-step split into passes over nodes,
+// elements and Voronoi regions (Gazzola, Dudte, McCormick & Mahadevan 2018, "Forward and inverse
+// problems in the mechanics of soft filaments", R. Soc. Open Sci. 5:171628: the model pyelastica
+// 0.3.3 implements and SophT couples its rods through).
+//
+// Every function here is __host__ __device__ and free of CUDA runtime calls: the batched kernel
+// (rod.cu) runs the passes with one CTA per rod and barriers between them, and a host driver
+// compiled from this same header runs them in sequence, which is how the arithmetic is checked
+// against the numpy model on a machine without a GPU.
+//
+// Per sub-step (h = dt / 2):  drift x += h v and rotate Q <- exp(-h [w]x) Q;  element pass
+// (tangent, dilatation e, strain sigma = e Q t - e3, stress n = S (sigma - sigma0), the lab force
+// Q^T n / e, the shear couple (Q t x n) l0, the transport term (J w / e) x w and the dilatation
+// term (J w / e^2) de/dt);  Voronoi pass (kappa = -log(Q_{k+1} Q_k^T) / D0, eps, m = B (kappa -
+// kappa0), m / eps^3 and (kappa x m) D0 / eps^3);  node update (force differences, v += dt a) and
+// element update (couple differences and averages, w += dt e J^-1 (couple + C_ext));  drift and
+// rotate again.  A clamped rod keeps node 0 and the directors of element 0 fixed.
+#pragma once
+
+#include <math.h>
+
+#include "../../include/sopht_gb300.h"
+
+#ifdef __CUDACC__
+#define SG_ROD_FN __host__ __device__ inline
+#else
+#define SG_ROD_FN inline
+#endif
+
+namespace sg {
+namespace rod {
+
+// One rod of a batch: its slices of the batch arrays (C order, as sg_rod_batch documents).
+struct View {
+    int n;
+    double* x;
+    double* v;
+    double* q;
+    double* w;
+    const double* mass;
+    const double* l0;
+    const double* d0;
+    const double* shear;
+    const double* bend;
+    const double* inertia;
+    const double* inv_inertia;
+    const double* sigma0;
+    const double* kappa0;
+    const double* f_ext;
+    const double* c_ext;
+    int clamped;
+    const double* clamp_x;
+    const double* clamp_q;
+};
+
+SG_ROD_FN View view_of(const sg_rod_batch& b, int r) {
+    const int n = b.n_elems;
+    const int64_t nn = n + 1, ne = n, nv = n - 1;
+    View v;
+    v.n = n;
+    v.x = b.position + r * 3 * nn;
+    v.v = b.velocity + r * 3 * nn;
+    v.q = b.directors + r * 9 * ne;
+    v.w = b.omega + r * 3 * ne;
+    v.mass = b.mass + r * nn;
+    v.l0 = b.rest_lengths + r * ne;
+    v.d0 = b.rest_voronoi_lengths + r * nv;
+    v.shear = b.shear_matrix + r * 9 * ne;
+    v.bend = b.bend_matrix + r * 9 * nv;
+    v.inertia = b.mass_second_moment + r * 9 * ne;
+    v.inv_inertia = b.inv_mass_second_moment + r * 9 * ne;
+    v.sigma0 = b.rest_sigma + r * 3 * ne;
+    v.kappa0 = b.rest_kappa + r * 3 * nv;
+    v.f_ext = b.external_forces + r * 3 * nn;
+    v.c_ext = b.external_torques + r * 3 * ne;
+    v.clamped = b.clamped ? b.clamped[r] : 0;
+    v.clamp_x = b.clamp_position + r * 3;
+    v.clamp_q = b.clamp_directors + r * 9;
+    return v;
+}
+
+// Work arrays of one rod (shared memory on the GPU): 16 n + 6 (n - 1) doubles.
+struct Scratch {
+    double* nlab;       // (3, n)  Q^T n / e
+    double* shear_c;    // (3, n)  (Q t x n) l0
+    double* transport;  // (3, n)  (J w / e) x w
+    double* dil_c;      // (3, n)  (J w / e^2) de/dt
+    double* e;          // (n)
+    double* len;        // (n)
+    double* bend_c;     // (3, n-1) m / eps^3
+    double* twist_c;    // (3, n-1) (kappa x m) D0 / eps^3
+};
+
+SG_ROD_FN int scratch_doubles(int n) { return 16 * n + 6 * (n > 1 ? n - 1 : 0); }
+
+SG_ROD_FN Scratch carve(double* base, int n) {
+    Scratch s;
+    const int nv = n > 1 ? n - 1 : 0;
+    s.nlab = base;
+    s.shear_c = s.nlab + 3 * n;
+    s.transport = s.shear_c + 3 * n;
+    s.dil_c = s.transport + 3 * n;
+    s.e = s.dil_c + 3 * n;
+    s.len = s.e + n;
+    s.bend_c = s.len + n;
+    s.twist_c = s.bend_c + 3 * nv;
+    return s;
+}
+
+// ---------------------------------------------------------------- rotations
+
+// exp([a]x) by Rodrigues' formula, row-major 3x3.
+SG_ROD_FN void rotation_exp(const double a[3], double r[9]) {
+    const double theta = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    const double safe = theta < 1e-12 ? 1.0 : theta;
+    const double k0 = a[0] / safe, k1 = a[1] / safe, k2 = a[2] / safe;
+    const double s = sin(theta), c1 = 1.0 - cos(theta);
+    const double kx[9] = {0.0, -k2, k1, k2, 0.0, -k0, -k1, k0, 0.0};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double k2ij = 0.0;
+            for (int m = 0; m < 3; ++m) k2ij += kx[i * 3 + m] * kx[m * 3 + j];
+            r[i * 3 + j] = (i == j ? 1.0 : 0.0) + s * kx[i * 3 + j] + c1 * k2ij;
+        }
+}
+
+// The rotation vector of r (angle below pi).
+SG_ROD_FN void rotation_log(const double r[9], double a[3]) {
+    double cosv = (r[0] + r[4] + r[8] - 1.0) / 2.0;
+    cosv = cosv < -1.0 ? -1.0 : (cosv > 1.0 ? 1.0 : cosv);
+    const double theta = acos(cosv);
+    const double s = sin(theta);
+    const double f = theta < 1e-6 ? 0.5 + theta * theta / 12.0 : theta / (2.0 * (s == 0.0 ? 1.0 : s));
+    a[0] = f * (r[7] - r[5]);
+    a[1] = f * (r[2] - r[6]);
+    a[2] = f * (r[3] - r[1]);
+}
+
+SG_ROD_FN void cross(const double a[3], const double b[3], double c[3]) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// m (3, 3, count) at column e times v.
+SG_ROD_FN void matvec(const double* m, int count, int e, const double v[3], double out[3]) {
+    for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc += m[(i * 3 + j) * count + e] * v[j];
+        out[i] = acc;
+    }
+}
+
+// --------------------------------------------------------------- the passes
+
+SG_ROD_FN void clamp_node0(View& r) {
+    for (int a = 0; a < 3; ++a) {
+        r.x[a * (r.n + 1)] = r.clamp_x[a];
+        r.v[a * (r.n + 1)] = 0.0;
+    }
+}
+
+SG_ROD_FN void clamp_element0(View& r) {
+    for (int a = 0; a < 9; ++a) r.q[a * r.n] = r.clamp_q[a];
+    for (int a = 0; a < 3; ++a) r.w[a * r.n] = 0.0;
+}
+
+SG_ROD_FN void drift_node(View& r, int i, double h) {
+    const int nn = r.n + 1;
+    for (int a = 0; a < 3; ++a) r.x[a * nn + i] += h * r.v[a * nn + i];
+    if (r.clamped && i == 0) clamp_node0(r);
+}
+
+SG_ROD_FN void rotate_element(View& r, int e, double h) {
+    const int n = r.n;
+    double a[3], rot[9], q[9];
+    for (int k = 0; k < 3; ++k) a[k] = -h * r.w[k * n + e];
+    rotation_exp(a, rot);
+    for (int k = 0; k < 9; ++k) q[k] = r.q[k * n + e];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int m = 0; m < 3; ++m) acc += rot[i * 3 + m] * q[m * 3 + j];
+            r.q[(i * 3 + j) * n + e] = acc;
+        }
+    if (r.clamped && e == 0) clamp_element0(r);
+}
+
+SG_ROD_FN void element_pass(const View& r, const Scratch& s, int e) {
+    const int n = r.n, nn = n + 1;
+    double d[3], t[3], qt[3], sig[3], stress[3];
+    for (int a = 0; a < 3; ++a) d[a] = r.x[a * nn + e + 1] - r.x[a * nn + e];
+    const double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for (int a = 0; a < 3; ++a) t[a] = d[a] / len;
+    const double dil = len / r.l0[e];
+    matvec(r.q, n, e, t, qt);
+    for (int a = 0; a < 3; ++a) sig[a] = dil * qt[a] - (a == 2 ? 1.0 : 0.0) - r.sigma0[a * n + e];
+    matvec(r.shear, n, e, sig, stress);
+    for (int a = 0; a < 3; ++a) {  // Q^T n / e
+        double acc = 0.0;
+        for (int b = 0; b < 3; ++b) acc += r.q[(b * 3 + a) * n + e] * stress[b];
+        s.nlab[a * n + e] = acc / dil;
+    }
+    double sc[3];
+    cross(qt, stress, sc);
+    for (int a = 0; a < 3; ++a) s.shear_c[a * n + e] = sc[a] * r.l0[e];
+    double w[3], jw[3], tr[3];
+    for (int a = 0; a < 3; ++a) w[a] = r.w[a * n + e];
+    matvec(r.inertia, n, e, w, jw);
+    cross(jw, w, tr);
+    double rate = 0.0;
+    for (int a = 0; a < 3; ++a) rate += t[a] * (r.v[a * nn + e + 1] - r.v[a * nn + e]);
+    rate /= r.l0[e];
+    for (int a = 0; a < 3; ++a) {
+        s.transport[a * n + e] = tr[a] / dil;
+        s.dil_c[a * n + e] = jw[a] / (dil * dil) * rate;
+    }
+    s.e[e] = dil;
+    s.len[e] = len;
+}
+
+SG_ROD_FN void voronoi_pass(const View& r, const Scratch& s, int k) {
+    const int n = r.n, nv = n - 1;
+    double rel[9], lg[3], kappa[3], m[3], km[3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {  // Q_{k+1} Q_k^T
+            double acc = 0.0;
+            for (int c = 0; c < 3; ++c) acc += r.q[(i * 3 + c) * n + k + 1] * r.q[(j * 3 + c) * n + k];
+            rel[i * 3 + j] = acc;
+        }
+    rotation_log(rel, lg);
+    for (int a = 0; a < 3; ++a) kappa[a] = -lg[a] / r.d0[k];
+    const double eps = 0.5 * (s.len[k + 1] + s.len[k]) / r.d0[k];
+    const double eps3 = eps * eps * eps;
+    double dk[3];
+    for (int a = 0; a < 3; ++a) dk[a] = kappa[a] - r.kappa0[a * nv + k];
+    matvec(r.bend, nv, k, dk, m);
+    cross(kappa, m, km);
+    for (int a = 0; a < 3; ++a) {
+        s.bend_c[a * nv + k] = m[a] / eps3;
+        s.twist_c[a * nv + k] = km[a] * r.d0[k] / eps3;
+    }
+}
+
+SG_ROD_FN void node_update(View& r, const Scratch& s, int i, double dt, double decay) {
+    const int n = r.n, nn = n + 1;
+    for (int a = 0; a < 3; ++a) {
+        double f = 0.0;
+        if (i < n) f += s.nlab[a * n + i];
+        if (i > 0) f -= s.nlab[a * n + i - 1];
+        r.v[a * nn + i] += dt * (f + r.f_ext[a * nn + i]) / r.mass[i];
+        r.v[a * nn + i] *= decay;
+    }
+    if (r.clamped && i == 0) clamp_node0(r);
+}
+
+SG_ROD_FN void element_update(View& r, const Scratch& s, int e, double dt, double decay) {
+    const int n = r.n, nv = n - 1;
+    double c[3];
+    for (int a = 0; a < 3; ++a) {
+        double acc = 0.0;
+        if (e < nv) acc += s.bend_c[a * nv + e];
+        if (e > 0) acc -= s.bend_c[a * nv + e - 1];
+        if (e < nv) acc += 0.5 * s.twist_c[a * nv + e];
+        if (e > 0) acc += 0.5 * s.twist_c[a * nv + e - 1];
+        acc += s.shear_c[a * n + e];
+        acc += s.transport[a * n + e];
+        acc += s.dil_c[a * n + e];
+        c[a] = acc + r.c_ext[a * n + e];
+    }
+    double alpha[3];
+    matvec(r.inv_inertia, n, e, c, alpha);
+    for (int a = 0; a < 3; ++a) {
+        r.w[a * n + e] += dt * s.e[e] * alpha[a];
+        r.w[a * n + e] *= decay;
+    }
+    if (r.clamped && e == 0) clamp_element0(r);
+}
+
+}  // namespace rod
+}  // namespace sg
