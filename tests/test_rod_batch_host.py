@@ -80,7 +80,7 @@ def _batch(rods):
 
     from sopht_gb300._lib import RodBatch
     b = RodBatch()
-    b.n_rods, b.n_elems = len(rods), N
+    b.n_rods, b.n_elems = len(rods), rods[0].n
     for field, attr in (("position", "position"), ("velocity", "velocity"), ("directors", "directors"),
                         ("omega", "omega"), ("mass", "mass"), ("rest_lengths", "rest_lengths"),
                         ("rest_voronoi_lengths", "rest_voronoi"), ("shear_matrix", "shear_matrix"),
@@ -116,3 +116,28 @@ def test_host_passes_match_the_rod_model(host_lib, damping):
     for r, rod in enumerate(rods):
         if rod.clamped is not None:
             np.testing.assert_array_equal(arrays["position"][r][:, 0], rod.clamped[0])
+
+
+@pytest.mark.parametrize("n", [1, 2])
+def test_host_passes_short_rods(host_lib, n):
+    """One element (no Voronoi region) and two elements (one), free and clamped."""
+    rng = np.random.default_rng(n)
+    rods = []
+    for clamp in (False, True):
+        rod = CosseratRod(n, start=[0.0, 0.0, 0.0], direction=[0.1, 0.0, 1.0], normal=[1.0, 0.0, 0.0],
+                          length=0.1 * n, radius=0.02, density=1.0, youngs_modulus=1e3)
+        rod.velocity = 0.05 * rng.standard_normal(rod.velocity.shape)
+        rod.omega = 0.5 * rng.standard_normal(rod.omega.shape)
+        rod.external_forces = 1e-4 * rng.standard_normal(rod.external_forces.shape)
+        if clamp:
+            rod.clamp_start()
+        rods.append(rod)
+    b, arrays = _batch(rods)
+    assert host_lib.rod_host_step(ctypes.byref(b), 200, 1e-5, 1.0) == 0
+    for r, rod in enumerate(rods):
+        for _ in range(200):
+            rod.step(1e-5)
+        for name, ref in (("position", rod.position), ("velocity", rod.velocity),
+                          ("directors", rod.directors), ("omega", rod.omega)):
+            scale = max(np.abs(ref).max(), 1e-30)
+            assert np.abs(arrays[name][r] - ref).max() <= 1e-10 * scale, (n, r, name)
