@@ -404,14 +404,24 @@ def gen_laplacian_filter_kernel_3d(filter_order, filter_flux_buffer, field_buffe
     return kernel
 
 
-def gen_divergence_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False):
-    """divergence_3d.py: central divergence with ghost ring zero."""
+def gen_divergence_pyst_kernel_3d(real_t, num_threads=False, fixed_grid_size=False, reset_ghost_zone=True):
+    """divergence_3d.py:13-98: central divergence on [1:-1]^3; the one-cell ring of the output is
+    set to 0 (``reset_ghost_zone``, the default) or left as it was."""
     real_t = normalize_real_t(real_t)
+    cache: dict = {}
 
     def kernel(divergence, field, inv_dx):
         _, nz, ny, nx = field.shape
-        _lib.call("sg_divergence_3d", sg_dtype(real_t), nz, ny, nx, ptr(field), ptr(divergence),
+        out = divergence
+        if not reset_ghost_zone:  # the kernel zeroes the ring: compute aside, keep the caller's ring
+            key = (tuple(divergence.shape), divergence.dtype, divergence.device)
+            out = cache.get(key)
+            if out is None:
+                out = cache[key] = torch.empty(divergence.shape, dtype=divergence.dtype, device=divergence.device)
+        _lib.call("sg_divergence_3d", sg_dtype(real_t), nz, ny, nx, ptr(field), ptr(out),
                   float(real_t(inv_dx)), stream_ptr(field.device))
+        if out is not divergence:
+            divergence[1:-1, 1:-1, 1:-1] = out[1:-1, 1:-1, 1:-1]
 
     return kernel
 

@@ -921,9 +921,44 @@ def validate_shims(ref_root: str, spne) -> None:
     print(f"shim validation: {checked} reference-test restatements agree")
 
 
+SIGNATURE_MODULES = ("sopht.simulator", "sopht.numeric.eulerian_grid_ops", "sopht.numeric.immersed_boundary_ops",
+                     "sopht.utils")
+
+
+def write_signatures() -> None:
+    """The parameter names and defaults of every public callable of the reference's API modules
+    (classes: their constructors), as ``reference_signatures.json``."""
+    import importlib
+    import inspect
+    import json
+    out = {}
+    for modname in SIGNATURE_MODULES:
+        mod = importlib.import_module(modname)
+        for name in sorted(getattr(mod, "__all__", [])):
+            obj = getattr(mod, name)
+            if not callable(obj):
+                continue
+            try:
+                sig = inspect.signature(obj.__init__ if inspect.isclass(obj) else obj)
+            except (TypeError, ValueError):
+                continue
+            params = []
+            for p in sig.parameters.values():
+                if p.name == "self" or p.kind in (p.VAR_POSITIONAL, p.VAR_KEYWORD):
+                    continue
+                default = None if p.default is inspect.Parameter.empty else repr(p.default)
+                params.append([p.name, default])
+            out[f"{modname}.{name}"] = params
+    path = HERE / "reference_signatures.json"
+    path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(f"{path.name}: {len(out)} callables")
+
+
 def main(ref_root: str = "/root/reference", *groups: str) -> None:
     """Validate the stand-ins, then write every group's fixtures (or only the named ``groups``)."""
     spne, spib, sps = _import_reference(ref_root)
+    if not groups or "signatures" in groups:
+        write_signatures()
     validate_shims(ref_root, spne)
     mods = {"spne": spne, "spib": spib, "sps": sps}
     for group, (modname, fn, seed) in GROUPS.items():
