@@ -292,6 +292,32 @@ class VirtualBoundaryForcing:
         self._interaction(eul_grid_velocity_field, lag_grid_position_field, lag_grid_velocity_field)
         self._spread(eul_grid_forcing_field, reset=True)
 
+    # The three elementwise steps of the feedback law as the reference exposes them
+    # (VirtualBoundaryForcing.py:132-185), in place on the first argument, for numpy arrays and
+    # tensors alike.  The interaction launch computes all three fused; these serve callers that
+    # compose the law themselves.
+
+    @staticmethod
+    def compute_lag_grid_velocity_mismatch_field(lag_grid_velocity_mismatch_field, lag_grid_flow_velocity_field,
+                                                 lag_grid_body_velocity_field):
+        """dU = U_flow - U_body."""
+        lag_grid_velocity_mismatch_field[...] = lag_grid_flow_velocity_field - lag_grid_body_velocity_field
+
+    @staticmethod
+    def update_lag_grid_position_mismatch_field_via_euler_forward(lag_grid_position_mismatch_field,
+                                                                  lag_grid_velocity_mismatch_field, dt):
+        """xi += dt * dU."""
+        lag_grid_position_mismatch_field[...] = (lag_grid_position_mismatch_field
+                                                 + dt * lag_grid_velocity_mismatch_field)
+
+    @staticmethod
+    def compute_lag_grid_forcing_field(lag_grid_forcing_field, lag_grid_position_mismatch_field,
+                                       lag_grid_velocity_mismatch_field, virtual_boundary_stiffness_coeff,
+                                       virtual_boundary_damping_coeff):
+        """F = K xi + C dU."""
+        lag_grid_forcing_field[...] = (virtual_boundary_stiffness_coeff * lag_grid_position_mismatch_field
+                                       + virtual_boundary_damping_coeff * lag_grid_velocity_mismatch_field)
+
     def time_step(self, dt):
         """VirtualBoundaryForcing.py:276-283: xi += dt * dU (deferred to the next interaction)."""
         self._flush_time_step()

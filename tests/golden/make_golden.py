@@ -925,9 +925,19 @@ SIGNATURE_MODULES = ("sopht.simulator", "sopht.numeric.eulerian_grid_ops", "soph
                      "sopht.utils")
 
 
+def _params(sig):
+    import inspect
+    params = []
+    for p in sig.parameters.values():
+        if p.name == "self" or p.kind in (p.VAR_POSITIONAL, p.VAR_KEYWORD):
+            continue
+        params.append([p.name, None if p.default is inspect.Parameter.empty else repr(p.default)])
+    return params
+
+
 def write_signatures() -> None:
     """The parameter names and defaults of every public callable of the reference's API modules
-    (classes: their constructors), as ``reference_signatures.json``."""
+    (classes: their constructors and public methods), as ``reference_signatures.json``."""
     import importlib
     import inspect
     import json
@@ -942,13 +952,15 @@ def write_signatures() -> None:
                 sig = inspect.signature(obj.__init__ if inspect.isclass(obj) else obj)
             except (TypeError, ValueError):
                 continue
-            params = []
-            for p in sig.parameters.values():
-                if p.name == "self" or p.kind in (p.VAR_POSITIONAL, p.VAR_KEYWORD):
-                    continue
-                default = None if p.default is inspect.Parameter.empty else repr(p.default)
-                params.append([p.name, default])
-            out[f"{modname}.{name}"] = params
+            out[f"{modname}.{name}"] = _params(sig)
+            if inspect.isclass(obj):  # and the public methods the class defines or inherits
+                for meth_name, meth in inspect.getmembers(obj, inspect.isfunction):
+                    if meth_name.startswith("_"):
+                        continue
+                    try:
+                        out[f"{modname}.{name}.{meth_name}"] = _params(inspect.signature(meth))
+                    except (TypeError, ValueError):
+                        continue
     path = HERE / "reference_signatures.json"
     path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
     print(f"{path.name}: {len(out)} callables")

@@ -75,3 +75,19 @@ def test_grid_deviation_error_l2_norm():
     inter, _ = _cylinder_interactor(16)
     inter.lag_grid_position_mismatch_field[...] = 2.0
     assert inter.get_grid_deviation_error_l2_norm() == pytest.approx(2.0 * np.sqrt(2))
+
+
+def test_feedback_law_helpers_in_place():
+    """VirtualBoundaryForcing's static helpers (VirtualBoundaryForcing.py:132-185) on host arrays."""
+    from sopht_gb300.numeric.immersed_boundary_ops import VirtualBoundaryForcing as vbf
+    rng = np.random.default_rng(4)
+    u_flow, u_body, xi = (rng.standard_normal((3, 7)).astype(np.float32) for _ in range(3))
+    du = np.empty_like(u_flow)
+    vbf.compute_lag_grid_velocity_mismatch_field(du, u_flow, u_body)
+    np.testing.assert_array_equal(du, u_flow - u_body)
+    xi0 = xi.copy()
+    vbf.update_lag_grid_position_mismatch_field_via_euler_forward(xi, du, 0.25)
+    np.testing.assert_array_equal(xi, xi0 + np.float32(0.25) * du)
+    f = np.empty_like(xi)
+    vbf.compute_lag_grid_forcing_field(f, xi, du, -3.0, -0.5)
+    np.testing.assert_array_equal(f, np.float32(-3.0) * xi + np.float32(-0.5) * du)
