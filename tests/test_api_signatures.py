@@ -100,3 +100,14 @@ def test_same_parameters_and_defaults(qualified):
     # the reference's positional order is kept for the parameters both have
     shared = [n for n in ref_names if n in positional]
     assert shared == [n for n in positional if n in shared], qualified
+
+
+def test_factory_functions_reject_unknown_flow_types_before_any_device_work():
+    """flow_simulators_{2,3}d.py: an unknown flow_type is a ValueError."""
+    import sopht_gb300.simulator as sps
+    with pytest.raises(ValueError, match="Invalid flow type given"):
+        sps.create_unbounded_flow_simulator_2d(grid_size=(8, 8), x_range=1.0, kinematic_viscosity=1e-3,
+                                               flow_type="passive_scalar")
+    with pytest.raises(ValueError, match="Invalid flow type given"):
+        sps.create_unbounded_flow_simulator_3d(grid_size=(8, 8, 8), x_range=1.0, kinematic_viscosity=1e-3,
+                                               flow_type="stokes")
