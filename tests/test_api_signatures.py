@@ -111,3 +111,39 @@ def test_factory_functions_reject_unknown_flow_types_before_any_device_work():
     with pytest.raises(ValueError, match="Invalid flow type given"):
         sps.create_unbounded_flow_simulator_3d(grid_size=(8, 8, 8), x_range=1.0, kinematic_viscosity=1e-3,
                                                flow_type="stokes")
+
+
+@pytest.mark.parametrize("cls,kwargs,message", [
+    ("PassiveTransportFlowSimulator", dict(grid_dim=3, grid_size=(8, 8, 8), field_type="tensor"),
+     "Invalid field type. Supported values include 'scalar' and 'vector'"),
+    ("PassiveTransportFlowSimulator", dict(grid_dim=2, grid_size=(8, 8), field_type="vector"),
+     "Passive transport of vector 2D fields not supported yet."),
+    ("PassiveTransportFlowSimulator", dict(grid_dim=4, grid_size=(8, 8)),
+     "Invalid grid dimensions. Supported values include 2 and 3."),
+    ("UnboundedNavierStokesFlowSimulator3D", dict(grid_size=(8, 8, 8), poisson_solver_type="fft"),
+     "Invalid Poisson solver type given"),
+    ("UnboundedNavierStokesFlowSimulator3D",
+     dict(grid_size=(8, 8, 8), filter_vorticity=True, filter_setting_dict={"order": 2, "type": "bogus"}),
+     "Invalid filter type"),
+])
+def test_constructor_errors_like_the_reference(cls, kwargs, message):
+    """The reference's argument errors (same type and message), raised before any device work."""
+    import sopht_gb300.simulator as sps
+    kw = dict(kinematic_viscosity=1e-3, x_range=1.0, **kwargs)
+    with pytest.raises(ValueError) as err:
+        getattr(sps, cls)(**kw)
+    assert str(err.value) == message
+
+
+@pytest.mark.parametrize("kwargs,message", [
+    (dict(grid_dim=4), "Invalid grid dimensions, must be either 2 or 3"),
+    (dict(grid_dim=2, interp_kernel_width=3), "Interpolation kernel inconsistent with interpolation kernel width!"),
+])
+def test_virtual_boundary_forcing_errors_like_the_reference(kwargs, message):
+    from sopht_gb300.numeric.immersed_boundary_ops import VirtualBoundaryForcing
+    import numpy as np
+    base = dict(virtual_boundary_stiffness_coeff=1.0, virtual_boundary_damping_coeff=1.0, dx=0.1, num_lag_nodes=3,
+                real_t=np.float32, **kwargs)
+    with pytest.raises(ValueError) as err:
+        VirtualBoundaryForcing(**base)
+    assert str(err.value) == message
