@@ -2,6 +2,7 @@
 
 from .adjoint import BodyForceObjective2D, time_integrated_body_force
 from .batch import BatchedFlowSimulator2D
+from .rods import CosseratRodBatch
 from .flow import (
     FlowSimulator,
     PassiveTransportFlowSimulator,
@@ -36,6 +37,7 @@ __all__ = [
     "BodyForceObjective2D",
     "CircularCylinderForcingGrid",
     "CosseratRodEdgeForcingGrid",
+    "CosseratRodBatch",
     "CosseratRodElementCentricForcingGrid",
     "CosseratRodFlowInteraction",
     "CosseratRodNodalForcingGrid",

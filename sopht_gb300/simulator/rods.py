@@ -1,0 +1,98 @@
+"""A batch of Cosserat rods advanced on the GPU (``sg_rod_batch_step``).
+
+The rods' state and material arrays are gathered once into FP64 device tensors
+with the rod index first (the ``sg_rod_batch`` layout), from rod objects with
+pyelastica's ``CosseratRod`` attribute names (``position_collection``,
+``velocity_collection``, ``director_collection``, ``omega_collection``,
+``mass``, ``rest_lengths``, ``rest_voronoi_lengths``, ``shear_matrix``,
+``bend_matrix``, ``mass_second_moment_of_inertia``,
+``inv_mass_second_moment_of_inertia``, ``rest_sigma``, ``rest_kappa``,
+``external_forces``, ``external_torques``).  ``step`` runs every sub-step of a
+call in one launch; ``upload_loads`` refreshes the external forces and torques
+(the flow forces change every sub-step in the coupled loop of
+flow_past_rod_case.py:231-250); ``download_into`` copies the state back.
+
+A clamped rod keeps node 0 and the directors of element 0 where they were when
+the batch was made (pyelastica's ``OneEndFixedBC`` at the start of the rod).
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..utils import default_device, stream_ptr
+
+STATE = ("position_collection", "velocity_collection", "director_collection", "omega_collection")
+MATERIAL = ("mass", "rest_lengths", "rest_voronoi_lengths", "shear_matrix", "bend_matrix",
+            "mass_second_moment_of_inertia", "inv_mass_second_moment_of_inertia", "rest_sigma", "rest_kappa")
+LOADS = ("external_forces", "external_torques")
+# sg_rod_batch field of each array
+_FIELD = {"position_collection": "position", "velocity_collection": "velocity", "director_collection": "directors",
+          "omega_collection": "omega", "mass": "mass", "rest_lengths": "rest_lengths",
+          "rest_voronoi_lengths": "rest_voronoi_lengths", "shear_matrix": "shear_matrix",
+          "bend_matrix": "bend_matrix", "mass_second_moment_of_inertia": "mass_second_moment",
+          "inv_mass_second_moment_of_inertia": "inv_mass_second_moment", "rest_sigma": "rest_sigma",
+          "rest_kappa": "rest_kappa", "external_forces": "external_forces", "external_torques": "external_torques"}
+
+
+class CosseratRodBatch:
+    """Rods of one element count, their arrays on ``device`` (FP64, rod index first)."""
+
+    def __init__(self, rods, clamped=None, device=None):
+        rods = list(rods)
+        if not rods:
+            raise ValueError("a rod batch needs at least one rod")
+        n = int(rods[0].n_elems)
+        if any(int(r.n_elems) != n for r in rods):
+            raise ValueError("every rod of a batch has the same number of elements")
+        if not 1 <= n <= 1024:
+            raise ValueError("rods of 1 to 1024 elements")
+        self.n_rods, self.n_elems = len(rods), n
+        self.device = torch.device(device) if device is not None else default_device()
+        self.arrays = {}
+        for name in STATE + MATERIAL + LOADS:
+            host = np.stack([np.asarray(getattr(r, name), dtype=np.float64) for r in rods])
+            self.arrays[name] = torch.from_numpy(np.ascontiguousarray(host)).to(self.device)
+        flags = [False] * len(rods) if clamped is None else [bool(c) for c in clamped]
+        if len(flags) != len(rods):
+            raise ValueError("one clamp flag per rod")
+        self.clamped = torch.tensor(flags, dtype=torch.int32, device=self.device)
+        self.clamp_position = self.arrays["position_collection"][:, :, 0].clone()
+        self.clamp_directors = self.arrays["director_collection"][..., 0].clone()
+        self._batch = self._struct()
+
+    def _struct(self):
+        b = _lib.RodBatch()
+        b.n_rods, b.n_elems = self.n_rods, self.n_elems
+        for name, t in self.arrays.items():
+            setattr(b, _FIELD[name], t.data_ptr())
+        b.clamped = self.clamped.data_ptr()
+        b.clamp_position = self.clamp_position.data_ptr()
+        b.clamp_directors = self.clamp_directors.data_ptr()
+        return b
+
+    def upload_loads(self, rods) -> None:
+        """Copy each rod's ``external_forces`` and ``external_torques`` to the device."""
+        for name in LOADS:
+            host = np.stack([np.asarray(getattr(r, name), dtype=np.float64) for r in rods])
+            self.arrays[name].copy_(torch.from_numpy(host))
+
+    def step(self, dt: float, n_substeps: int = 1, damping_rate: float = 0.0) -> None:
+        """``n_substeps`` position-Verlet steps of ``dt`` for every rod, in one launch on the
+        current stream; loads stay fixed over the call."""
+        if self.device.type != "cuda":
+            raise RuntimeError("CosseratRodBatch.step runs on a CUDA device; this batch lives on "
+                               f"{self.device}")
+        _lib.call("sg_rod_batch_step", ctypes.byref(self._batch), int(n_substeps), float(dt), float(damping_rate),
+                  stream_ptr(self.device))
+
+    def download_into(self, rods) -> None:
+        """Copy the batch's positions, velocities, directors and angular velocities into the rods."""
+        host = {name: self.arrays[name].cpu().numpy() for name in STATE}
+        for i, r in enumerate(rods):
+            for name in STATE:
+                getattr(r, name)[...] = host[name][i]

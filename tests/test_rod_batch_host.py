@@ -141,3 +141,45 @@ def test_host_passes_short_rods(host_lib, n):
                           ("directors", rod.directors), ("omega", rod.omega)):
             scale = max(np.abs(ref).max(), 1e-30)
             assert np.abs(arrays[name][r] - ref).max() <= 1e-10 * scale, (n, r, name)
+
+
+class _PyelasticaNamed:
+    """An oracle rod seen through pyelastica's CosseratRod attribute names."""
+
+    def __init__(self, rod):
+        self.n_elems = rod.n
+        self.position_collection, self.velocity_collection = rod.position, rod.velocity
+        self.director_collection, self.omega_collection = rod.directors, rod.omega
+        self.mass, self.rest_lengths, self.rest_voronoi_lengths = rod.mass, rod.rest_lengths, rod.rest_voronoi
+        self.shear_matrix, self.bend_matrix = rod.shear_matrix, rod.bend_matrix
+        self.mass_second_moment_of_inertia = rod.mass_second_moment
+        self.inv_mass_second_moment_of_inertia = rod.inv_mass_second_moment
+        self.rest_sigma, self.rest_kappa = rod.rest_sigma, rod.rest_kappa
+        self.external_forces, self.external_torques = rod.external_forces, rod.external_torques
+
+
+def test_rod_batch_layout_without_a_gpu():
+    """CosseratRodBatch gathers the rods into the sg_rod_batch layout (checked on CPU tensors; its
+    step needs a CUDA device and says so)."""
+    import sopht_gb300.simulator as sps
+    rods = _rods()
+    named = [_PyelasticaNamed(r) for r in rods]
+    batch = sps.CosseratRodBatch(named, clamped=[r.clamped is not None for r in rods], device="cpu")
+    assert (batch.n_rods, batch.n_elems) == (3, N)
+    for field in ("position", "velocity", "directors", "omega", "mass", "rest_lengths", "rest_voronoi_lengths",
+                  "shear_matrix", "bend_matrix", "mass_second_moment", "inv_mass_second_moment", "rest_sigma",
+                  "rest_kappa", "external_forces", "external_torques"):
+        assert getattr(batch._batch, field)  # a pointer into the batch's own tensors
+    np.testing.assert_array_equal(batch.arrays["director_collection"].numpy(), np.stack([r.directors for r in rods]))
+    np.testing.assert_array_equal(batch.clamped.numpy(), [1, 0, 1])
+    np.testing.assert_array_equal(batch.clamp_position.numpy()[0], rods[0].clamped[0])
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        batch.step(1e-5)
+    # the state goes back into the rods
+    for r in named:
+        r.velocity_collection[...] = 0.0
+    batch.download_into(named)
+    np.testing.assert_array_equal(named[2].velocity_collection, batch.arrays["velocity_collection"][2].numpy())
+    with pytest.raises(ValueError, match="same number of elements"):
+        sps.CosseratRodBatch([named[0], _PyelasticaNamed(CosseratRod(3, [0, 0, 0], [0, 0, 1], [1, 0, 0], 1.0,
+                                                                     0.1, 1.0, 1e3))], device="cpu")
