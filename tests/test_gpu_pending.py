@@ -1,0 +1,71 @@
+"""GPU checks of code that has not yet run on a GPU; each moves to its topic's module once it has.
+
+* the batched rod kernel against the numpy rod model: three rods (clamped and
+  free, bent, twisted, loaded) in one ``CosseratRodBatch``, 300 sub-steps in
+  one launch and again one launch per sub-step with damping, compared with
+  ``oracle.rod.CosseratRod`` at 1e-10 of scale (FP64; the host run of the same
+  passes agrees to 8e-14);
+* ``gen_divergence_pyst_kernel_3d(reset_ghost_zone=False)`` keeps the output's
+  ring and writes the same interior as the default.
+
+The module waits for ``SOPHT_GB300_PENDING_GPU=1``, set by whoever runs these
+first, so that a suite run elsewhere does not stop on them.
+"""
+
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("SOPHT_GB300_PENDING_GPU") != "1",
+                                 reason="first GPU run not yet made (set SOPHT_GB300_PENDING_GPU=1)")]
+
+
+@pytest.mark.parametrize("per_call,damping", [(300, 0.0), (1, 3.0)])
+def test_rod_batch_on_gpu_matches_the_rod_model(per_call, damping):
+    import torch
+
+    import sopht_gb300.simulator as sps
+    from sopht_gb300 import _lib
+    from sopht_gb300.build import build
+    from test_rod_batch_host import _PyelasticaNamed, _rods
+    build()
+    _lib.load()
+    rods = _rods()
+    batch = sps.CosseratRodBatch([_PyelasticaNamed(r) for r in rods], clamped=[r.clamped is not None for r in rods])
+    dt, steps = 2e-5, 300
+    for _ in range(steps // per_call):
+        batch.step(dt, n_substeps=per_call, damping_rate=damping)
+    torch.cuda.synchronize()
+    for i, rod in enumerate(rods):
+        rod.damping_rate = damping
+        for _ in range(steps):
+            rod.step(dt)
+        for name, ref in (("position_collection", rod.position), ("velocity_collection", rod.velocity),
+                          ("director_collection", rod.directors), ("omega_collection", rod.omega)):
+            got = batch.arrays[name][i].cpu().numpy()
+            assert np.abs(got - ref).max() <= 1e-10 * max(np.abs(ref).max(), 1e-30), (i, name)
+
+
+def test_divergence_keeps_the_ring_without_reset():
+    import torch
+
+    import sopht_gb300.numeric.eulerian_grid_ops as ops
+    from sopht_gb300 import _lib
+    from sopht_gb300.build import build
+    build()
+    _lib.load()
+    field = torch.from_numpy(np.random.default_rng(1).standard_normal((3, 9, 10, 11))).cuda()
+    reset = torch.empty((9, 10, 11), dtype=torch.float64, device="cuda")
+    ops.gen_divergence_pyst_kernel_3d(np.float64)(divergence=reset, field=field, inv_dx=2.0)
+    kept = torch.full((9, 10, 11), 7.0, dtype=torch.float64, device="cuda")
+    ops.gen_divergence_pyst_kernel_3d(np.float64, reset_ghost_zone=False)(divergence=kept, field=field, inv_dx=2.0)
+    torch.cuda.synchronize()
+    r, k = reset.cpu().numpy(), kept.cpu().numpy()
+    np.testing.assert_array_equal(k[1:-1, 1:-1, 1:-1], r[1:-1, 1:-1, 1:-1])
+    ring = np.ones_like(k, dtype=bool)
+    ring[1:-1, 1:-1, 1:-1] = False
+    assert (k[ring] == 7.0).all() and (r[ring] == 0.0).all()
