@@ -52,6 +52,12 @@ def test_library_exports_every_declared_symbol(lib):
     assert lib.sg_version() >= 100
 
 
+def test_integration_notes_name_every_entry():
+    """Each function the header declares has its row (reference interface or reason) in INTEGRATION.md."""
+    doc = (REPO / "INTEGRATION.md").read_text()
+    assert not [s for s in sorted(_header_symbols()) if s not in doc]
+
+
 def test_argument_validation_without_gpu(lib):
     plan = ctypes.c_void_p()
     assert lib.sg_poisson_plan_create(4, 8, 8, 8, 1.0, 0, 1, ctypes.byref(plan)) == 1
