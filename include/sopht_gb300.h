@@ -62,6 +62,8 @@ typedef struct sg_step_scalars {
 } sg_step_scalars;
 
 /* ---------------------------------------------------------------- general */
+/* No reference counterpart: the calling thread's message for its last failed
+ * call, and the library version (major * 100 + minor). */
 const char* sg_last_error(void);
 int sg_version(void);
 
