@@ -488,8 +488,8 @@ typedef struct sg_rod_batch {
     const double* inv_mass_second_moment; /* (n_rods, 3, 3, n)   */
     const double* rest_sigma;             /* (n_rods, 3, n)   */
     const double* rest_kappa;             /* (n_rods, 3, n-1) */
-    const double* external_forces;        /* (n_rods, 3, n+1) */
-    const double* external_torques;       /* (n_rods, 3, n)   */
+    double* external_forces;              /* (n_rods, 3, n+1) */
+    double* external_torques;             /* (n_rods, 3, n)   */
     const int* clamped;                   /* (n_rods) 1 = node 0 and element 0's directors fixed, or NULL */
     const double* clamp_position;         /* (n_rods, 3)      */
     const double* clamp_directors;        /* (n_rods, 3, 3)   */
@@ -504,6 +504,21 @@ typedef struct sg_rod_batch {
  * 1 <= n_elems <= 1024.  The batch struct is read on the host. */
 int sg_rod_batch_step(const sg_rod_batch* batch, int n_substeps, double dt, double damping_rate,
                       void* stream);
+/* The element-centric forcing grid of every rod of the batch at once
+ * (cosserat_rod_forcing_grids.py:82-130), in the marker layout of one
+ * VirtualBoundaryForcing over the batch: (dim, n_rods * n), marker r * n + e.
+ * sg_rod_batch_element_markers writes the markers' positions (the element
+ * centres) and velocities (the mass-weighted mean of the two nodes), float64
+ * device arrays; sg_rod_batch_element_loads turns the Lagrangian forcing of
+ * those markers (dtype SG_F32 or SG_F64) into each rod's external_forces (the
+ * reaction -F/2 on both nodes of an element, components past dim 0) and sets
+ * external_torques to 0, as transfer_forcing_from_grid_to_body and
+ * FlowForces.apply_forces (flow_forces.py:22-25) do for a rod whose only load
+ * is the flow. */
+int sg_rod_batch_element_markers(const sg_rod_batch* batch, int dim, double* position, double* velocity,
+                                 void* stream);
+int sg_rod_batch_element_loads(const sg_rod_batch* batch, int dim, int dtype, const void* lag_forcing,
+                               void* stream);
 
 #ifdef __cplusplus
 }

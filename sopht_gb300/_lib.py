@@ -141,6 +141,8 @@ _SIGNATURES = {
                                  c_void_p]),
     "sg_lag_weighted_sum": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "sg_rod_batch_step": (c_int, [POINTER(RodBatch), c_int, c_double, c_double, c_void_p]),
+    "sg_rod_batch_element_markers": (c_int, [POINTER(RodBatch), c_int, c_void_p, c_void_p, c_void_p]),
+    "sg_rod_batch_element_loads": (c_int, [POINTER(RodBatch), c_int, c_int, c_void_p, c_void_p]),
     "sg_batch2d_create": (c_int, [c_int, POINTER(Batch2DMember), POINTER(c_void_p)]),
     "sg_batch2d_set_tuning": (c_int, [c_void_p, c_int, c_int, c_int]),
     "sg_batch2d_step": (c_int, [c_void_p, c_void_p]),

@@ -277,5 +277,38 @@ SG_ROD_FN void element_update(View& r, const Scratch& s, int e, double dt, doubl
     if (r.clamped && e == 0) clamp_element0(r);
 }
 
+// ------------------------------------------- the element-centric forcing grid of a batch
+// cosserat_rod_forcing_grids.py:82-130 for every rod at once, in the marker layout of one
+// VirtualBoundaryForcing over the whole batch: (dim, n_rods * n), marker r * n + e.
+
+// Marker (r, e): position (x_e + x_{e+1}) / 2 and the mass-weighted velocity of its two nodes.
+SG_ROD_FN void element_marker(const View& r, int rod, int e, int dim, int64_t n_markers, double* pos,
+                              double* vel) {
+    const int n = r.n, nn = n + 1;
+    const int64_t m = (int64_t)rod * n + e;
+    const double m0 = r.mass[e], m1 = r.mass[e + 1];
+    for (int d = 0; d < dim; ++d) {
+        pos[d * n_markers + m] = (r.x[d * nn + e + 1] + r.x[d * nn + e]) / 2.0;
+        vel[d * n_markers + m] = (m1 * r.v[d * nn + e + 1] + m0 * r.v[d * nn + e]) / (m1 + m0);
+    }
+}
+
+// Node i of rod `rod`: the reaction -F/2 of each neighbouring element's marker (the element
+// before first), into external_forces (components past dim are 0), external_torques 0.
+template <typename F>
+SG_ROD_FN void element_reaction(View& r, int rod, int i, int dim, int64_t n_markers, const F* forcing,
+                                double* f_ext, double* c_ext) {
+    const int n = r.n, nn = n + 1;
+    for (int d = 0; d < 3; ++d) {
+        double f = 0.0;
+        if (d < dim) {
+            if (i > 0) f -= 0.5 * (double)forcing[d * n_markers + (int64_t)rod * n + i - 1];
+            if (i < n) f -= 0.5 * (double)forcing[d * n_markers + (int64_t)rod * n + i];
+        }
+        f_ext[d * nn + i] = f;
+        if (i < n) c_ext[d * n + i] = 0.0;
+    }
+}
+
 }  // namespace rod
 }  // namespace sg

@@ -10,7 +10,10 @@ pyelastica's ``CosseratRod`` attribute names (``position_collection``,
 ``external_forces``, ``external_torques``).  ``step`` runs every sub-step of a
 call in one launch; ``upload_loads`` refreshes the external forces and torques
 (the flow forces change every sub-step in the coupled loop of
-flow_past_rod_case.py:231-250); ``download_into`` copies the state back.
+flow_past_rod_case.py:231-250); ``element_markers`` and ``set_element_loads``
+are the element-centric forcing grid of the whole batch on the device (markers
+laid out for one VirtualBoundaryForcing over the batch, reaction loads read
+back from its forcing); ``download_into`` copies the state back.
 
 A clamped rod keeps node 0 and the directors of element 0 where they were when
 the batch was made (pyelastica's ``OneEndFixedBC`` at the start of the rod).
@@ -84,11 +87,31 @@ class CosseratRodBatch:
     def step(self, dt: float, n_substeps: int = 1, damping_rate: float = 0.0) -> None:
         """``n_substeps`` position-Verlet steps of ``dt`` for every rod, in one launch on the
         current stream; loads stay fixed over the call."""
-        if self.device.type != "cuda":
-            raise RuntimeError("CosseratRodBatch.step runs on a CUDA device; this batch lives on "
-                               f"{self.device}")
+        self._require_cuda()
         _lib.call("sg_rod_batch_step", ctypes.byref(self._batch), int(n_substeps), float(dt), float(damping_rate),
                   stream_ptr(self.device))
+
+    def element_markers(self, position, velocity, dim: int = 3) -> None:
+        """The element-centric markers of every rod into ``position`` and ``velocity``, float64 CUDA
+        tensors (dim, n_rods * n_elems) (marker r * n + e): one launch, on the current stream."""
+        self._require_cuda(position, velocity)
+        _lib.call("sg_rod_batch_element_markers", ctypes.byref(self._batch), int(dim), position.data_ptr(),
+                  velocity.data_ptr(), stream_ptr(self.device))
+
+    def set_element_loads(self, lag_forcing, dim: int = 3) -> None:
+        """Each rod's external forces from the Lagrangian forcing of its element markers (the
+        reaction, half on each node) and its external torques zeroed: one launch."""
+        self._require_cuda(lag_forcing)
+        dtype = _lib.SG_F32 if lag_forcing.dtype == torch.float32 else _lib.SG_F64
+        _lib.call("sg_rod_batch_element_loads", ctypes.byref(self._batch), int(dim), dtype, lag_forcing.data_ptr(),
+                  stream_ptr(self.device))
+
+    def _require_cuda(self, *tensors):
+        if self.device.type != "cuda":
+            raise RuntimeError(f"CosseratRodBatch runs on a CUDA device; this batch lives on {self.device}")
+        for t in tensors:
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous()):
+                raise ValueError("marker arrays must be C-contiguous CUDA tensors")
 
     def download_into(self, rods) -> None:
         """Copy the batch's positions, velocities, directors and angular velocities into the rods."""

@@ -27,3 +27,27 @@ extern "C" int rod_host_step(const sg_rod_batch* b, int n_substeps, double dt, d
     }
     return 0;
 }
+
+// The element-centric markers and reaction loads of the batch, in the kernels' order.
+extern "C" int rod_host_markers(const sg_rod_batch* b, int dim, double* pos, double* vel) {
+    using namespace sg::rod;
+    const int64_t total = (int64_t)b->n_rods * b->n_elems;
+    for (int r = 0; r < b->n_rods; ++r) {
+        const View v = view_of(*b, r);
+        for (int e = 0; e < b->n_elems; ++e) element_marker(v, r, e, dim, total, pos, vel);
+    }
+    return 0;
+}
+
+extern "C" int rod_host_loads(const sg_rod_batch* b, int dim, const double* forcing) {
+    using namespace sg::rod;
+    const int n = b->n_elems, nn = n + 1;
+    const int64_t n_markers = (int64_t)b->n_rods * n;
+    for (int r = 0; r < b->n_rods; ++r) {
+        View v = view_of(*b, r);
+        for (int i = 0; i <= n; ++i)
+            element_reaction(v, r, i, dim, n_markers, forcing, b->external_forces + (int64_t)r * 3 * nn,
+                             b->external_torques + (int64_t)r * 3 * n);
+    }
+    return 0;
+}

@@ -5,6 +5,8 @@
   one launch and again one launch per sub-step with damping, compared with
   ``oracle.rod.CosseratRod`` at 1e-10 of scale (FP64; the host run of the same
   passes agrees to 8e-14);
+* the batch's element-centric markers and reaction loads on the device,
+  bitwise the forcing grid's numpy formulas;
 * ``gen_divergence_pyst_kernel_3d(reset_ghost_zone=False)`` keeps the output's
   ring and writes the same interior as the default.
 
@@ -69,3 +71,36 @@ def test_divergence_keeps_the_ring_without_reset():
     ring = np.ones_like(k, dtype=bool)
     ring[1:-1, 1:-1, 1:-1] = False
     assert (k[ring] == 7.0).all() and (r[ring] == 0.0).all()
+
+
+@pytest.mark.parametrize("dim,dtype", [(3, "float64"), (2, "float32")])
+def test_rod_batch_element_markers_and_loads_on_gpu(dim, dtype):
+    import torch
+
+    import sopht_gb300.simulator as sps
+    from sopht_gb300 import _lib
+    from sopht_gb300.build import build
+    from sopht_gb300.simulator.immersed_body import _node_to_element_velocity
+    from test_rod_batch_host import N, _PyelasticaNamed, _rods
+    build()
+    _lib.load()
+    rods = _rods()
+    batch = sps.CosseratRodBatch([_PyelasticaNamed(r) for r in rods])
+    m = len(rods) * N
+    pos = torch.zeros((dim, m), dtype=torch.float64, device="cuda")
+    vel = torch.zeros_like(pos)
+    batch.element_markers(pos, vel, dim=dim)
+    forcing = torch.from_numpy(np.random.default_rng(7).standard_normal((dim, m)).astype(dtype)).cuda()
+    batch.set_element_loads(forcing, dim=dim)
+    torch.cuda.synchronize()
+    f_host = forcing.cpu().numpy().astype(np.float64)
+    for r, rod in enumerate(rods):
+        p = rod.position
+        np.testing.assert_array_equal(pos.cpu().numpy()[:, r * N:(r + 1) * N], (p[:dim, 1:] + p[:dim, :-1]) / 2.0)
+        np.testing.assert_array_equal(vel.cpu().numpy()[:, r * N:(r + 1) * N],
+                                      _node_to_element_velocity(rod.mass, rod.velocity)[:dim])
+        ref = np.zeros((3, N + 1))
+        ref[:dim, 1:] -= 0.5 * f_host[:, r * N:(r + 1) * N]
+        ref[:dim, :-1] -= 0.5 * f_host[:, r * N:(r + 1) * N]
+        np.testing.assert_array_equal(batch.arrays["external_forces"][r].cpu().numpy(), ref)
+        assert not batch.arrays["external_torques"][r].cpu().numpy().any()

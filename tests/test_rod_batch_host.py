@@ -41,6 +41,8 @@ def host_lib(tmp_path_factory):
     from sopht_gb300._lib import RodBatch
     lib.rod_host_step.argtypes = [ctypes.POINTER(RodBatch), ctypes.c_int, ctypes.c_double, ctypes.c_double]
     lib.rod_host_step.restype = ctypes.c_int
+    lib.rod_host_markers.argtypes = [ctypes.POINTER(RodBatch), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.rod_host_loads.argtypes = [ctypes.POINTER(RodBatch), ctypes.c_int, ctypes.c_void_p]
     return lib
 
 
@@ -183,3 +185,29 @@ def test_rod_batch_layout_without_a_gpu():
     with pytest.raises(ValueError, match="same number of elements"):
         sps.CosseratRodBatch([named[0], _PyelasticaNamed(CosseratRod(3, [0, 0, 0], [0, 0, 1], [1, 0, 0], 1.0,
                                                                      0.1, 1.0, 1e3))], device="cpu")
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_host_element_markers_and_loads_match_the_forcing_grid(host_lib, dim):
+    """The batch's element-centric markers and reaction loads (rod.cuh) against the forcing grid's
+    numpy formulas (cosserat_rod_forcing_grids.py:82-130), bitwise."""
+    from sopht_gb300.simulator.immersed_body import _node_to_element_velocity
+    rods = _rods()
+    b, arrays = _batch(rods)
+    n_markers = len(rods) * N
+    pos, vel = np.zeros((dim, n_markers)), np.zeros((dim, n_markers))
+    assert host_lib.rod_host_markers(ctypes.byref(b), dim, pos.ctypes.data, vel.ctypes.data) == 0
+    for r, rod in enumerate(rods):
+        p = rod.position
+        np.testing.assert_array_equal(pos[:, r * N:(r + 1) * N], ((p[:dim, 1:] + p[:dim, :-1]) / 2.0))
+        np.testing.assert_array_equal(vel[:, r * N:(r + 1) * N],
+                                      _node_to_element_velocity(rod.mass, rod.velocity)[:dim])
+    forcing = np.random.default_rng(7).standard_normal((dim, n_markers))
+    assert host_lib.rod_host_loads(ctypes.byref(b), dim, forcing.ctypes.data) == 0
+    for r in range(len(rods)):
+        f = forcing[:, r * N:(r + 1) * N]
+        ref = np.zeros((3, N + 1))
+        ref[:dim, 1:] -= 0.5 * f
+        ref[:dim, :-1] -= 0.5 * f
+        np.testing.assert_array_equal(arrays["external_forces"][r], ref)
+        assert not arrays["external_torques"][r].any()
