@@ -89,6 +89,22 @@ def test_argument_validation_of_the_operator_entries(lib):
     assert lib.sg_passive_transport_step(0, 3, 8, 8, 8, 2, a, b, c, 0.1, 0.1, None) == 1  # 2 components
     assert lib.sg_passive_transport_step(0, 4, 8, 8, 8, 1, a, b, c, 0.1, 0.1, None) == 1  # dim
     assert b"dim" in lib.sg_last_error()
+    # the rod batch entries
+    from sopht_gb300._lib import RodBatch
+    rb = RodBatch()
+    assert lib.sg_rod_batch_step(None, 1, 1e-5, 0.0, None) == 1
+    rb.n_rods, rb.n_elems = 2, 0
+    assert lib.sg_rod_batch_step(ctypes.byref(rb), 1, 1e-5, 0.0, None) == 2  # no elements
+    rb.n_elems = 2000
+    assert lib.sg_rod_batch_step(ctypes.byref(rb), 1, 1e-5, 0.0, None) == 2  # above 1024 elements
+    rb.n_elems = 8
+    assert lib.sg_rod_batch_step(ctypes.byref(rb), 1, 1e-5, 0.0, None) == 1  # null arrays
+    for field in ("position", "velocity", "mass", "external_forces", "external_torques"):
+        setattr(rb, field, a)
+    assert lib.sg_rod_batch_element_markers(ctypes.byref(rb), 4, b, c, None) == 1  # dim
+    assert lib.sg_rod_batch_element_markers(ctypes.byref(rb), 3, None, c, None) == 1  # no output
+    assert lib.sg_rod_batch_element_loads(ctypes.byref(rb), 3, 7, b, None) == 1  # dtype
+    assert lib.sg_rod_batch_element_loads(ctypes.byref(rb), 2, 0, None, None) == 1  # no forcing
 
 
 def _clamped_penalise(field, width, cx, cy, cz=None):
