@@ -50,15 +50,15 @@ template <typename C> __host__ __device__ __forceinline__ C cmake(decltype(C::x)
     c.y = im;
     return c;
 }
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return cmake<C>(a.x + b.x, a.y + b.y); }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) { return cmake<C>(a.x - b.x, a.y - b.y); }
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cmake<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cmake<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
     return cmake<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-template <typename C> __device__ __forceinline__ C cconj(C a) { return cmake<C>(a.x, -a.y); }
-template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { return cmake<C>(a.x * s, a.y * s); }
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) { return cmake<C>(a.x, -a.y); }
+template <typename C, typename T> __host__ __device__ __forceinline__ C cscale(C a, T s) { return cmake<C>(a.x * s, a.y * s); }
 // multiply by (0 + i*s): i*(x + i y) = -y + i x
-template <typename C> __device__ __forceinline__ C cmul_i(C a) { return cmake<C>(-a.y, a.x); }
+template <typename C> __host__ __device__ __forceinline__ C cmul_i(C a) { return cmake<C>(-a.y, a.x); }
 
 inline int dtype_size(int dtype) { return dtype == SG_F64 ? 8 : 4; }
 

@@ -55,7 +55,7 @@ template <typename C> struct Cx {
     using T = decltype(C::x);
 };
 
-template <bool INV, typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
+template <bool INV, typename C> __host__ __device__ __forceinline__ void dft2(C& a, C& b) {
     C t = a;
     a = cadd(t, b);
     b = csub(t, b);
@@ -75,7 +75,7 @@ template <bool INV, typename C> __device__ __forceinline__ void dft3(C& a, C& b,
     c = csub(m, r);
 }
 
-template <bool INV, typename C> __device__ __forceinline__ void dft4(C& v0, C& v1, C& v2, C& v3) {
+template <bool INV, typename C> __host__ __device__ __forceinline__ void dft4(C& v0, C& v1, C& v2, C& v3) {
     C a = cadd(v0, v2), b = csub(v0, v2), c = cadd(v1, v3), e = csub(v1, v3);
     // forward: d = -i * e ; inverse: d = +i * e
     C d = INV ? cmake<C>(-e.y, e.x) : cmake<C>(e.y, -e.x);
@@ -153,7 +153,7 @@ __host__ __device__ constexpr double w16_sin(int m) {
 // 16-point DFT as 4 x 4: DFT-4 over n1 for each n2 (input n = 4 n1 + n2), the
 // twiddles w16^(n2 k1), then DFT-4 over n2 (output k = k1 + 4 k2).  HALF_IN:
 // inputs 8..15 are zero and the first DFT-4s skip them.
-template <bool INV, bool HALF_IN = false, typename C> __device__ __forceinline__ void dft16(C* v) {
+template <bool INV, bool HALF_IN = false, typename C> __host__ __device__ __forceinline__ void dft16(C* v) {
     using T = typename Cx<C>::T;
     C y[4][4];
 #pragma unroll

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "poisson.cuh"
+#include "fft_reg.cuh"
 
 namespace sg {
 
@@ -251,11 +252,58 @@ int poisson_spectral_passes(sg_poisson_plan_s* p, int ncomp, cudaStream_t stream
     return SG_OK;
 }
 
+// fp32 y and z passes of lengths 256 and 512 on the register line kernels (fft_reg.cuh): y lines
+// are slabs of nx + 1 adjacent lines per (component, z plane), z lines one slab of 2 ny (nx + 1)
+// lines per component.  Returns SG_ERR_UNSUPPORTED for the other lengths.
+static int reg_pass3d(sg_poisson_plan_s* p, int ncomp, int pass, cudaStream_t stream) {
+    float2* spec = reinterpret_cast<float2*>(p->spec);
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    RegLinesParams r{};
+    r.in = spec;
+    r.out = spec;
+    if (pass == 1) {
+        const int64_t plane = (int64_t)2 * ny * (nx + 1);
+        SG_REQUIRE((int64_t)ncomp * plane < (1LL << 31), SG_ERR_SHAPE, "z pass: too many lines");
+        r.n_lines = (int)(ncomp * plane);
+        r.slab_lines = (int)plane;
+        r.slab_stride = p->spec_comp_elems;
+        r.stride = plane;
+        r.n_in = nz;
+        r.n_out = nz;
+        r.tw = (const float2*)p->tw_z;
+        r.g = (const float*)p->greens;
+        r.g_kstride = (int64_t)(ny + 1) * (nx + 1);
+        r.g_mstride = nx + 1;
+        r.g_div = nx + 1;
+        r.g_mmod = 2 * ny;
+        return launch_reg_lines<RL_CONV>(r, 2 * nz, stream);
+    }
+    SG_REQUIRE((int64_t)ncomp * nz * (nx + 1) < (1LL << 31), SG_ERR_SHAPE, "y pass: too many lines");
+    r.n_lines = ncomp * nz * (nx + 1);
+    r.slab_lines = nx + 1;
+    r.slab_stride = (int64_t)2 * ny * (nx + 1);
+    r.stride = nx + 1;
+    r.tw = (const float2*)p->tw_y;
+    if (pass == 0) {
+        r.n_in = ny;
+        r.n_out = 2 * ny;
+        return launch_reg_lines<RL_FWD>(r, 2 * ny, stream);
+    }
+    r.n_in = 2 * ny;
+    r.n_out = ny;
+    return launch_reg_lines<RL_INV>(r, 2 * ny, stream);
+}
+
+static bool reg_length(int n) { return n == 256 || n == 512; }
+
 template <typename T>
 int poisson_spectral_pass3d(sg_poisson_plan_s* p, int ncomp, int pass, cudaStream_t stream) {
     using C = cplx_t<T>;
     C* spec = reinterpret_cast<C*>(p->spec);
     const int nx = p->nx, ny = p->ny, nz = p->nz;
+    if constexpr (sizeof(T) == 4) {
+        if (reg_length(pass == 1 ? 2 * nz : 2 * ny)) return reg_pass3d(p, ncomp, pass, stream);
+    }
     // y lines: forward (Ny non-zero points -> 2 Ny bins) or inverse (keep Ny)
     LinesParams<T> ly{};
     ly.in = spec;

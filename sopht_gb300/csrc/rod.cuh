@@ -282,6 +282,23 @@ SG_ROD_FN void element_update(View& r, const Scratch& s, int e, double dt, doubl
 // VirtualBoundaryForcing over the whole batch: (dim, n_rods * n), marker r * n + e.
 
 // Marker (r, e): position (x_e + x_{e+1}) / 2 and the mass-weighted velocity of its two nodes.
+// Separately rounded product and sum: device code would otherwise contract a * b + c into one
+// fused multiply-add, which rounds once where numpy rounds twice.
+SG_ROD_FN double mul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+SG_ROD_FN double add_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+
 SG_ROD_FN void element_marker(const View& r, int rod, int e, int dim, int64_t n_markers, double* pos,
                               double* vel) {
     const int n = r.n, nn = n + 1;
@@ -289,7 +306,8 @@ SG_ROD_FN void element_marker(const View& r, int rod, int e, int dim, int64_t n_
     const double m0 = r.mass[e], m1 = r.mass[e + 1];
     for (int d = 0; d < dim; ++d) {
         pos[d * n_markers + m] = (r.x[d * nn + e + 1] + r.x[d * nn + e]) / 2.0;
-        vel[d * n_markers + m] = (m1 * r.v[d * nn + e + 1] + m0 * r.v[d * nn + e]) / (m1 + m0);
+        // products rounded before the sum, as numpy does (no fused multiply-add on the device)
+        vel[d * n_markers + m] = add_rn(mul_rn(m1, r.v[d * nn + e + 1]), mul_rn(m0, r.v[d * nn + e])) / (m1 + m0);
     }
 }
 

@@ -94,6 +94,8 @@ class CosseratRodBatch:
     def element_markers(self, position, velocity, dim: int = 3) -> None:
         """The element-centric markers of every rod into ``position`` and ``velocity``, float64 CUDA
         tensors (dim, n_rods * n_elems) (marker r * n + e): one launch, on the current stream."""
+        for name, t in (("position", position), ("velocity", velocity)):
+            self._check_marker_array(name, t, dim, (torch.float64,))
         self._require_cuda(position, velocity)
         _lib.call("sg_rod_batch_element_markers", ctypes.byref(self._batch), int(dim), position.data_ptr(),
                   velocity.data_ptr(), stream_ptr(self.device))
@@ -101,10 +103,28 @@ class CosseratRodBatch:
     def set_element_loads(self, lag_forcing, dim: int = 3) -> None:
         """Each rod's external forces from the Lagrangian forcing of its element markers (the
         reaction, half on each node) and its external torques zeroed: one launch."""
+        self._check_marker_array("lag_forcing", lag_forcing, dim, (torch.float32, torch.float64))
         self._require_cuda(lag_forcing)
         dtype = _lib.SG_F32 if lag_forcing.dtype == torch.float32 else _lib.SG_F64
         _lib.call("sg_rod_batch_element_loads", ctypes.byref(self._batch), int(dim), dtype, lag_forcing.data_ptr(),
                   stream_ptr(self.device))
+
+    def _check_marker_array(self, name, t, dim, dtypes):
+        """The native entries write or read (dim, n_rods * n_elems) elements of the marker arrays as
+        raw pointers: the dtype, shape, layout and device are checked here, before any launch."""
+        if dim not in (2, 3):
+            raise ValueError(f"dim must be 2 or 3 (got {dim})")
+        if not isinstance(t, torch.Tensor):
+            raise ValueError(f"{name} must be a torch tensor")
+        if t.dtype not in dtypes:
+            raise ValueError(f"{name} must be {' or '.join(str(d) for d in dtypes)} (got {t.dtype})")
+        shape = (dim, self.n_rods * self.n_elems)
+        if tuple(t.shape) != shape:
+            raise ValueError(f"{name} must have shape {shape} (got {tuple(t.shape)})")
+        if not t.is_contiguous():
+            raise ValueError(f"{name} must be C-contiguous")
+        if t.device != self.device:
+            raise ValueError(f"{name} lives on {t.device}; the batch lives on {self.device}")
 
     def _require_cuda(self, *tensors):
         if self.device.type != "cuda":

@@ -1,0 +1,112 @@
+// Test infrastructure: the register line FFT kernels of sopht_gb300/csrc/fft_reg.cuh run on the
+// host.  For every block, each phase of the kernel runs for all 256 threads before the next phase
+// starts (the kernel's barriers), with each thread's registers kept between phases, so the index
+// arithmetic (line addressing, the stage A / stage B split, the shared-memory slots, pruning and
+// the Green's lookup) is checked against a numpy FFT without a GPU.  Built by
+// tests/test_fft_reg_host.py with nvcc as host code; nothing here runs on a device.
+#include <vector>
+
+#include "../sopht_gb300/csrc/fft_reg.cuh"
+
+namespace {
+
+using namespace sg;
+
+template <int N, int MODE, bool HIN, bool HOUT>
+void run_pass(const RegLinesParams& p) {
+    constexpr int E = rl::Shape<N>::E;
+    const int blocks = (p.n_lines + rl::kLines - 1) / rl::kLines;
+    std::vector<float2> buf((size_t)N * rl::kLines);
+    std::vector<float2> regs((size_t)rl::kThreads * E);
+    for (int blk = 0; blk < blocks; ++blk) {
+        auto each = [&](auto&& phase) {
+            for (int tid = 0; tid < rl::kThreads; ++tid) {
+                const int l = tid % rl::kLines, q = tid / rl::kLines;
+                phase(l, q, rl::line_of(p, blk, l), regs.data() + (size_t)tid * E);
+            }
+        };
+        if (MODE == RL_INV) {
+            each([&](int l, int q, const rl::Line& L, float2* v) {
+                rl::load_b<N>(p, L, q, v);
+                rl::dft_b<N, true>(v);
+                rl::write_b<N>(buf.data(), l, q, v);
+            });
+            each([&](int l, int q, const rl::Line& L, float2* v) {
+                rl::read_a<N>(buf.data(), l, q, v);
+                rl::inv_a<N, HOUT>(p, q, v);
+                rl::store_a<N, HOUT>(p, L, q, v);
+            });
+        } else {
+            each([&](int l, int q, const rl::Line& L, float2* v) {
+                rl::load_a<N, HIN>(p, L, q, v);
+                rl::fwd_a<N, HIN>(p, q, v);
+                rl::write_a<N>(buf.data(), l, q, v);
+            });
+            if (MODE == RL_FWD) {
+                each([&](int l, int q, const rl::Line& L, float2* v) {
+                    rl::read_b<N>(buf.data(), l, q, v);
+                    rl::dft_b<N, false>(v);
+                    rl::store_b<N>(p, L, q, v);
+                });
+            } else {
+                each([&](int l, int q, const rl::Line& L, float2* v) {
+                    rl::read_b<N>(buf.data(), l, q, v);
+                    rl::dft_b<N, false>(v);
+                    rl::green_b<N>(p, L, q, v);
+                    rl::dft_b<N, true>(v);
+                });
+                each([&](int l, int q, const rl::Line&, float2* v) { rl::write_b<N>(buf.data(), l, q, v); });
+                each([&](int l, int q, const rl::Line& L, float2* v) {
+                    rl::read_a<N>(buf.data(), l, q, v);
+                    rl::inv_a<N, HOUT>(p, q, v);
+                    rl::store_a<N, HOUT>(p, L, q, v);
+                });
+            }
+        }
+    }
+}
+
+template <int N, int MODE>
+int dispatch(const RegLinesParams& p) {
+    const bool hin = MODE != RL_INV && 2 * p.n_in <= N;
+    const bool hout = MODE != RL_FWD && 2 * p.n_out <= N;
+    if (hin && hout) run_pass<N, MODE, MODE != RL_INV, MODE != RL_FWD>(p);
+    else if (hin) run_pass<N, MODE, MODE != RL_INV, false>(p);
+    else if (hout) run_pass<N, MODE, false, MODE != RL_FWD>(p);
+    else run_pass<N, MODE, false, false>(p);
+    return 0;
+}
+
+}  // namespace
+
+// mode: 0 forward, 1 inverse, 2 convolution; complex arrays interleaved (re, im) float32.
+extern "C" int rl_host_pass(int mode, int N, const float* in, float* out, int n_lines, int slab_lines,
+                            long long slab_stride, long long stride, int n_in, int n_out, const float* tw,
+                            const float* g, long long g_kstride, long long g_mstride, int g_div, int g_mmod) {
+    RegLinesParams p{};
+    p.in = reinterpret_cast<const float2*>(in);
+    p.out = reinterpret_cast<float2*>(out);
+    p.n_lines = n_lines;
+    p.slab_lines = slab_lines;
+    p.slab_stride = slab_stride;
+    p.stride = stride;
+    p.n_in = n_in;
+    p.n_out = n_out;
+    p.tw = reinterpret_cast<const float2*>(tw);
+    p.g = g;
+    p.g_kstride = g_kstride;
+    p.g_mstride = g_mstride;
+    p.g_div = g_div;
+    p.g_mmod = g_mmod;
+    if (N == 512) {
+        if (mode == RL_FWD) return dispatch<512, RL_FWD>(p);
+        if (mode == RL_INV) return dispatch<512, RL_INV>(p);
+        return dispatch<512, RL_CONV>(p);
+    }
+    if (N == 256) {
+        if (mode == RL_FWD) return dispatch<256, RL_FWD>(p);
+        if (mode == RL_INV) return dispatch<256, RL_INV>(p);
+        return dispatch<256, RL_CONV>(p);
+    }
+    return -1;
+}

@@ -1,0 +1,116 @@
+"""Index arithmetic of the register line FFT kernels, checked on the host.
+
+``sopht_gb300/csrc/fft_reg.cuh`` writes the phases of its kernels as
+host-and-device functions; ``tests/fft_reg_host.cu`` runs each block's 256
+threads phase by phase on the CPU (the kernel's barriers between phases).
+These tests lay out spectra the way the 3D Poisson passes do (y lines: slabs of
+nx + 1 adjacent lines per z plane; z lines: one slab of 2 ny (nx + 1) lines per
+component) and compare the forward, inverse and Green's-convolution passes
+with numpy's FFT, in float32, including line counts that leave the last block
+partly empty and the pruned (zero-padded input, cropped output) variants.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        pytest.skip("nvcc not available")
+    out = tmp_path_factory.mktemp("rl") / "librl_host.so"
+    cmd = [nvcc, "-O1", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC", "-shared",
+           "-gencode", "arch=compute_103a,code=sm_103a", str(ROOT / "tests" / "fft_reg_host.cu"), "-o", str(out)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    h = ctypes.CDLL(str(out))
+    h.rl_host_pass.restype = ctypes.c_int
+    h.rl_host_pass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
+                               ctypes.c_int, ctypes.c_int]
+    return h
+
+
+def _twiddles(n):
+    m = np.arange(n)
+    return np.exp(-2j * np.pi * m / n).astype(np.complex64)
+
+
+def _run(h, mode, N, buf, n_lines, slab_lines, slab_stride, stride, n_in, n_out, table=None,
+         g_kstride=0, g_mstride=0, g_div=1, g_mmod=0):
+    tw = _twiddles(N)
+    g = table if table is not None else np.zeros(1, np.float32)
+    rc = h.rl_host_pass(mode, N, buf.ctypes.data, buf.ctypes.data, n_lines, slab_lines, slab_stride, stride,
+                        n_in, n_out, tw.ctypes.data, g.ctypes.data, g_kstride, g_mstride, g_div, g_mmod)
+    assert rc == 0
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("N,ncomp,ny,nx", [(512, 2, 3, 6), (256, 3, 2, 4), (512, 1, 8, 1)])
+def test_z_convolution_pass(lib, N, ncomp, ny, nx):
+    rng = np.random.default_rng(N + ny)
+    nz = N // 2
+    nxp = nx + 1
+    plane = 2 * ny * nxp
+    spec = np.zeros((ncomp, nz, 2 * ny, nxp), np.complex64)
+    spec[...] = (rng.standard_normal(spec.shape) + 1j * rng.standard_normal(spec.shape)).astype(np.complex64)
+    table = rng.uniform(0.5, 1.5, (nz + 1, ny + 1, nxp)).astype(np.float32)
+    x = np.zeros((ncomp, N, 2 * ny, nxp), np.complex128)
+    x[:, :nz] = spec
+    X = np.fft.fft(x, axis=1)
+    k = np.arange(N)
+    ks = np.minimum(k, N - k)
+    m = np.arange(2 * ny)
+    ms = np.minimum(m, 2 * ny - m)
+    X *= table[ks][:, ms, :][None]
+    ref = (np.fft.ifft(X, axis=1) * N)[:, :nz]
+    buf = spec.copy()
+    _run(lib, 2, N, buf, ncomp * plane, plane, nz * plane, plane, nz, nz, table,
+         g_kstride=(ny + 1) * nxp, g_mstride=nxp, g_div=nxp, g_mmod=2 * ny)
+    assert _rel(buf, ref) < 2e-6
+
+
+@pytest.mark.parametrize("N,ncomp,nz,nx,half_in", [(512, 2, 3, 6, True), (256, 3, 2, 5, True),
+                                                    (512, 1, 2, 3, False), (256, 1, 1, 16, False)])
+def test_y_forward_pass(lib, N, ncomp, nz, nx, half_in):
+    rng = np.random.default_rng(N + nz + nx)
+    ny = N // 2
+    nxp = nx + 1
+    spec = np.zeros((ncomp, nz, N, nxp), np.complex64)
+    n_in = ny if half_in else N
+    spec[:, :, :n_in] = (rng.standard_normal((ncomp, nz, n_in, nxp))
+                         + 1j * rng.standard_normal((ncomp, nz, n_in, nxp))).astype(np.complex64)
+    ref = np.fft.fft(spec.astype(np.complex128), axis=2)
+    buf = spec.copy()
+    _run(lib, 0, N, buf, ncomp * nz * nxp, nxp, N * nxp, nxp, n_in, N)
+    assert _rel(buf, ref) < 2e-6
+
+
+@pytest.mark.parametrize("N,ncomp,nz,nx,half_out", [(512, 2, 3, 6, True), (256, 3, 2, 5, True),
+                                                     (512, 1, 2, 3, False), (256, 2, 1, 8, False)])
+def test_y_inverse_pass(lib, N, ncomp, nz, nx, half_out):
+    rng = np.random.default_rng(7 * N + nz + nx)
+    nxp = nx + 1
+    spec = (rng.standard_normal((ncomp, nz, N, nxp))
+            + 1j * rng.standard_normal((ncomp, nz, N, nxp))).astype(np.complex64)
+    n_out = N // 2 if half_out else N
+    ref = (np.fft.ifft(spec.astype(np.complex128), axis=2) * N)[:, :, :n_out]
+    buf = spec.copy()
+    _run(lib, 1, N, buf, ncomp * nz * nxp, nxp, N * nxp, nxp, N, n_out)
+    assert _rel(buf[:, :, :n_out], ref) < 2e-6
+    if half_out:  # points beyond the crop are left as they were
+        np.testing.assert_array_equal(buf[:, :, n_out:], spec[:, :, n_out:])

@@ -94,8 +94,10 @@ def test_poisson_2d_vs_oracle_sizes(precision, shape):
 
 
 @pytest.mark.parametrize("shape", [(32, 48, 64), (24, 24, 24), (16, 32, 48), (64, 64, 64), (32, 64, 128),
-                                   (128, 128, 128)])
+                                   (128, 128, 128), (256, 64, 64), (64, 256, 64), (128, 256, 32), (64, 64, 256)])
 def test_poisson_3d_vs_oracle_sizes(precision, shape):
+    """Doubled lengths 256 and 512 along y and z take the register line kernels in fp32 (shared-memory
+    kernels in fp64); the others the shared-memory kernels."""
     from oracle.poisson import UnboundedPoisson3D
     from sopht_gb300.numeric import UnboundedPoissonSolver3D as GPUPoisson
     rt = real_t_of(precision)
@@ -105,6 +107,22 @@ def test_poisson_3d_vs_oracle_sizes(precision, shape):
     sol = torch.zeros_like(dev(rhs))
     solver.vector_field_solve(sol, dev(rhs))
     assert rel_l2(host(sol), ref) < (2e-6 if rt == np.float32 else 1e-13)
+
+
+def test_poisson_3d_256_cube_vs_oracle():
+    """The 256^3 vector solve (512-point y and z line passes, the configuration of the 16-rod carpet)
+    against the FP64 oracle."""
+    from oracle.poisson import UnboundedPoisson3D
+    from sopht_gb300.numeric import UnboundedPoissonSolver3D as GPUPoisson
+    shape = (256, 256, 256)
+    rhs = np.random.default_rng(9).standard_normal((3, *shape)).astype(np.float32)
+    ora = UnboundedPoisson3D(*shape, 1.0, np.float64, greens_dtype=np.float64)
+    solver = GPUPoisson(*shape, 1.0, real_t=np.float32)
+    sol = torch.zeros_like(dev(rhs))
+    solver.vector_field_solve(sol, dev(rhs))
+    out = host(sol)
+    for c in range(3):
+        assert rel_l2(out[c], ora.solve(rhs[c].astype(np.float64))) < 2e-6, c
 
 
 # ---------------------------------------------------------- single operators

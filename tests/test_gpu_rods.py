@@ -1,4 +1,4 @@
-"""GPU checks of code that has not yet run on a GPU; each moves to its topic's module once it has.
+"""GPU checks of the batched rod kernels and of the divergence without a ring reset.
 
 * the batched rod kernel against the numpy rod model: three rods (clamped and
   free, bent, twisted, loaded) in one ``CosseratRodBatch``, 300 sub-steps in
@@ -9,21 +9,14 @@
   bitwise the forcing grid's numpy formulas;
 * ``gen_divergence_pyst_kernel_3d(reset_ghost_zone=False)`` keeps the output's
   ring and writes the same interior as the default.
-
-The module waits for ``SOPHT_GB300_PENDING_GPU=1``, set by whoever runs these
-first, so that a suite run elsewhere does not stop on them.
 """
 
 from __future__ import annotations
 
-import os
-
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("SOPHT_GB300_PENDING_GPU") != "1",
-                                 reason="first GPU run not yet made (set SOPHT_GB300_PENDING_GPU=1)")]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("per_call,damping", [(300, 0.0), (1, 3.0)])

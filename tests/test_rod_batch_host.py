@@ -187,6 +187,42 @@ def test_rod_batch_layout_without_a_gpu():
                                                                      0.1, 1.0, 1e3))], device="cpu")
 
 
+def test_rod_batch_marker_arrays_are_checked_before_any_launch():
+    """The marker and forcing arrays go to the native entries as raw pointers, so their dtype, shape,
+    layout and device are checked in Python (ValueError) before the CUDA requirement (RuntimeError)."""
+    import torch
+
+    import sopht_gb300.simulator as sps
+    rods = _rods()
+    batch = sps.CosseratRodBatch([_PyelasticaNamed(r) for r in rods], device="cpu")
+    m = len(rods) * N
+    good = torch.zeros((3, m), dtype=torch.float64)
+    bad = {
+        "float32 position": (torch.zeros((3, m), dtype=torch.float32), good),
+        "short position": (torch.zeros((3, m - 1), dtype=torch.float64), good),
+        "2D-shaped position for dim 3": (torch.zeros((2, m), dtype=torch.float64), good),
+        "strided velocity": (good, torch.zeros((m, 3), dtype=torch.float64).t()),
+        "numpy velocity": (good, np.zeros((3, m))),
+    }
+    for what, (pos, vel) in bad.items():
+        with pytest.raises(ValueError):
+            batch.element_markers(pos, vel, dim=3)
+        assert what
+    with pytest.raises(ValueError, match="dim"):
+        batch.element_markers(good, good, dim=4)
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        batch.element_markers(good, good.clone(), dim=3)
+    for forcing in (torch.zeros((3, m), dtype=torch.float16), torch.zeros((3, m + 1)), torch.zeros((2, m)),
+                    torch.zeros((3, m), dtype=torch.int64)):
+        with pytest.raises(ValueError):
+            batch.set_element_loads(forcing, dim=3)
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        batch.set_element_loads(torch.zeros((2, m), dtype=torch.float32), dim=2)
+    if torch.cuda.is_available():  # a tensor on another device than the batch's
+        with pytest.raises(ValueError, match="lives on"):
+            batch.set_element_loads(torch.zeros((3, m), device="cuda"), dim=3)
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_host_element_markers_and_loads_match_the_forcing_grid(host_lib, dim):
     """The batch's element-centric markers and reaction loads (rod.cuh) against the forcing grid's
