@@ -520,6 +520,52 @@ int sg_rod_batch_element_markers(const sg_rod_batch* batch, int dim, double* pos
 int sg_rod_batch_element_loads(const sg_rod_batch* batch, int dim, int dtype, const void* lag_forcing,
                                void* stream);
 
+/* The flow coupling of a rod batch over one flow step, 3D.  Replaces the rod
+ * loop of the reference examples (flow_past_rod_case.py:231-243,
+ * immersed_magnetic_cilia_carpet.py:231-240): rod_time_steps =
+ * int(flow_dt / min(flow_dt, max_rod_dt)) sub-steps of flow_dt /
+ * rod_time_steps, each one pyelastica's position-Verlet do_step with
+ * FlowForces.apply_forces (flow_forces.py:22-25) evaluated at the half-step
+ * configuration -- the element-centric markers (cosserat_rod_forcing_grids.py:
+ * 82-130), the interaction force of VirtualBoundaryForcing.
+ * compute_interaction_force_on_lag_grid (VirtualBoundaryForcing.py:187-230)
+ * and its reaction as the rods' external forces -- followed by
+ * VirtualBoundaryForcing.time_step (xi += dt dU, :276-283).  One launch, one
+ * CTA per rod; the sub-step count is read on the device, so the call can be
+ * part of a step whose dt never leaves the GPU.  Lagrangian fields are
+ * (3, n_rods * n_elems) in the flow precision `dtype`; marker positions and
+ * velocities float64.  A driven clamp (drive_phase not NULL) turns each
+ * clamped rod's element 0 about the lab axis drive_axis by
+ * theta(t) = drive_amplitude sin(2 pi drive_frequency t + drive_phase[rod]),
+ * its node 0 held in place.  damping_rate as in sg_rod_batch_step.  Markers
+ * whose support leaves the grid set *status to SG_ERR_OUT_OF_DOMAIN. */
+typedef struct sg_rod_coupling {
+    int dtype;                      /* SG_F32 or SG_F64 */
+    int nz, ny, nx;
+    double dx, shift;               /* Eulerian spacing and coordinate shift (dx / 2) */
+    int kernel_type;                /* 0 cosine, 1 Peskin */
+    const void* flow_velocity;      /* (3, nz, ny, nx), read only */
+    double* marker_position;        /* (3, n_markers) float64, written */
+    double* marker_velocity;        /* (3, n_markers) float64, written */
+    int32_t* nearest;               /* (3, n_markers) */
+    void* weights;                  /* (64, n_markers) */
+    void* flow_velocity_lag;        /* (3, n_markers) */
+    void* velocity_mismatch;        /* (3, n_markers) */
+    void* position_mismatch;        /* (3, n_markers) */
+    void* lag_forcing;              /* (3, n_markers) */
+    double stiffness, damping;      /* K, C after the Lagrangian-spacing rescale */
+    double flow_dt, flow_time;      /* used when dev_scalars is NULL */
+    const sg_step_scalars* dev_scalars; /* device dt of the flow step, or NULL */
+    const double* dev_time_end;     /* with dev_scalars: device flow time after the step's dt */
+    double max_rod_dt;
+    double damping_rate;
+    const double* drive_phase;      /* (n_rods) device, or NULL */
+    double drive_amplitude, drive_frequency;
+    double drive_axis[3];
+    int32_t* status;                /* device status word */
+} sg_rod_coupling;
+int sg_rod_batch_coupled_substeps(const sg_rod_batch* batch, const sg_rod_coupling* coupling, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,10 @@ struct RegLinesParams {
     int64_t g_mstride;
     int g_div;
     int g_mmod;
+    // > 1: consecutive blocks take the same 16 lines of `interleave` consecutive slabs (the three
+    // components of the z pass share their Green's table rows through L2); needs slab_lines % 16 == 0
+    // and n_lines == interleave * slab_lines
+    int interleave;
 };
 
 enum { RL_FWD = 0, RL_INV = 1, RL_CONV = 2 };
@@ -67,7 +71,8 @@ template <int N> struct Shape {
     static_assert(N == 256 || N == 512, "register line FFT lengths: 256 and 512");
     static constexpr int E = N / 16;  // points per thread
     static constexpr int B = E / 16;  // length-16 DFTs per thread in stage B
-    static constexpr size_t smem_bytes = sizeof(float2) * (size_t)N * kLines;
+    static constexpr int TW = 16 * E;  // stage-A twiddles w_N^(g k2), [g][k2]
+    static constexpr size_t smem_bytes = sizeof(float2) * ((size_t)N * kLines + TW);
 };
 
 // cos and sin of 2 pi m / 32, m < 16 (the twiddles inside a 32-point DFT)
@@ -125,6 +130,14 @@ struct Line {
 
 SG_RL_FN Line line_of(const RegLinesParams& p, int block, int l) {
     Line L;
+    if (p.interleave > 1) {
+        const int grp = block / p.interleave, slab = block - grp * p.interleave;
+        L.w = grp * kLines + l;
+        L.live = L.w < p.slab_lines;
+        if (!L.live) L.w = 0;
+        L.base = (int64_t)slab * p.slab_stride + L.w;
+        return L;
+    }
     const int q = block * kLines + l;
     L.live = q < p.n_lines;
     const int qq = L.live ? q : 0;
@@ -132,6 +145,12 @@ SG_RL_FN Line line_of(const RegLinesParams& p, int block, int l) {
     L.w = qq - slab * p.slab_lines;
     L.base = (int64_t)slab * p.slab_stride + L.w;
     return L;
+}
+
+// The stage-A twiddle table of a block: tw_a[g * E + k2] = w_N^(g k2), g < 16, k2 < E (g k2 < N).
+template <int N> SG_RL_FN void stage_twiddles(const RegLinesParams& p, float2* tw_a, int tid, int nt) {
+    constexpr int E = Shape<N>::E;
+    for (int i = tid; i < 16 * E; i += nt) tw_a[i] = p.tw[(i / E) * (i % E)];
 }
 
 // ---- stage A (thread (l, g)): points g + 16 j
@@ -147,18 +166,20 @@ SG_RL_FN void load_a(const RegLinesParams& p, const Line& L, int g, float2* v) {
 }
 
 template <int N, bool HIN>
-SG_RL_FN void fwd_a(const RegLinesParams& p, int g, float2* v) {
+SG_RL_FN void fwd_a(const float2* tw_a, int g, float2* v) {
     constexpr int E = Shape<N>::E;
     dft_e<E, false, HIN, false>(v);
+    const float2* w = tw_a + g * E;
 #pragma unroll
-    for (int k2 = 1; k2 < E; ++k2) v[k2] = cmul(v[k2], p.tw[g * k2]);
+    for (int k2 = 1; k2 < E; ++k2) v[k2] = cmul(v[k2], w[k2]);
 }
 
 template <int N, bool HOUT>
-SG_RL_FN void inv_a(const RegLinesParams& p, int g, float2* v) {
+SG_RL_FN void inv_a(const float2* tw_a, int g, float2* v) {
     constexpr int E = Shape<N>::E;
+    const float2* w = tw_a + g * E;
 #pragma unroll
-    for (int k2 = 1; k2 < E; ++k2) v[k2] = cmul(v[k2], cconj(p.tw[g * k2]));
+    for (int k2 = 1; k2 < E; ++k2) v[k2] = cmul(v[k2], cconj(w[k2]));
     dft_e<E, true, false, HOUT>(v);
 }
 
@@ -234,13 +255,16 @@ SG_RL_FN void green_b(const RegLinesParams& p, const Line& L, int t, float2* v) 
     const int kx = L.w - m * p.g_div;
     const int ms = p.g_mmod > 0 ? (m < p.g_mmod - m ? m : p.g_mmod - m) : 0;
     const float* gl = p.g + (int64_t)ms * p.g_mstride + kx;
+    // point k = t + 16 b + E r; for r < 8, k < N/2 and the folded index is k, else N - k
+    const int64_t kst = p.g_kstride;
+    const float* lo = gl + (int64_t)t * kst;
+    const float* hi = gl + (int64_t)(N - t) * kst;
 #pragma unroll
     for (int b = 0; b < Shape<N>::B; ++b)
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
-            const int k = point_b<N>(t, b, r);
-            const int ks = k < N - k ? k : N - k;
-            const float gv = L.live ? gl[(int64_t)ks * p.g_kstride] : 0.f;
+            const int64_t off = (int64_t)(16 * b + Shape<N>::E * r) * kst;
+            const float gv = L.live ? (r < 8 ? lo[off] : hi[-off]) : 0.f;
             v[b * 16 + r] = cscale(v[b * 16 + r], gv);
         }
 }
@@ -254,20 +278,23 @@ SG_RL_FN void green_b(const RegLinesParams& p, const Line& L, int t, float2* v) 
 template <int N, int MODE, bool HIN, bool HOUT>
 __global__ void __launch_bounds__(rl::kThreads, (N == 512 ? 2 : 3)) reg_lines_kernel(RegLinesParams p) {
     extern __shared__ __align__(16) float2 rl_buf[];
+    float2* tw_a = rl_buf + N * rl::kLines;
     const int tid = threadIdx.x, l = tid & (rl::kLines - 1), q = tid / rl::kLines;
     const rl::Line L = rl::line_of(p, blockIdx.x, l);
     float2 v[rl::Shape<N>::E];
+    rl::stage_twiddles<N>(p, tw_a, tid, rl::kThreads);
     if constexpr (MODE == RL_INV) {
         rl::load_b<N>(p, L, q, v);
         rl::dft_b<N, true>(v);
         rl::write_b<N>(rl_buf, l, q, v);
         __syncthreads();
         rl::read_a<N>(rl_buf, l, q, v);
-        rl::inv_a<N, HOUT>(p, q, v);
+        rl::inv_a<N, HOUT>(tw_a, q, v);
         rl::store_a<N, HOUT>(p, L, q, v);
     } else {
         rl::load_a<N, HIN>(p, L, q, v);
-        rl::fwd_a<N, HIN>(p, q, v);
+        __syncthreads();  // the twiddle table
+        rl::fwd_a<N, HIN>(tw_a, q, v);
         rl::write_a<N>(rl_buf, l, q, v);
         __syncthreads();
         rl::read_b<N>(rl_buf, l, q, v);
@@ -281,7 +308,7 @@ __global__ void __launch_bounds__(rl::kThreads, (N == 512 ? 2 : 3)) reg_lines_ke
             rl::write_b<N>(rl_buf, l, q, v);
             __syncthreads();
             rl::read_a<N>(rl_buf, l, q, v);
-            rl::inv_a<N, HOUT>(p, q, v);
+            rl::inv_a<N, HOUT>(tw_a, q, v);
             rl::store_a<N, HOUT>(p, L, q, v);
         }
     }
@@ -293,6 +320,9 @@ template <int MODE>
 int launch_reg_lines(const RegLinesParams& p, int N, cudaStream_t stream) {
     const bool hin = MODE != RL_INV && 2 * p.n_in <= N;
     const bool hout = MODE != RL_FWD && 2 * p.n_out <= N;
+    const bool inter_ok = p.interleave <= 1 || (p.slab_lines % rl::kLines == 0 &&
+                                               (int64_t)p.interleave * p.slab_lines == p.n_lines);
+    SG_REQUIRE(inter_ok, SG_ERR_INVALID_ARG, "register lines: interleave needs whole 16-line groups");
     const unsigned blocks = ceil_div(p.n_lines, rl::kLines);
     if (p.n_lines <= 0) return SG_OK;
     auto run = [&](auto kern, size_t smem) -> int {

@@ -276,6 +276,8 @@ static int reg_pass3d(sg_poisson_plan_s* p, int ncomp, int pass, cudaStream_t st
         r.g_mstride = nx + 1;
         r.g_div = nx + 1;
         r.g_mmod = 2 * ny;
+        // the components of one 16-line group in consecutive blocks: their Green's rows are shared
+        r.interleave = (ncomp > 1 && plane % rl::kLines == 0) ? ncomp : 1;
         return launch_reg_lines<RL_CONV>(r, 2 * nz, stream);
     }
     SG_REQUIRE((int64_t)ncomp * nz * (nx + 1) < (1LL << 31), SG_ERR_SHAPE, "y pass: too many lines");

@@ -5,6 +5,7 @@
 // barrier separates the passes that read neighbours from the ones that write them.  The per-rod
 // work arrays live in shared memory.
 #include "common.cuh"
+#include "ib.cuh"
 #include "rod.cuh"
 
 namespace sg {
@@ -51,6 +52,86 @@ __global__ void __launch_bounds__(256) rod_loads_kernel(sg_rod_batch b, int dim,
         rod::View v = rod::view_of(b, r);
         rod::element_reaction(v, r, i, dim, n_markers, forcing, b.external_forces + (int64_t)r * 3 * nn,
                               b.external_torques + (int64_t)r * 3 * n);
+    }
+}
+
+// ------------------------------------------------------------------ flow coupling
+// One flow step of the rod loop of the reference examples for every rod of a batch (one CTA per
+// rod): rod_time_steps = int(dt / min(dt, max_rod_dt)) position-Verlet sub-steps of dt /
+// rod_time_steps, each with the flow forces of the half-step configuration (the element-centric
+// markers, the virtual-boundary interaction of ib_interaction_body on those markers, the reaction
+// on the nodes) and followed by xi += dt_sub dU.  The sub-step count comes from the device dt, so
+// a captured step needs no host value.
+template <typename T> struct RodCouplingArgs {
+    IBParams<T> ib;           // marker arrays of the whole batch (n_lag = n_rods * n_elems)
+    double* marker_pos;       // == ib.pos, written here
+    double* marker_vel;       // == ib.body_vel
+    double host_dt, host_time;
+    const sg_step_scalars* dev;
+    const double* dev_time_end;
+    double max_rod_dt, damping_rate;
+    const double* drive_phase;
+    double drive_amp, drive_freq;
+    double axis[3];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCouplingArgs<T> c) {
+    extern __shared__ double rod_smem[];
+    const int r = blockIdx.x, n = b.n_elems, t = threadIdx.x, nt = blockDim.x;
+    rod::View v = rod::view_of(b, r);
+    const rod::Scratch s = rod::carve(rod_smem, n);
+    double* clamp = rod_smem + rod::scratch_doubles(n);  // q (9), w (3) of a driven clamp
+    const bool driven = c.drive_phase != nullptr && v.clamped;
+    if (driven) {
+        v.clamp_q = clamp;
+        v.clamp_w = clamp + 9;
+    }
+    const double dt = c.dev ? c.dev->dt : c.host_dt;
+    const double t0 = c.dev ? *c.dev_time_end - dt : c.host_time;
+    const int n_sub = dt > c.max_rod_dt ? (int)(dt / c.max_rod_dt) : 1;
+    const double h = dt / n_sub;
+    const double decay = c.damping_rate != 0.0 ? exp(-c.damping_rate * h) : 1.0;
+    const int64_t n_markers = (int64_t)b.n_rods * n;
+    const int warp = t >> 5, n_warps = nt >> 5;
+    const double* q0 = b.clamp_directors + r * 9;
+    const double phase = driven ? c.drive_phase[r] : 0.0;
+    for (int k = 0; k < n_sub; ++k) {
+        const double tk = t0 + k * h;
+        if (driven && t == 0) rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + 0.5 * h, clamp,
+                                                clamp + 9);
+        __syncthreads();
+        for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
+        for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
+        __syncthreads();
+        // FlowForces.apply_forces at the half step: markers, interaction, reaction
+        for (int e = t; e < n; e += nt) rod::element_marker(v, r, e, 3, n_markers, c.marker_pos, c.marker_vel);
+        __syncthreads();
+        for (int e = warp; e < n; e += n_warps) ib_interaction_body<T, 3>(c.ib, r * n + e);
+        __syncthreads();
+        for (int i = t; i <= n; i += nt)
+            rod::element_reaction(v, r, i, 3, n_markers, c.ib.forcing, b.external_forces + (int64_t)r * 3 * (n + 1),
+                                  b.external_torques + (int64_t)r * 3 * n);
+        __syncthreads();
+        for (int e = t; e < n; e += nt) rod::element_pass(v, s, e);
+        __syncthreads();
+        for (int q = t; q < n - 1; q += nt) rod::voronoi_pass(v, s, q);
+        __syncthreads();
+        for (int i = t; i <= n; i += nt) rod::node_update(v, s, i, h, decay);
+        for (int e = t; e < n; e += nt) rod::element_update(v, s, e, h, decay);
+        __syncthreads();
+        if (driven && t == 0) rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + h, clamp,
+                                                clamp + 9);
+        __syncthreads();
+        for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
+        for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
+        // VirtualBoundaryForcing.time_step(local_rod_dt) of this rod's markers
+        const T hT = (T)h;
+        for (int e = t; e < n; e += nt)
+            for (int d = 0; d < 3; ++d) {
+                const int64_t m = d * n_markers + (int64_t)r * n + e;
+                c.ib.pos_mismatch[m] = c.ib.pos_mismatch[m] + hT * c.ib.vel_mismatch[m];
+            }
     }
 }
 
@@ -121,4 +202,85 @@ extern "C" int sg_rod_batch_step(const sg_rod_batch* batch, int n_substeps, doub
     const int threads = (b.n_elems + 1 + 31) / 32 * 32 < 256 ? (b.n_elems + 1 + 31) / 32 * 32 : 256;
     sg::rod_batch_kernel<<<b.n_rods, threads, smem, (cudaStream_t)stream>>>(b, n_substeps, dt, decay);
     return sg::launch_status("rod batch step");
+}
+
+namespace sg {
+template <typename T>
+static int rod_coupled_launch(const sg_rod_batch& b, const sg_rod_coupling& cp, cudaStream_t stream) {
+    RodCouplingArgs<T> c{};
+    IBParams<T>& ip = c.ib;
+    ip.dim = 3;
+    ip.nz = cp.nz;
+    ip.ny = cp.ny;
+    ip.nx = cp.nx;
+    ip.n_lag = b.n_rods * b.n_elems;
+    ip.kernel = cp.kernel_type;
+    ip.dx = cp.dx;
+    ip.shift = cp.shift;
+    ip.pos = cp.marker_position;
+    ip.body_vel = cp.marker_velocity;
+    ip.u = (const T*)cp.flow_velocity;
+    ip.nearest = cp.nearest;
+    ip.weights = (T*)cp.weights;
+    ip.flow_vel = (T*)cp.flow_velocity_lag;
+    ip.vel_mismatch = (T*)cp.velocity_mismatch;
+    ip.pos_mismatch = (T*)cp.position_mismatch;
+    ip.forcing = (T*)cp.lag_forcing;
+    ip.K = cp.stiffness;
+    ip.C = cp.damping;
+    ip.xi_step = 0;
+    ip.dev = nullptr;
+    ip.status = cp.status;
+    ip.dyn = nullptr;
+    c.marker_pos = cp.marker_position;
+    c.marker_vel = cp.marker_velocity;
+    c.host_dt = cp.flow_dt;
+    c.host_time = cp.flow_time;
+    c.dev = cp.dev_scalars;
+    c.dev_time_end = cp.dev_time_end;
+    c.max_rod_dt = cp.max_rod_dt;
+    c.damping_rate = cp.damping_rate;
+    c.drive_phase = cp.drive_phase;
+    c.drive_amp = cp.drive_amplitude;
+    c.drive_freq = cp.drive_frequency;
+    for (int a = 0; a < 3; ++a) c.axis[a] = cp.drive_axis[a];
+    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 12) * sizeof(double);
+    if (smem > 48 * 1024)
+        SG_TRY(cuda_status(cudaFuncSetAttribute(rod_coupled_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem),
+                           "rod coupled smem"));
+    rod_coupled_kernel<T><<<b.n_rods, 256, smem, stream>>>(b, c);
+    return launch_status("rod coupled sub-steps");
+}
+}  // namespace sg
+
+extern "C" int sg_rod_batch_coupled_substeps(const sg_rod_batch* batch, const sg_rod_coupling* cp, void* stream) {
+    SG_TRY(rod_batch_check(batch, 3));
+    SG_REQUIRE(cp, SG_ERR_INVALID_ARG, "rod coupling: null coupling");
+    const sg_rod_batch& b = *batch;
+    SG_REQUIRE(b.n_elems <= 1024, SG_ERR_SHAPE, "rod coupling: 1 to 1024 elements per rod");
+    SG_REQUIRE(b.directors && b.omega && b.rest_lengths && b.shear_matrix && b.mass_second_moment &&
+                   b.inv_mass_second_moment && b.rest_sigma,
+               SG_ERR_INVALID_ARG, "rod coupling: null rod array");
+    SG_REQUIRE(b.n_elems == 1 || (b.rest_voronoi_lengths && b.bend_matrix && b.rest_kappa), SG_ERR_INVALID_ARG,
+               "rod coupling: null Voronoi array");
+    SG_REQUIRE(!b.clamped || (b.clamp_position && b.clamp_directors), SG_ERR_INVALID_ARG,
+               "rod coupling: clamped rods need the clamp position and directors");
+    SG_REQUIRE(cp->dtype == SG_F32 || cp->dtype == SG_F64, SG_ERR_INVALID_ARG, "rod coupling: bad dtype");
+    SG_REQUIRE(cp->kernel_type == 0 || cp->kernel_type == 1, SG_ERR_INVALID_ARG, "rod coupling: bad kernel type");
+    SG_REQUIRE(cp->nz >= 4 && cp->ny >= 4 && cp->nx >= 4 && cp->dx > 0, SG_ERR_SHAPE, "rod coupling: bad grid");
+    SG_REQUIRE(cp->flow_velocity && cp->marker_position && cp->marker_velocity && cp->nearest && cp->weights &&
+                   cp->flow_velocity_lag && cp->velocity_mismatch && cp->position_mismatch && cp->lag_forcing &&
+                   cp->status,
+               SG_ERR_INVALID_ARG, "rod coupling: null marker or field array");
+    SG_REQUIRE(cp->dev_scalars ? cp->dev_time_end != nullptr : cp->flow_dt > 0, SG_ERR_INVALID_ARG,
+               "rod coupling: a positive host dt, or the device dt and time");
+    SG_REQUIRE(cp->max_rod_dt > 0, SG_ERR_INVALID_ARG, "rod coupling: max_rod_dt must be positive");
+    if (cp->drive_phase) {
+        const double* a = cp->drive_axis;
+        const double norm = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        SG_REQUIRE(fabs(norm - 1.0) < 1e-12, SG_ERR_INVALID_ARG, "rod coupling: drive_axis must be a unit vector");
+    }
+    auto s = (cudaStream_t)stream;
+    return cp->dtype == SG_F32 ? sg::rod_coupled_launch<float>(b, *cp, s) : sg::rod_coupled_launch<double>(b, *cp, s);
 }

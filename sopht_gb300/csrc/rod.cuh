@@ -51,6 +51,7 @@ struct View {
     int clamped;
     const double* clamp_x;
     const double* clamp_q;
+    const double* clamp_w;  // angular velocity of a driven clamp (local frame), or null: at rest
 };
 
 SG_ROD_FN View view_of(const sg_rod_batch& b, int r) {
@@ -76,6 +77,7 @@ SG_ROD_FN View view_of(const sg_rod_batch& b, int r) {
     v.clamped = b.clamped ? b.clamped[r] : 0;
     v.clamp_x = b.clamp_position + r * 3;
     v.clamp_q = b.clamp_directors + r * 9;
+    v.clamp_w = nullptr;
     return v;
 }
 
@@ -162,7 +164,31 @@ SG_ROD_FN void clamp_node0(View& r) {
 
 SG_ROD_FN void clamp_element0(View& r) {
     for (int a = 0; a < 9; ++a) r.q[a * r.n] = r.clamp_q[a];
-    for (int a = 0; a < 3; ++a) r.w[a * r.n] = 0.0;
+    for (int a = 0; a < 3; ++a) r.w[a * r.n] = r.clamp_w ? r.clamp_w[a] : 0.0;
+}
+
+// A clamp driven by a rotation of the rod's base: element 0's directors at time t are Q0 R^T, with
+// R = exp([theta a]x) the turn of the lab frame by theta(t) = A sin(2 pi f t + phi) about the unit lab
+// axis a (each director d_i -> R d_i), and its angular velocity in the local frame Q0 R^T (theta' a).
+SG_ROD_FN void driven_clamp(const double* q0, const double axis[3], double amp, double freq, double phase,
+                            double t, double q[9], double w[3]) {
+    const double two_pi = 6.283185307179586476925286766559;
+    const double arg = two_pi * freq * t + phase;
+    const double theta = amp * sin(arg), rate = amp * two_pi * freq * cos(arg);
+    const double a[3] = {theta * axis[0], theta * axis[1], theta * axis[2]};
+    double rot[9];
+    rotation_exp(a, rot);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int m = 0; m < 3; ++m) acc += q0[i * 3 + m] * rot[j * 3 + m];
+            q[i * 3 + j] = acc;
+        }
+    for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc += q[i * 3 + j] * axis[j] * rate;
+        w[i] = acc;
+    }
 }
 
 SG_ROD_FN void drift_node(View& r, int i, double h) {

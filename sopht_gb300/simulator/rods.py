@@ -42,6 +42,67 @@ _FIELD = {"position_collection": "position", "velocity_collection": "velocity", 
           "rest_kappa": "rest_kappa", "external_forces": "external_forces", "external_torques": "external_torques"}
 
 
+SHEAR_COEFFICIENT = 4.0 / 3.0  # shear correction factor of a circular cross-section
+
+
+class StraightRod:
+    """A straight Cosserat rod at rest, with pyelastica's ``CosseratRod`` attribute names.
+
+    Pyelastica (``CosseratRod.straight_rod``) builds the rods SophT couples to its flows; it is not
+    a dependency of this package, so this class lays out the same discrete model for the GPU batch:
+    n elements of rest length L / n between n + 1 nodes from ``start`` along ``direction``, directors
+    with rows (normal, direction x normal, direction), a circular cross-section of radius r (A = pi
+    r^2, I = pi r^4 / 4), node masses from the element masses rho A l0 (half to each end node),
+    shear/stretch matrix diag(4/3 G A, 4/3 G A, E A), bend/twist matrix diag(E I, E I, G 2I) averaged
+    onto the Voronoi regions with the rest-length weights, mass second moment rho l0 diag(I, I, 2I)
+    and straight rest configuration.  ``G`` defaults to E / 3 (incompressible, Poisson ratio 1/2).
+    """
+
+    def __init__(self, n_elements, start, direction, normal, base_length, base_radius, density, youngs_modulus,
+                 shear_modulus=None):
+        n = int(n_elements)
+        if n < 1:
+            raise ValueError("a rod needs at least one element")
+        direction = np.asarray(direction, dtype=np.float64)
+        normal = np.asarray(normal, dtype=np.float64)
+        direction = direction / np.linalg.norm(direction)
+        normal = normal / np.linalg.norm(normal)
+        if abs(float(direction @ normal)) > 1e-12:
+            raise ValueError("the normal must be perpendicular to the rod direction")
+        g = youngs_modulus / 3.0 if shear_modulus is None else float(shear_modulus)
+        s = np.linspace(0.0, float(base_length), n + 1)
+        self.n_elems = n
+        self.position_collection = np.asarray(start, dtype=np.float64)[:, None] + np.outer(direction, s)
+        self.velocity_collection = np.zeros((3, n + 1))
+        frame = np.stack([normal, np.cross(direction, normal), direction])
+        self.director_collection = np.repeat(frame[:, :, None], n, axis=2)
+        self.omega_collection = np.zeros((3, n))
+        self.rest_lengths = np.diff(s)
+        self.lengths = self.rest_lengths.copy()
+        self.rest_voronoi_lengths = 0.5 * (self.rest_lengths[1:] + self.rest_lengths[:-1])
+        self.radius = np.full(n, float(base_radius))
+        area = np.pi * self.radius**2
+        inertia = area**2 / (4.0 * np.pi)
+        element_mass = density * area * self.rest_lengths
+        self.mass = np.zeros(n + 1)
+        self.mass[:-1] += 0.5 * element_mass
+        self.mass[1:] += 0.5 * element_mass
+        eye = np.eye(3)[:, :, None]
+        self.shear_matrix = eye * np.stack([SHEAR_COEFFICIENT * g * area, SHEAR_COEFFICIENT * g * area,
+                                            youngs_modulus * area])[None]
+        bend = eye * np.stack([youngs_modulus * inertia, youngs_modulus * inertia, 2.0 * g * inertia])[None]
+        w = self.rest_lengths
+        self.bend_matrix = (bend[..., 1:] * w[1:] + bend[..., :-1] * w[:-1]) / (w[1:] + w[:-1])
+        self.mass_second_moment_of_inertia = eye * np.stack([inertia, inertia, 2.0 * inertia])[None] * (
+            density * self.rest_lengths)
+        self.inv_mass_second_moment_of_inertia = eye / np.stack(
+            [inertia, inertia, 2.0 * inertia])[None] / (density * self.rest_lengths)
+        self.rest_sigma = np.zeros((3, n))
+        self.rest_kappa = np.zeros((3, n - 1))
+        self.external_forces = np.zeros((3, n + 1))
+        self.external_torques = np.zeros((3, n))
+
+
 class CosseratRodBatch:
     """Rods of one element count, their arrays on ``device`` (FP64, rod index first)."""
 

@@ -18,6 +18,8 @@ void run_pass(const RegLinesParams& p) {
     const int blocks = (p.n_lines + rl::kLines - 1) / rl::kLines;
     std::vector<float2> buf((size_t)N * rl::kLines);
     std::vector<float2> regs((size_t)rl::kThreads * E);
+    std::vector<float2> tw_a(rl::Shape<N>::TW);
+    rl::stage_twiddles<N>(p, tw_a.data(), 0, 1);
     for (int blk = 0; blk < blocks; ++blk) {
         auto each = [&](auto&& phase) {
             for (int tid = 0; tid < rl::kThreads; ++tid) {
@@ -33,13 +35,13 @@ void run_pass(const RegLinesParams& p) {
             });
             each([&](int l, int q, const rl::Line& L, float2* v) {
                 rl::read_a<N>(buf.data(), l, q, v);
-                rl::inv_a<N, HOUT>(p, q, v);
+                rl::inv_a<N, HOUT>(tw_a.data(), q, v);
                 rl::store_a<N, HOUT>(p, L, q, v);
             });
         } else {
             each([&](int l, int q, const rl::Line& L, float2* v) {
                 rl::load_a<N, HIN>(p, L, q, v);
-                rl::fwd_a<N, HIN>(p, q, v);
+                rl::fwd_a<N, HIN>(tw_a.data(), q, v);
                 rl::write_a<N>(buf.data(), l, q, v);
             });
             if (MODE == RL_FWD) {
@@ -58,7 +60,7 @@ void run_pass(const RegLinesParams& p) {
                 each([&](int l, int q, const rl::Line&, float2* v) { rl::write_b<N>(buf.data(), l, q, v); });
                 each([&](int l, int q, const rl::Line& L, float2* v) {
                     rl::read_a<N>(buf.data(), l, q, v);
-                    rl::inv_a<N, HOUT>(p, q, v);
+                    rl::inv_a<N, HOUT>(tw_a.data(), q, v);
                     rl::store_a<N, HOUT>(p, L, q, v);
                 });
             }
@@ -82,7 +84,8 @@ int dispatch(const RegLinesParams& p) {
 // mode: 0 forward, 1 inverse, 2 convolution; complex arrays interleaved (re, im) float32.
 extern "C" int rl_host_pass(int mode, int N, const float* in, float* out, int n_lines, int slab_lines,
                             long long slab_stride, long long stride, int n_in, int n_out, const float* tw,
-                            const float* g, long long g_kstride, long long g_mstride, int g_div, int g_mmod) {
+                            const float* g, long long g_kstride, long long g_mstride, int g_div, int g_mmod,
+                            int interleave) {
     RegLinesParams p{};
     p.in = reinterpret_cast<const float2*>(in);
     p.out = reinterpret_cast<float2*>(out);
@@ -98,6 +101,7 @@ extern "C" int rl_host_pass(int mode, int N, const float* in, float* out, int n_
     p.g_mstride = g_mstride;
     p.g_div = g_div;
     p.g_mmod = g_mmod;
+    p.interleave = interleave;
     if (N == 512) {
         if (mode == RL_FWD) return dispatch<512, RL_FWD>(p);
         if (mode == RL_INV) return dispatch<512, RL_INV>(p);

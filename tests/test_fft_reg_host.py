@@ -38,7 +38,7 @@ def lib(tmp_path_factory):
     h.rl_host_pass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
-                               ctypes.c_int, ctypes.c_int]
+                               ctypes.c_int, ctypes.c_int, ctypes.c_int]
     return h
 
 
@@ -48,11 +48,12 @@ def _twiddles(n):
 
 
 def _run(h, mode, N, buf, n_lines, slab_lines, slab_stride, stride, n_in, n_out, table=None,
-         g_kstride=0, g_mstride=0, g_div=1, g_mmod=0):
+         g_kstride=0, g_mstride=0, g_div=1, g_mmod=0, interleave=1):
     tw = _twiddles(N)
     g = table if table is not None else np.zeros(1, np.float32)
     rc = h.rl_host_pass(mode, N, buf.ctypes.data, buf.ctypes.data, n_lines, slab_lines, slab_stride, stride,
-                        n_in, n_out, tw.ctypes.data, g.ctypes.data, g_kstride, g_mstride, g_div, g_mmod)
+                        n_in, n_out, tw.ctypes.data, g.ctypes.data, g_kstride, g_mstride, g_div, g_mmod,
+                        interleave)
     assert rc == 0
 
 
@@ -60,8 +61,10 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("N,ncomp,ny,nx", [(512, 2, 3, 6), (256, 3, 2, 4), (512, 1, 8, 1)])
-def test_z_convolution_pass(lib, N, ncomp, ny, nx):
+@pytest.mark.parametrize("N,ncomp,ny,nx,interleave", [(512, 2, 3, 6, 1), (256, 3, 2, 4, 1), (512, 1, 8, 1, 1),
+                                                       (512, 3, 4, 7, 3), (256, 2, 8, 3, 2)])
+def test_z_convolution_pass(lib, N, ncomp, ny, nx, interleave):
+    """interleave > 1: consecutive blocks take the same lines of consecutive components."""
     rng = np.random.default_rng(N + ny)
     nz = N // 2
     nxp = nx + 1
@@ -80,7 +83,7 @@ def test_z_convolution_pass(lib, N, ncomp, ny, nx):
     ref = (np.fft.ifft(X, axis=1) * N)[:, :nz]
     buf = spec.copy()
     _run(lib, 2, N, buf, ncomp * plane, plane, nz * plane, plane, nz, nz, table,
-         g_kstride=(ny + 1) * nxp, g_mstride=nxp, g_div=nxp, g_mmod=2 * ny)
+         g_kstride=(ny + 1) * nxp, g_mstride=nxp, g_div=nxp, g_mmod=2 * ny, interleave=interleave)
     assert _rel(buf, ref) < 2e-6
 
 
