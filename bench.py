@@ -2,18 +2,20 @@
 
 Workloads (``--workload``, one GPU each; the default is the headline one):
 
+  carpet256  (default) 3D 256^3, fp32, a 4 x 4 carpet of 16 Cosserat rods (100
+             elements, length 0.2, radius 0.005, E = 1e5, density 1) clamped on the
+             plane z0 = 6 dx whose bases turn by 0.2 sin(2 pi t + phase) rad about y
+             (seeded phases), element-centric cosine-delta forcing (K = -2e4, C = -1e2),
+             U = 1 along x, Re = 500 on the rod length.
   rod128     3D unbounded vorticity Navier-Stokes on 128^3, fp32, cubic domain of
-             side 1 (Poisson by domain doubling, 256^3 FFT), one clamped rod of 64
-             elements (length 0.3, radius 0.01) at the domain centre with an
-             element-centric forcing grid and cosine-delta virtual-boundary
-             coupling (K = -2e4, C = -1e2), inflow U = 1, Re = 100 on the rod
-             length, dt from the stable-timestep rule at CFL 0.1.
+             side 1 (Poisson by domain doubling, 256^3 FFT), one clamped Cosserat rod of
+             64 elements (length 0.3, radius 0.01, E = 1e5, density 1) at the domain
+             centre with an element-centric forcing grid and cosine-delta
+             virtual-boundary coupling (K = -2e4, C = -1e2), inflow U = 1, Re = 100 on
+             the rod length.
   cylinder2d 2D 256(y) x 512(x), fp32, x-domain 1, cylinder of diameter 0.1 at
              (0.25, 0.25) with 96 markers, K = -5e4, C = -20, U = 1,
              Re = 200 on the diameter, CFL 0.1.
-  carpet256  3D 256^3, fp32, a 4 x 4 carpet of 16 clamped rods (100 elements,
-             length 0.2, radius 0.005) standing on the plane z0 = 6 dx, one
-             interactor per rod, U = 1 along x, Re = 500 on the rod length.
   batch64    64 2D cylinder flows of uneven sizes (128x256 to 512x1024) and
              Reynolds numbers advanced by the batched persistent launches, against
              the same 64 instances run one after another.
@@ -24,18 +26,21 @@ Workloads (``--workload``, one GPU each; the default is the headline one):
   pointsource256  passive transport (ENO3 advection + diffusion) of a vector point
              source at 256^3, with the reference example's 128^3 run for accuracy.
 
-One step is: stable dt, every interactor's time_step + interaction +
-spreading, then the flow time step.  Rods and the cylinder stay on the host
-(pyelastica's role); they are held at their initial, clamped pose, so the body
-integrator is not part of the timed path in either arm.
+One step of a rod workload is the reference examples' loop
+(flow_past_rod_case.py:231-250): the stable dt with dt_prefac 0.25, the rods
+advanced through it in int(dt / rod_dt) position-Verlet sub-steps with the flow
+forces at each half step (one launch for every rod), the interaction and
+spreading of the final configuration, then the flow time step.  rod_dt is half
+the explicit stability limit of the rods' axial and shear waves, dl sqrt(rho / E).
+The cylinder is held in place.
 
 Arms
   default            this repository's GPU path.
-      value  : device-resident steps/s: a CUDA graph of the whole coupled step
-               (device dt + IB interaction + spread + flow step) replayed K times.
-      e2e    : the same steps through the public Python API, per step uploading
-               the marker kinematics from pinned host memory and reading the
-               Lagrangian forcing back (what a host body integrator needs).
+      value  : device-resident steps/s: a CUDA graph of K whole coupled steps
+               (device dt + rod sub-steps + IB interaction + spread + flow step),
+               replayed until about a second has passed; the median replay.
+      e2e    : the same steps through the public Python API (host dt each step,
+               the Lagrangian forcing read back each step).
   --impl reference   the reference algorithm's CPU implementation (the numpy/
                scipy oracle of this repository, since the reference's own JIT
                dependencies are not installable), all host cores, bounded sample.
@@ -62,33 +67,12 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "flow steps/s & Gcell-updates/s vs plain GPU path at stated FP64-oracle L2 error"
 
-# algorithmic bytes per cell per pass of the fp32 step (read + write)
+# bytes per cell moved by each pass of this fp32 step (read + write), for the per-pass GB/s
 PASSES_3D = {"stencils": 96, "poisson_load": 60, "y_fft": 72, "z_conv": 108, "y_ifft": 72, "x_c2r": 36, "curl": 24}
 PASSES_2D = {"sweep": 24, "poisson_load": 32, "y_conv": 20, "x_c2r": 12, "curl": 12}
-
-
-class RodState:
-    """A straight rod along z with the attributes the forcing grids read."""
-
-    def __init__(self, base, length, radius, n_elem):
-        s = np.linspace(0.0, length, n_elem + 1)
-        self.n_elems = n_elem
-        self.position_collection = np.asarray(base, dtype=np.float64)[:, None] + np.outer([0.0, 0.0, 1.0], s)
-        self.velocity_collection = np.zeros((3, n_elem + 1))
-        area = np.pi * radius**2
-        self.mass = np.full(n_elem + 1, area * length / n_elem)
-        self.mass[[0, -1]] *= 0.5
-        self.lengths = np.full(n_elem, length / n_elem)
-        self.director_collection = np.repeat(np.eye(3)[:, :, None], n_elem, axis=2)
-        self.base = np.asarray(base, dtype=np.float64)
-        self.s = s
-
-    def set_pose(self, theta, theta_dot):
-        """Rigid rotation about the base, in the x-z plane, by theta (rad) at rate theta_dot."""
-        d = np.array([np.sin(theta), 0.0, np.cos(theta)])
-        dd = np.array([np.cos(theta), 0.0, -np.sin(theta)]) * theta_dot
-        self.position_collection[...] = self.base[:, None] + np.outer(d, self.s)
-        self.velocity_collection[...] = np.outer(dd, self.s)
+# compulsory bytes per cell-step of the fused design (fp32): 408 in 3D, 88 in 2D -- the step roofline
+STEP_BYTES = {3: 408, 2: 88}
+ROD_MATERIAL = {"E": 1e5, "density": 1.0, "G": 1e5 / 1.5}  # G = E / (1 + Poisson 0.5), the examples' rule
 
 
 @dataclass
@@ -107,6 +91,13 @@ class Workload:
     n_markers: int = 96
     actuation: dict = None         # rods: {"amplitude", "frequency", "phases"} of a sinusoidal base rotation
     accuracy_checkpoints: tuple = (1, 10, 100)
+    dt_prefac: float = 1.0
+
+    @property
+    def rod_dt(self):
+        """Half the explicit stability limit of the rods' axial and shear waves: 0.5 dl sqrt(rho / E)."""
+        b = self.bodies[0]
+        return 0.5 * (b["length"] / b["n_elem"]) * np.sqrt(ROD_MATERIAL["density"] / ROD_MATERIAL["E"])
 
     @property
     def dim(self):
@@ -144,11 +135,12 @@ def make_workload(name: str) -> Workload:
     if name == "rod128":
         length = 0.3
         return Workload(
-            name, "3D unbounded vorticity NS 128^3 fp32 (256^3 doubled FFT), one clamped rod (64 elements, "
-                  "element-centric cosine-delta forcing), U=1 inflow, Re=100 on rod length, CFL 0.1",
+            name, "3D unbounded vorticity NS 128^3 fp32 (256^3 doubled FFT), one clamped Cosserat rod (64 "
+                  "elements, E 1e5, density 1) integrated on the GPU, element-centric cosine-delta forcing, U=1 "
+                  "inflow, Re=100 on rod length, CFL 0.1 with dt_prefac 0.25",
             (128, 128, 128), 1.0 * length / 100.0, np.array([1.0, 0.0, 0.0]), "rods",
             bodies=[dict(base=(0.5, 0.5, 0.5 - length / 2), length=length, radius=0.01, n_elem=64)],
-            K=-2e4, C=-1e2, accuracy_checkpoints=(1, 10, 100, 500))
+            K=-2e4, C=-1e2, accuracy_checkpoints=(1, 10, 100, 500), dt_prefac=0.25)
     if name == "cylinder2d":
         return Workload(
             name, "2D unbounded vorticity NS 256x512 fp32, cylinder D=0.1 at (0.25, 0.25), 96 markers, "
@@ -167,12 +159,13 @@ def make_workload(name: str) -> Workload:
                                    radius=0.005, n_elem=100))
         phases = np.random.default_rng(42).uniform(0.0, 2 * np.pi, len(bodies))
         return Workload(
-            name, "3D unbounded vorticity NS 256^3 fp32 (512^3 doubled FFT), 4x4 carpet of 16 rods (100 elements "
-                  "each, one interactor per rod) clamped at z0 = 6 dx with a sinusoidal base rotation (frequency 1, "
-                  "amplitude 0.2 rad, seeded phases), U=1 along x, Re=500 on rod length, CFL 0.1",
+            name, "3D unbounded vorticity NS 256^3 fp32 (512^3 doubled FFT), 4x4 carpet of 16 Cosserat rods (100 "
+                  "elements each, E 1e5, density 1) integrated on the GPU, clamped at z0 = 6 dx with bases turning "
+                  "0.2 sin(2 pi t + phase) rad about y (seeded phases), U=1 along x, Re=500 on rod length, CFL 0.1 "
+                  "with dt_prefac 0.25",
             (n, n, n), 1.0 * length / 500.0, np.array([1.0, 0.0, 0.0]), "rods", bodies=bodies, K=-2e4, C=-1e2,
             actuation={"amplitude": 0.2, "frequency": 1.0, "phases": phases},
-            accuracy_checkpoints=tuple(range(20, 201, 20)))
+            accuracy_checkpoints=tuple(range(20, 201, 20)), dt_prefac=0.25)
     raise ValueError(f"unknown workload {name}")
 
 
@@ -263,52 +256,54 @@ def make_gpu_case(wl: Workload, real_t, device):
     sim = Sim(grid_size=wl.grid, x_range=wl.x_range, kinematic_viscosity=wl.nu, cfl=wl.cfl, real_t=real_t,
               with_forcing=True, with_free_stream_flow=True, device=device)
     sim.vorticity_field.copy_(torch.from_numpy(wl.initial_vorticity(real_t)).to(device))
-    inters = []
-    for b in wl.bodies:
-        if wl.kind == "cylinder":
+    if wl.kind == "cylinder":
+        inters = []
+        for b in wl.bodies:
             cyl = sps.Cylinder(b["centre"], base_radius=b["radius"])
             inters.append(sps.RigidBodyFlowInteraction(
                 rigid_body=cyl, eul_grid_forcing_field=sim.eul_grid_forcing_field,
                 eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=wl.K,
                 virtual_boundary_damping_coeff=wl.C, dx=sim.dx, grid_dim=2, real_t=real_t,
                 forcing_grid_cls=sps.CircularCylinderForcingGrid, num_forcing_points=wl.n_markers))
-        else:
-            rod = RodState(b["base"], b["length"], b["radius"], b["n_elem"])
-            inters.append(sps.CosseratRodFlowInteraction(
-                cosserat_rod=rod, eul_grid_forcing_field=sim.eul_grid_forcing_field,
-                eul_grid_velocity_field=sim.velocity_field, virtual_boundary_stiffness_coeff=wl.K,
-                virtual_boundary_damping_coeff=wl.C, dx=sim.dx, grid_dim=3, real_t=real_t,
-                forcing_grid_cls=sps.CosseratRodElementCentricForcingGrid))
-    return sim, inters
-
-
-def actuate(wl, inters, t):
-    """Prescribed base rotation of every rod at time t (the host body update of a coupled loop)."""
-    if not wl.actuation:
-        return
-    a, f = wl.actuation["amplitude"], wl.actuation["frequency"]
-    for inter, phi in zip(inters, wl.actuation["phases"], strict=True):
-        w = 2 * np.pi * f
-        inter.forcing_grid.cosserat_rod.set_pose(a * np.sin(w * t + phi), a * w * np.cos(w * t + phi))
+        return sim, inters
+    m = ROD_MATERIAL
+    rods = [sps.StraightRod(b["n_elem"], b["base"], [0.0, 0.0, 1.0], [1.0, 0.0, 0.0], b["length"], b["radius"],
+                            m["density"], m["E"], shear_modulus=m["G"]) for b in wl.bodies]
+    batch = sps.CosseratRodBatch(rods, clamped=[True] * len(rods), device=device)
+    inter = sps.CosseratRodBatchFlowInteraction(batch, sim.eul_grid_forcing_field, sim.velocity_field, wl.K, wl.C,
+                                                dx=sim.dx, real_t=real_t)
+    if wl.actuation:
+        a = wl.actuation
+        inter.set_base_drive(a["amplitude"], a["frequency"], a["phases"], axis=(0.0, 1.0, 0.0))
+    return sim, [inter]
 
 
 def public_api_step(wl, sim, inters):
     """One coupled step through the drop-in API (the reference example loops' order)."""
-    actuate(wl, inters, sim.time)
-    dt = sim.compute_stable_timestep()
+    dt = sim.compute_stable_timestep(dt_prefac=wl.dt_prefac)
     for inter in inters:
-        inter.time_step(dt=dt)
+        if wl.kind == "rods":
+            inter.advance_rods(dt, wl.rod_dt, flow_time=sim.time)
+        else:
+            inter.time_step(dt=dt)
         inter()
     sim.time_step(dt=dt, free_stream_velocity=wl.u_inf)
+    if wl.kind == "rods":
+        return [inter.lag_grid_forcing_field.cpu() for inter in inters]
     return [inter.lag_grid_forcing_host() for inter in inters]
 
 
-def device_step(wl, sim, inters, events=None):
+def device_step(wl, sim, inters, events=None, rod_event=None, stream=None):
     """The same step with dt on the device (capturable)."""
     from sopht_gb300 import _lib
-    dsc = sim.device_stable_timestep(free_stream_velocity=wl.u_inf, recompute_max=False)
+    dsc = sim.device_stable_timestep(dt_prefac=wl.dt_prefac, free_stream_velocity=wl.u_inf, recompute_max=False)
+    if rod_event is not None:
+        _lib.call("sg_event_record", rod_event.cuda_event, stream.cuda_stream)
     for inter in inters:
-        inter.device_call(dsc)
+        if wl.kind == "rods":
+            inter.device_call(dsc, sim.device_time_slot(), wl.rod_dt)
+        else:
+            inter.device_call(dsc)
     if events is not None:
         arr = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
         _lib.call("sg_flow_set_timing_events", sim._plan, len(events), arr)
@@ -326,8 +321,9 @@ def run_gpu(args, wl: Workload, rank, world):
     device = torch.device("cuda", local)
     rt = np.float32
     sim, inters = make_gpu_case(wl, rt, device)
-    for inter in inters:
-        inter.upload_kinematics()
+    if wl.kind == "cylinder":
+        for inter in inters:
+            inter.upload_kinematics()
     sim.prime_velocity_max()
     stream = torch.cuda.Stream(device)
     torch.cuda.synchronize()
@@ -335,34 +331,38 @@ def run_gpu(args, wl: Workload, rank, world):
         for _ in range(args.warmup):
             device_step(wl, sim, inters)
     torch.cuda.synchronize()
-    seg = min(args.steps, 25)
-    n_seg = max(1, args.steps // seg)
-    steps = seg * n_seg
+    steps = max(1, args.steps)
     pass_names = list(wl.passes)
     n_ev = len(pass_names) + 1
+    seg = min(steps, 25)
     events = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ev)] for _ in range(seg)]
+    rod_events = [torch.cuda.Event(enable_timing=True) for _ in range(seg)]
     with torch.cuda.stream(stream):
-        for ev_list in events:  # torch creates the CUDA events lazily, on first record
+        for ev_list in events + [rod_events]:  # torch creates the CUDA events lazily, on first record
             for e in ev_list:
                 e.record(stream)
     torch.cuda.synchronize()
-    # the timed graph has no timing nodes; a second, instrumented graph of the same steps gives
-    # the per-pass breakdown (event nodes between the passes add a little time of their own)
+    # the timed graph holds exactly K = --steps coupled steps and no timing nodes; a second,
+    # instrumented graph of the same steps gives the per-pass breakdown
     graph = torch.cuda.CUDAGraph()
     graph_inst = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
         stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.graph(graph, stream=stream):
-            for _ in range(seg):
+            for _ in range(steps):
                 device_step(wl, sim, inters)
         with torch.cuda.graph(graph_inst, stream=stream):
             for k in range(seg):
-                device_step(wl, sim, inters, events[k])
+                device_step(wl, sim, inters, events[k], rod_events[k], stream)
     torch.cuda.synchronize()
+    t_probe = time.perf_counter()
     with torch.cuda.stream(stream):
-        graph.replay()  # one untimed replay after capture
+        graph.replay()  # one untimed replay after capture, also sizing the number of timed replays
     torch.cuda.synchronize()
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    probe_s = time.perf_counter() - t_probe
+    replays = int(min(200, max(7, np.ceil(1.5 / max(probe_s, 1e-4)))))
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(replays)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(replays)]
     clocks = ClockSampler(local)
     if world > 1:
         torch.distributed.barrier()
@@ -370,16 +370,17 @@ def run_gpu(args, wl: Workload, rank, world):
     clocks.start()
     t_wall = time.perf_counter()
     with torch.cuda.stream(stream):
-        start.record(stream)
-        for _ in range(n_seg):
+        for r in range(replays):
+            starts[r].record(stream)
             graph.replay()
-        stop.record(stream)
+            stops[r].record(stream)
     torch.cuda.synchronize()
     wall_ms = (time.perf_counter() - t_wall) * 1e3
     clock_info = clocks.stop()
-    elapsed_ms = start.elapsed_time(stop)
-    if elapsed_ms < 0.5 * wall_ms:
-        raise RuntimeError(f"event time {elapsed_ms:.3f} ms disagrees with wall time {wall_ms:.3f} ms")
+    replay_ms = np.array([a.elapsed_time(b) for a, b in zip(starts, stops, strict=True)])
+    if replay_ms.sum() < 0.5 * wall_ms:
+        raise RuntimeError(f"event time {replay_ms.sum():.3f} ms disagrees with wall time {wall_ms:.3f} ms")
+    elapsed_ms = float(np.median(replay_ms))
     if world > 1:
         elapsed_ms = max_over_ranks(elapsed_ms, device)
         torch.distributed.barrier()
@@ -388,6 +389,10 @@ def run_gpu(args, wl: Workload, rank, world):
     torch.cuda.synchronize()
     cells = wl.cells
     kernels = {}
+    if wl.kind == "rods":
+        vals = [rod_events[k].elapsed_time(events[k][0]) for k in range(seg)]
+        kernels["rods_and_ib"] = {"ms": round(float(np.mean(vals)), 5), "launches_timed": len(vals),
+                                  "what": "rod sub-steps (one launch), element markers, interaction, spreading"}
     for i, name in enumerate(pass_names):
         vals = [events[k][i].elapsed_time(events[k][i + 1]) for k in range(seg)]
         ms = float(np.mean(vals))
@@ -398,8 +403,14 @@ def run_gpu(args, wl: Workload, rank, world):
     value = world * steps / (elapsed_ms * 1e-3)
     graph.reset()
     del graph
+    n_sub = None
+    if wl.kind == "rods":
+        dt_now = float(sim.compute_stable_timestep(dt_prefac=wl.dt_prefac))
+        n_sub = int(dt_now / min(dt_now, wl.rod_dt))
+        inters[0].check_markers_in_domain()
+    del sim, inters
 
-    # end to end through the public API: host dt, H2D marker kinematics, D2H forcing
+    # end to end through the public API: host dt, the rod loop, interaction, flow step, forcing read back
     sim_e, inters_e = make_gpu_case(wl, rt, device)
     for _ in range(args.warmup):
         public_api_step(wl, sim_e, inters_e)
@@ -414,8 +425,12 @@ def run_gpu(args, wl: Workload, rank, world):
     if world > 1:
         e2e_s = max_over_ranks(e2e_s, device)
     n_lag = sum(inter.num_lag_nodes for inter in inters_e)
-    h2d = 2 * wl.dim * n_lag * 8
-    d2h = wl.dim * n_lag * 4 + 8
+    if wl.kind == "rods":
+        h2d = 56  # the step's host scalars (dt and prefactors)
+        d2h = 8 + wl.dim * n_lag * 4  # the velocity max for the host dt, the Lagrangian forcing
+    else:
+        h2d = 2 * wl.dim * n_lag * 8 + 56  # marker kinematics, host scalars
+        d2h = 8 + wl.dim * n_lag * 4
     del sim_e, inters_e
 
     accuracy = None
@@ -425,9 +440,12 @@ def run_gpu(args, wl: Workload, rank, world):
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = run_cpu_sample(wl, args.cpu_seconds)
+    others = None
+    if rank == 0 and world == 1 and not args.no_others:
+        others = run_other_configs(args, exclude=wl.name)
     if rank != 0:
         return
-    top = max(kernels, key=lambda k: kernels[k]["ms"])
+    top = max(pass_names, key=lambda k: kernels[k]["ms"])
     hbm = load_peaks().get("hbm_gbs")
     peak = hbm or 6800.0
     algo = wl.passes[top] * cells
@@ -437,35 +455,68 @@ def run_gpu(args, wl: Workload, rank, world):
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "fallback 6800 GB/s",
                 "traffic": traffic_from_profiles(wl.name, top), "algorithmic_bytes_per_launch": algo}
     step_ms = elapsed_ms / steps
-    step_bytes = sum(wl.passes.values()) * cells
-    launches_per_step = 1 + 2 * len(inters) + (9 if wl.dim == 3 else 5)
+    step_bytes = STEP_BYTES[wl.dim] * cells
+    launches_per_step = (2 + (5 if wl.kind == "rods" else 2 * len(wl.bodies)) + (9 if wl.dim == 3 else 5))
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "flow steps/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "gcell_updates_per_s": round(world * cells * steps / (elapsed_ms * 1e-3) / 1e9, 3),
         "config": {"workload": wl.description, "name": wl.name, "grid": list(wl.grid),
-                   "dt_rule": "compute_stable_timestep, CFL 0.1", "bodies": len(wl.bodies),
-                   "body_kinematics": ("sinusoidal base rotation on the host in e2e and the accuracy run; initial "
-                                       "pose in the device-resident graph" if wl.actuation else
-                                       "clamped/fixed pose on the host; body integrator not timed"),
+                   "dt_rule": f"compute_stable_timestep, CFL 0.1, dt_prefac {wl.dt_prefac}",
+                   "bodies": len(wl.bodies),
+                   "body_kinematics": (f"Cosserat rods integrated on the GPU inside the timed step: {n_sub} rod "
+                                       f"sub-steps of at most {wl.rod_dt:.3e} per flow step, flow forces at each "
+                                       "half step" + ("; clamped bases driven by a sinusoidal rotation"
+                                                      if wl.actuation else "; clamped base")
+                                       if wl.kind == "rods" else "cylinder held in place"),
                    "parallelism": "replicas only" if world > 1 else "single GPU",
                    "l2": "no flush: the step working set exceeds the 126 MB L2" if cells * 4 * 20 > 126e6 else
-                         "working set fits in L2 (launch-latency-bound size)"},
+                         "working set fits in L2 (launch-latency-bound size)",
+                   "timing": f"a graph of the {steps} steps replayed {replays} times; the median replay"},
         "roofline": roofline,
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
+                          "bytes_per_cell_step": STEP_BYTES[wl.dim],
                           "achieved_GB_s": round(step_bytes / (step_ms * 1e-3) / 1e9, 1),
                           "frac": round(step_bytes / (step_ms * 1e-3) / 1e9 / peak, 3)},
+        "replay_ms": {"min": round(float(replay_ms.min()), 4), "median": round(float(np.median(replay_ms)), 4),
+                      "max": round(float(replay_ms.max()), 4), "replays": replays},
         "kernels": kernels,
         "e2e": {"value": round(world * steps / e2e_s, 2), "unit": "flow steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "note": "public API per step: host dt (sync), H2D marker positions+velocities, D2H lag forcing"},
+                "note": "public API per step: host dt (sync), the rod loop and interaction, the flow step, the "
+                        "Lagrangian forcing read back"},
         "gpu_launches": launches_per_step * steps,
         "clocks": clock_info,
         "accuracy": accuracy,
         "cpu_baseline": cpu,
+        "other_configs": others,
     }
     print(json.dumps(out), flush=True)
+
+
+def run_other_configs(args, exclude):
+    """The other configurations' own bench lines (device-timed numbers), run as separate processes
+    after the headline measurement, when the run time allows."""
+    out = {}
+    for name in ("rod128", "cylinder2d", "batch64", "adjoint2d"):
+        if name == exclude:
+            continue
+        cmd = [sys.executable, str(Path(__file__).resolve()), "--workload", name, "--steps", "20", "--warmup", "3",
+               "--skip-cpu", "--skip-accuracy", "--no-others", "--adjoint-steps", "200", "--adjoint-cpu-steps", "0"]
+        try:
+            res = subprocess.run(cmd, capture_output=True, text=True, timeout=240)
+            line = [ln for ln in res.stdout.splitlines() if ln.startswith("{")][-1]
+            d = json.loads(line)
+        except Exception as exc:  # noqa: BLE001 - report, do not fail the headline line
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"[:200]}
+            continue
+        keep = {k: d.get(k) for k in ("metric", "value", "unit", "ms_per_step", "gcell_updates_per_s",
+                                      "speedup_vs_sequential", "sequential_plain_gpu", "adjoint_over_forward",
+                                      "step_roofline", "e2e")}
+        keep["config"] = (d.get("config") or {}).get("workload")
+        out[name] = {k: v for k, v in keep.items() if v is not None}
+    return out
 
 
 def _batch_instances(spec, device):
@@ -1079,19 +1130,17 @@ def accuracy_checkpoints(wl, device, checkpoints, cpu_oracle=False):
                                                 "in tests)" + ("; plus the FP64 CPU oracle" if orc else "")}
     t = 0.0
     for step in range(1, max(checkpoints) + 1):
-        dt = float(runs[np.float64][0].compute_stable_timestep())
+        dt = float(runs[np.float64][0].compute_stable_timestep(dt_prefac=wl.dt_prefac))
         for rt, (sim, inters) in runs.items():
-            actuate(wl, inters, t)
             for inter in inters:
-                inter.time_step(dt=dt)
+                if wl.kind == "rods":
+                    inter.advance_rods(dt, wl.rod_dt, flow_time=t)
+                else:
+                    inter.time_step(dt=dt)
                 inter()
             sim.time_step(dt=dt, free_stream_velocity=wl.u_inf)
         if orc:
-            osim, ointers = orc
-            for inter in ointers:
-                inter.time_step(dt)
-                inter()
-            osim.time_step(dt, wl.u_inf)
+            cpu_step(wl, orc[0], orc[1], dt=dt, t=t)
         t += dt
         if step in checkpoints:
             torch.cuda.synchronize()
@@ -1153,31 +1202,52 @@ def make_cpu_case(wl: Workload, real_t=np.float32):
         NavierStokes2DOracle,
         RodElementCentricGridOracle,
     )
+    from oracle.rod import CosseratRod, element_centric_view
     from oracle.threaded import ThreadedNavierStokes3DOracle
     rt = real_t
     # 3D: every sweep on z-slabs across the host cores, bitwise the serial oracle
     Sim = NavierStokes2DOracle if wl.dim == 2 else ThreadedNavierStokes3DOracle
     sim = Sim(wl.grid, wl.x_range, wl.nu, cfl=wl.cfl, real_t=rt, with_forcing=True, with_free_stream_flow=True)
     sim.vorticity_field[...] = wl.initial_vorticity(rt)
-    inters = []
-    for b in wl.bodies:
+    inters, rods = [], []
+    for k, b in enumerate(wl.bodies):
         if wl.kind == "cylinder":
             grid = CircularCylinderOracle(b["centre"], b["radius"], wl.n_markers)
             forces, torques = np.zeros((3, 1)), np.zeros((3, 1))
         else:
-            rod = RodState(b["base"], b["length"], b["radius"], b["n_elem"])
-            grid = RodElementCentricGridOracle(rod)
-            forces, torques = np.zeros((3, rod.n_elems + 1)), np.zeros((3, rod.n_elems))
+            m = ROD_MATERIAL
+            rod = CosseratRod(b["n_elem"], b["base"], [0.0, 0.0, 1.0], [1.0, 0.0, 0.0], b["length"], b["radius"],
+                              m["density"], m["E"], shear_modulus=m["G"])
+            rod.clamp_start()
+            if wl.actuation:
+                a = wl.actuation
+                rod.drive = (a["amplitude"], a["frequency"], float(a["phases"][k]), np.array([0.0, 1.0, 0.0]))
+            rods.append(rod)
+            grid = RodElementCentricGridOracle(element_centric_view(rod))
+            forces, torques = np.zeros((3, rod.n + 1)), np.zeros((3, rod.n))
         inters.append(ImmersedBodyInteractionOracle(sim.eul_grid_forcing_field, sim.velocity_field, forces,
                                                     torques, grid, wl.K, wl.C, sim.dx, wl.dim, real_t=rt))
+    sim.rods = rods
     return sim, inters
 
 
-def cpu_step(wl, sim, inters):
-    dt = sim.compute_stable_timestep()
-    for inter in inters:
-        inter.time_step(dt)
-        inter()
+def cpu_step(wl, sim, inters, dt=None, t=None):
+    """One coupled step of the reference loop on the oracle (the rod loop of flow_past_rod_case.py:
+    231-250 for rod workloads)."""
+    from oracle.rod import coupled_rod_loop
+    if dt is None:
+        dt = sim.compute_stable_timestep(dt_prefac=wl.dt_prefac)
+    if wl.kind == "rods":
+        t0 = sim.time if t is None else t
+        for rod in sim.rods:
+            rod.time = t0
+        coupled_rod_loop(sim.rods, inters, dt, wl.rod_dt)
+        for inter in inters:
+            inter()
+    else:
+        for inter in inters:
+            inter.time_step(dt)
+            inter()
     sim.time_step(dt, wl.u_inf)
 
 
@@ -1196,7 +1266,8 @@ def run_cpu_sample(wl, seconds, max_steps=None):
     return {"value": round(n / el, 4), "unit": "flow steps/s", "cores": cores, "kind": "port",
             "sample": f"{n} coupled steps of the same workload ({wl.name}) after 1 warm-up step ({el:.1f} s), "
                       + ("numpy sweeps on z-slabs across all cores, " if wl.dim == 3 else "numpy sweeps, ")
-                      + "scipy.fft with workers = all cores, fp32"}
+                      + "scipy.fft with workers = all cores, fp32"
+                      + ("; the rods' sub-steps on the numpy rod model" if wl.kind == "rods" else "")}
 
 
 def run_reference(args, wl, rank, world):
@@ -1209,7 +1280,7 @@ def run_reference(args, wl, rank, world):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "ms_per_step": round(1e3 / cpu["value"], 2),
            "config": {"workload": wl.description, "name": wl.name, "grid": list(wl.grid),
-                      "dt_rule": "compute_stable_timestep, CFL 0.1"},
+                      "dt_rule": f"compute_stable_timestep, CFL 0.1, dt_prefac {wl.dt_prefac}"},
            "cpu_baseline": cpu,
            "e2e": {"value": cpu["value"], "unit": "flow steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "the reference's pystencils/pyfftw/numba stack is not installable offline; its algorithm runs "
@@ -1223,7 +1294,7 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rod128",
+    ap.add_argument("--workload", default="carpet256",
                     choices=["rod128", "cylinder2d", "carpet256", "batch64", "adjoint2d", "pointsource256"])
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-cpu-steps", type=int, default=200)
@@ -1231,6 +1302,7 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--no-others", action="store_true", help="skip the other configurations' lines")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload == "batch64":

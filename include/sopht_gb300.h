@@ -96,9 +96,11 @@ int sg_poisson_solve(sg_poisson_plan plan, const void* rhs, void* sol, int ncomp
  * nx <= 512; larger grids return SG_ERR_SHAPE.  The first call on a device
  * (and a call with a new ny, nx or x_range) looks up the array's address and
  * rebuilds the Green's table into it, so make that first call before any
- * stream capture.  All calls share the array: calls whose GPU work overlaps
- * (other streams, other host threads) race and must be serialised by the
- * caller. */
+ * stream capture; a rebuild asked for on a capturing stream returns
+ * SG_ERR_INVALID_ARG and leaves the array as it was.  The array holds the table
+ * of the last grid: a call on a new grid replaces it for every later reader.
+ * All calls share the array: calls whose GPU work overlaps (other streams,
+ * other host threads) race and must be serialised by the caller. */
 int sg_poisson2d_solve_noalloc(int ny, int nx, double x_range, const float* rhs, float* sol,
                                void* stream);
 
@@ -153,6 +155,15 @@ int sg_flow_host_max(sg_flow_plan plan, const void* velocity, double* host_out, 
 int sg_flow_device_dt(sg_flow_plan plan, const void* velocity, double cfl, double nu,
                       double flow_density, double dt_prefac, const double* free_stream,
                       const sg_step_scalars** dev_scalars_out, void* stream);
+/* No reference counterpart: the device address of the plan's accumulated
+ * device time (seconds added by sg_flow_device_dt since the plan was made;
+ * the flow's time is the host time at creation plus this), for kernels that
+ * read the time of the current step on the GPU. */
+int sg_flow_device_time_slot(sg_flow_plan plan, const double** slot_out);
+/* No reference counterpart (measurement hook): records a timing event on
+ * `stream`; while the stream is being captured the record becomes a node of
+ * the graph, so a replay times the work between two such records. */
+int sg_event_record(void* event, void* stream);
 
 /* ----------------------------------------------------- batched 2D instances */
 /* Many independent 2D simulators (uneven grids and Reynolds numbers, one
@@ -554,9 +565,12 @@ typedef struct sg_rod_coupling {
     void* position_mismatch;        /* (3, n_markers) */
     void* lag_forcing;              /* (3, n_markers) */
     double stiffness, damping;      /* K, C after the Lagrangian-spacing rescale */
-    double flow_dt, flow_time;      /* used when dev_scalars is NULL */
+    double flow_dt;                 /* the flow step's dt when dev_scalars is NULL */
+    double flow_time;               /* time at the start of the step; with dev_scalars, the time
+                                       the device time slot counts from */
     const sg_step_scalars* dev_scalars; /* device dt of the flow step, or NULL */
-    const double* dev_time_end;     /* with dev_scalars: device flow time after the step's dt */
+    const double* dev_time_end;     /* with dev_scalars: the device time slot, which already
+                                       holds the end of this step */
     double max_rod_dt;
     double damping_rate;
     const double* drive_phase;      /* (n_rods) device, or NULL */

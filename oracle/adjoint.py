@@ -264,6 +264,48 @@ def _step_recorded(flow: NavierStokes2DOracle, dt, free_stream):
     return w_a, w_b, u_n
 
 
+class frozen_branches:
+    """Context manager holding every ENO3 upwind choice of a rollout to a base trajectory's.
+
+    ``with frozen_branches() as fb: problem.loss(V, nu)`` records the masks of the base run (in call
+    order); later ``with fb.replay(): problem.loss(V + h dV, nu)`` runs with exactly those masks.  The
+    ENO3 flux is discontinuous where u_j = -u_{j+1}, so a finite step can move the flow across an
+    upwind switch; with the branches frozen the forward map is smooth (the map the adjoint
+    differentiates) and central differences converge at O(h^2) at any step size.
+    """
+
+    def __init__(self):
+        self.masks = []
+        self._replay = None
+
+    def __enter__(self):
+        st.BRANCH_HOOK = self._record
+        return self
+
+    def __exit__(self, *exc):
+        st.BRANCH_HOOK = None
+        return False
+
+    def _record(self, mask):
+        self.masks.append(mask.copy())
+        return mask
+
+    def replay(self):
+        outer = self
+
+        class _Replay:
+            def __enter__(self):
+                it = iter(outer.masks)
+                st.BRANCH_HOOK = lambda mask: next(it)
+                return outer
+
+            def __exit__(self, *exc):
+                st.BRANCH_HOOK = None
+                return False
+
+        return _Replay()
+
+
 def interpolate_adj(lag_bar, weights, nearest, eul_shape, dx):
     """Transpose of oracle.ib.interpolate (2D): eul_bar = dx^2 spread(lag_bar)."""
     out = np.zeros(eul_shape)
@@ -271,5 +313,5 @@ def interpolate_adj(lag_bar, weights, nearest, eul_shape, dx):
     return out
 
 
-__all__ = ["DragProblem2D", "curl_adj", "penalise_adj", "diffusion_adj", "eno3_adj", "forcing_curl_adj",
+__all__ = ["DragProblem2D", "frozen_branches", "curl_adj", "penalise_adj", "diffusion_adj", "eno3_adj", "forcing_curl_adj",
            "interpolate_adj", "interpolate"]

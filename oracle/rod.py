@@ -112,6 +112,7 @@ class CosseratRod:
         self.external_torques = np.zeros((3, n))
         self.damping_rate = damping_rate
         self.clamped = None  # (position of node 0, directors of element 0) when clamped
+        self.drive = None  # (amplitude, frequency, phase, unit lab axis) of a clamp that turns the base
         self.time = 0.0
 
     def clamp_start(self) -> None:
@@ -170,18 +171,37 @@ class CosseratRod:
     def _rotate(self, h):
         self.directors = np.einsum("ijk,jlk->ilk", rotation_exp(-h * self.omega), self.directors)
 
-    def _apply_clamp(self):
-        if self.clamped is not None:
-            self.position[:, 0] = self.clamped[0]
-            self.directors[..., 0] = self.clamped[1]
-            self.velocity[:, 0] = 0.0
-            self.omega[:, 0] = 0.0
+    def _clamp_frame(self, t):
+        """Directors and local angular velocity of element 0 at time t: fixed, or turned about the lab
+        axis a by theta(t) = A sin(2 pi f t + phi) (each director d -> R d, so Q0 R^T, and omega =
+        Q (theta' a))."""
+        q0 = self.clamped[1]
+        if self.drive is None:
+            return q0, np.zeros(3)
+        amp, freq, phase, axis = self.drive
+        arg = 2.0 * np.pi * freq * t + phase
+        theta, rate = amp * np.sin(arg), amp * 2.0 * np.pi * freq * np.cos(arg)
+        rot = rotation_exp((theta * np.asarray(axis, float))[:, None])[..., 0]
+        q = q0 @ rot.T
+        return q, q @ (rate * np.asarray(axis, float))
 
-    def step(self, dt: float) -> None:
+    def _apply_clamp(self, t=None):
+        if self.clamped is not None:
+            q, w = self._clamp_frame(self.time if t is None else t)
+            self.position[:, 0] = self.clamped[0]
+            self.directors[..., 0] = q
+            self.velocity[:, 0] = 0.0
+            self.omega[:, 0] = w
+
+    def step(self, dt: float, midpoint_loads=None) -> None:
+        """One position-Verlet step.  ``midpoint_loads(rod)``, when given, sets the external loads from
+        the half-step configuration (pyelastica evaluates its forcing there, inside do_step)."""
         half = 0.5 * dt
         self.position += half * self.velocity
         self._rotate(half)
-        self._apply_clamp()
+        self._apply_clamp(self.time + half)
+        if midpoint_loads is not None:
+            midpoint_loads(self)
         force, couple = self.internal_loads()
         _, _, e, _ = self._geometry()
         self.velocity += dt * (force + self.external_forces) / self.mass
@@ -190,10 +210,10 @@ class CosseratRod:
             decay = np.exp(-self.damping_rate * dt)
             self.velocity *= decay
             self.omega *= decay
-        self._apply_clamp()
+        self._apply_clamp(self.time + half)
         self.position += half * self.velocity
         self._rotate(half)
-        self._apply_clamp()
+        self._apply_clamp(self.time + dt)
         self.time += dt
 
     # ---------------------------------------------------------------- energy
@@ -208,3 +228,57 @@ class CosseratRod:
         kappa = self.curvature() - self.rest_kappa
         strain += 0.5 * np.sum(kappa * _matvec(self.bend_matrix, kappa) * self.rest_voronoi)
         return float(kinetic + strain)
+
+
+class _ElementCentricView:
+    """A rod under the attribute names the element-centric forcing grid reads."""
+
+    def __init__(self, rod):
+        self.rod = rod
+        self.n_elems = rod.n
+
+    @property
+    def position_collection(self):
+        return self.rod.position
+
+    @property
+    def velocity_collection(self):
+        return self.rod.velocity
+
+    @property
+    def mass(self):
+        return self.rod.mass
+
+    @property
+    def lengths(self):
+        return np.linalg.norm(np.diff(self.rod.position, axis=1), axis=0)
+
+
+def coupled_rod_loop(rods, interactors, flow_dt, rod_dt):
+    """The rod loop of one flow step of the reference examples (flow_past_rod_case.py:231-243): each
+    sub-step is one position-Verlet step of every rod with FlowForces.apply_forces (flow_forces.py:
+    22-25: compute_flow_forces_and_torques, then the body forces as the rod's external loads) at the
+    half step, then every interactor's time_step.  ``interactors[i]`` is an
+    ``oracle.flow.ImmersedBodyInteractionOracle`` over ``RodElementCentricGridOracle`` of rod i
+    (wrapped by ``element_centric_view``); the flow forces are the rods' only loads."""
+    n_sub = int(flow_dt / min(flow_dt, rod_dt))
+    h = flow_dt / n_sub
+
+    def loads(inter):
+        def apply(rod):
+            inter.compute_flow_forces_and_torques()
+            rod.external_forces[...] = inter.body_flow_forces
+            rod.external_torques[...] = inter.body_flow_torques
+        return apply
+
+    for _ in range(n_sub):
+        for rod, inter in zip(rods, interactors, strict=True):
+            rod.step(h, midpoint_loads=loads(inter))
+        for inter in interactors:
+            inter.time_step(h)
+    return n_sub
+
+
+def element_centric_view(rod):
+    """``rod`` as the element-centric forcing grid oracle expects it."""
+    return _ElementCentricView(rod)

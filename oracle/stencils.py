@@ -30,6 +30,12 @@ def forcing_curl_update_2d(vorticity, forcing, prefactor):
     ) * prefactor
 
 
+# When set, every ENO3 upwind choice (the boolean mask u_0 > -u_{+1} of a face pass) goes through
+# this callable, which returns the mask to use: ``oracle.adjoint.frozen_branches`` records the masks
+# of a base trajectory and replays them, so that finite differences see one smooth branch of the map.
+BRANCH_HOOK = None
+
+
 def _eno3_face_flux(q_m1, q_0, q_p1, q_p2, u_0, u_p1, real_t):
     """ENO3 flux through the face between cells 0 and +1 along one axis.
 
@@ -38,7 +44,10 @@ def _eno3_face_flux(q_m1, q_0, q_p1, q_p2, u_0, u_p1, real_t):
     third, five6, sixth = real_t(1 / 3), real_t(5 / 6), real_t(1 / 6)
     left = third * q_p1 + five6 * q_0 - sixth * q_m1
     right = third * q_0 + five6 * q_p1 - sixth * q_p2
-    return np.where(u_0 > -u_p1, left, right)
+    mask = u_0 > -u_p1
+    if BRANCH_HOOK is not None:
+        mask = BRANCH_HOOK(mask)
+    return np.where(mask, left, right)
 
 
 def eno3_flux_2d(field, velocity, inv_dx, out=None):

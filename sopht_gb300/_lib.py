@@ -58,6 +58,19 @@ class RodBatch(ctypes.Structure):
         "external_forces", "external_torques", "clamped", "clamp_position", "clamp_directors")]
 
 
+class RodCoupling(ctypes.Structure):
+    """Mirror of ``sg_rod_coupling`` (read on the host)."""
+
+    _fields_ = [("dtype", c_int), ("nz", c_int), ("ny", c_int), ("nx", c_int), ("dx", c_double), ("shift", c_double),
+                ("kernel_type", c_int)] + [(name, c_void_p) for name in (
+                    "flow_velocity", "marker_position", "marker_velocity", "nearest", "weights", "flow_velocity_lag",
+                    "velocity_mismatch", "position_mismatch", "lag_forcing")] + [
+                ("stiffness", c_double), ("damping", c_double), ("flow_dt", c_double), ("flow_time", c_double),
+                ("dev_scalars", c_void_p), ("dev_time_end", c_void_p), ("max_rod_dt", c_double),
+                ("damping_rate", c_double), ("drive_phase", c_void_p), ("drive_amplitude", c_double),
+                ("drive_frequency", c_double), ("drive_axis", c_double * 3), ("status", c_void_p)]
+
+
 _SIGNATURES = {
     "sg_last_error": (c_char_p, []),
     "sg_version": (c_int, []),
@@ -143,6 +156,9 @@ _SIGNATURES = {
     "sg_rod_batch_step": (c_int, [POINTER(RodBatch), c_int, c_double, c_double, c_void_p]),
     "sg_rod_batch_element_markers": (c_int, [POINTER(RodBatch), c_int, c_void_p, c_void_p, c_void_p]),
     "sg_rod_batch_element_loads": (c_int, [POINTER(RodBatch), c_int, c_int, c_void_p, c_void_p]),
+    "sg_rod_batch_coupled_substeps": (c_int, [POINTER(RodBatch), POINTER(RodCoupling), c_void_p]),
+    "sg_flow_device_time_slot": (c_int, [c_void_p, POINTER(c_void_p)]),
+    "sg_event_record": (c_int, [c_void_p, c_void_p]),
     "sg_batch2d_create": (c_int, [c_int, POINTER(Batch2DMember), POINTER(c_void_p)]),
     "sg_batch2d_set_tuning": (c_int, [c_void_p, c_int, c_int, c_int]),
     "sg_batch2d_step": (c_int, [c_void_p, c_void_p]),

@@ -473,6 +473,24 @@ extern "C" int sg_flow_read_device_time(sg_flow_plan p, double* host_out) {
                        "read device time");
 }
 
+extern "C" int sg_event_record(void* event, void* stream_) {
+    SG_REQUIRE(event, SG_ERR_INVALID_ARG, "event record: null event");
+    auto stream = (cudaStream_t)stream_;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e;
+    if (cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        e = cudaEventRecordWithFlags((cudaEvent_t)event, stream, cudaEventRecordExternal);
+    else
+        e = cudaEventRecord((cudaEvent_t)event, stream);
+    return cuda_status(e, "event record");
+}
+
+extern "C" int sg_flow_device_time_slot(sg_flow_plan p, const double** slot_out) {
+    SG_REQUIRE(p && slot_out, SG_ERR_INVALID_ARG, "device time slot: null argument");
+    *slot_out = p->time_slot();
+    return SG_OK;
+}
+
 extern "C" int sg_flow_plan_destroy(sg_flow_plan p) {
     flow_plan_free(p);
     return SG_OK;

@@ -585,6 +585,14 @@ extern "C" int sg_poisson2d_solve_noalloc(int ny, int nx, double x_range, const 
     }
     auto stream = (cudaStream_t)stream_;
     if (!st.table_ready || st.ny != ny || st.nx != nx || st.x_range != x_range) {
+        // A rebuild queued on a capturing stream would only be recorded, not run: refuse it rather
+        // than mark a table ready that no eager work has built.
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        SG_TRY(cuda_status(cudaStreamIsCapturing(stream, &cs), "poisson2d noalloc: capture status"));
+        SG_REQUIRE(cs == cudaStreamCaptureStatusNone, SG_ERR_INVALID_ARG,
+                   "poisson2d noalloc: the grid (%d, %d, x_range %g) needs a table rebuild, which cannot be "
+                   "queued while the stream is capturing; call once on this grid outside capture first",
+                   ny, nx, x_range);
         st.table_ready = false;
         SG_TRY(noalloc_build(st, p, stream));
         st.table_ready = true;

@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
         v.clamp_w = clamp + 9;
     }
     const double dt = c.dev ? c.dev->dt : c.host_dt;
-    const double t0 = c.dev ? *c.dev_time_end - dt : c.host_time;
+    const double t0 = c.dev ? c.host_time + (*c.dev_time_end - dt) : c.host_time;
     const int n_sub = dt > c.max_rod_dt ? (int)(dt / c.max_rod_dt) : 1;
     const double h = dt / n_sub;
     const double decay = c.damping_rate != 0.0 ? exp(-c.damping_rate * h) : 1.0;

@@ -221,6 +221,13 @@ class _UnboundedNavierStokesBase(FlowSimulator):
         """Record max sum_d |u_d| of the current velocity for the first device-resident dt."""
         _lib.call("sg_flow_prime_max", self._plan, ptr(self.velocity_field), stream_ptr(self.device))
 
+    def device_time_slot(self) -> int:
+        """Device address of the time the device-resident dt accumulates (seconds since the plan was
+        made, the end of the current step once its dt is computed)."""
+        out = ctypes.c_void_p()
+        _lib.call("sg_flow_device_time_slot", self._plan, ctypes.byref(out))
+        return out.value
+
     def device_time(self) -> float:
         """Time accumulated on the GPU by the device-resident dt (synchronises)."""
         out = ctypes.c_double()

@@ -27,7 +27,8 @@ import numpy as np
 import torch
 
 from .. import _lib
-from ..utils import default_device, stream_ptr
+from ..numeric.immersed_boundary_ops import KERNEL_TYPES, VirtualBoundaryForcing
+from ..utils import default_device, ptr, sg_dtype, stream_ptr
 
 STATE = ("position_collection", "velocity_collection", "director_collection", "omega_collection")
 MATERIAL = ("mass", "rest_lengths", "rest_voronoi_lengths", "shear_matrix", "bend_matrix",
@@ -200,3 +201,144 @@ class CosseratRodBatch:
         for i, r in enumerate(rods):
             for name in STATE:
                 getattr(r, name)[...] = host[name][i]
+
+
+class CosseratRodBatchFlowInteraction(VirtualBoundaryForcing):
+    """The element-centric forcing grid of every rod of a ``CosseratRodBatch``, in one interactor.
+
+    The reference couples each rod through a ``CosseratRodFlowInteraction`` with a
+    ``CosseratRodElementCentricForcingGrid`` (cosserat_rod_flow_interaction.py:9-58,
+    cosserat_rod_forcing_grids.py:82-130) and integrates it with pyelastica on the host, calling
+    ``FlowForces.apply_forces`` (flow_forces.py:22-25) inside every rod sub-step.  Here the markers of
+    the whole batch (marker r * n + e: element e of rod r) share one set of Lagrangian buffers, the
+    stiffness and damping are rescaled by the largest element length squared as
+    immersed_body_flow_interaction.py:83-86 does for each rod, and the rods stay on the GPU:
+
+    * ``advance_rods(flow_dt, rod_dt)`` is the rod loop of one flow step (flow_past_rod_case.py:231-243):
+      ``int(flow_dt / min(flow_dt, rod_dt))`` sub-steps, each a position-Verlet step whose flow forces
+      are evaluated at the half-step configuration, followed by ``time_step`` of the mismatch -- one
+      launch for every rod;
+    * ``__call__()`` is the interaction and spreading of the final configuration;
+    * ``device_call(dev_scalars, dev_time)`` does both with the flow step's dt and time read on the
+      GPU, for steps captured in a CUDA graph.
+
+    The flow forces are the rods' only external loads (``external_forces`` and ``external_torques`` are
+    overwritten by the reaction each sub-step).  ``set_base_drive`` makes the clamps of clamped rods
+    turn their base about a lab axis by theta(t) = amplitude sin(2 pi frequency t + phase).
+    """
+
+    def __init__(self, rod_batch, eul_grid_forcing_field, eul_grid_velocity_field, virtual_boundary_stiffness_coeff,
+                 virtual_boundary_damping_coeff, dx, real_t=np.float64, eul_grid_coord_shift=None,
+                 interp_kernel_width=None, enable_eul_grid_forcing_reset=False, num_threads=False, start_time=0.0,
+                 interp_kernel_type="cosine"):
+        if not isinstance(eul_grid_forcing_field, torch.Tensor) or not eul_grid_forcing_field.is_cuda:
+            raise ValueError("eul_grid_forcing_field must be the simulator's CUDA tensor")
+        if eul_grid_forcing_field.dim() != 4 or eul_grid_forcing_field.shape[0] != 3:
+            raise ValueError("the rod batch couples to a 3D flow: (3, nz, ny, nx) fields")
+        self.rod_batch = rod_batch
+        pos = rod_batch.arrays["position_collection"]
+        max_len = float(torch.linalg.vector_norm(pos[:, :, 1:] - pos[:, :, :-1], dim=1).max())
+        virtual_boundary_stiffness_coeff *= max_len ** 2
+        virtual_boundary_damping_coeff *= max_len ** 2
+        n_markers = rod_batch.n_rods * rod_batch.n_elems
+        super().__init__(virtual_boundary_stiffness_coeff, virtual_boundary_damping_coeff, 3, dx, n_markers, real_t,
+                         eul_grid_coord_shift, interp_kernel_width, enable_eul_grid_forcing_reset, num_threads,
+                         start_time, interp_kernel_type=interp_kernel_type, device=eul_grid_forcing_field.device)
+        if rod_batch.device != self.device:
+            raise ValueError(f"the rod batch lives on {rod_batch.device}, the flow on {self.device}")
+        self.eul_grid_forcing_field = eul_grid_forcing_field
+        self.eul_grid_velocity_field = eul_grid_velocity_field
+        self.position_field = torch.zeros((3, n_markers), dtype=torch.float64, device=self.device)
+        self.velocity_field = torch.zeros_like(self.position_field)
+        self._drive = None
+        self.compute_lag_grid_kinematics()
+
+    def set_base_drive(self, amplitude, frequency, phases, axis=(0.0, 1.0, 0.0)) -> None:
+        """Clamped rods turn their base by amplitude sin(2 pi frequency t + phases[rod]) about ``axis``."""
+        phases = np.asarray(phases, dtype=np.float64)
+        if phases.shape != (self.rod_batch.n_rods,):
+            raise ValueError(f"one phase per rod ({self.rod_batch.n_rods})")
+        axis = np.asarray(axis, dtype=np.float64)
+        axis = axis / np.linalg.norm(axis)
+        self._drive = (float(amplitude), float(frequency), torch.from_numpy(phases).to(self.device), axis)
+
+    def compute_lag_grid_kinematics(self) -> None:
+        """The element centres and mass-weighted element velocities of every rod (one launch)."""
+        self.rod_batch.element_markers(self.position_field, self.velocity_field, dim=3)
+
+    def __call__(self) -> None:
+        """immersed_body_flow_interaction.py:113-122 for the whole batch."""
+        self.compute_lag_grid_kinematics()
+        self.compute_interaction_forcing(eul_grid_forcing_field=self.eul_grid_forcing_field,
+                                         eul_grid_velocity_field=self.eul_grid_velocity_field,
+                                         lag_grid_position_field=self.position_field,
+                                         lag_grid_velocity_field=self.velocity_field)
+
+    def compute_flow_forces_and_torques(self) -> None:
+        """immersed_body_flow_interaction.py:124-131: the interaction on the markers and its reaction
+        as every rod's external forces (on the device)."""
+        self.compute_lag_grid_kinematics()
+        self.compute_interaction_force_on_lag_grid(self.eul_grid_velocity_field, self.position_field,
+                                                   self.velocity_field)
+        self.rod_batch.set_element_loads(self.lag_grid_forcing_field, dim=3)
+
+    def _coupling(self, flow_dt, flow_time, rod_dt, damping_rate, dev_scalars=None, dev_time=None):
+        u = self.eul_grid_velocity_field
+        if u.dtype != self.lag_grid_forcing_field.dtype or not u.is_contiguous() or tuple(u.shape[:1]) != (3,):
+            raise ValueError("the flow velocity must be a contiguous (3, nz, ny, nx) tensor of real_t")
+        c = _lib.RodCoupling()
+        c.dtype = sg_dtype(self.real_t)
+        c.nz, c.ny, c.nx = (int(x) for x in u.shape[1:])
+        c.dx, c.shift = float(self.dx), float(self.eul_grid_coord_shift)
+        c.kernel_type = KERNEL_TYPES[self.interp_kernel_type]
+        c.flow_velocity = ptr(u)
+        c.marker_position, c.marker_velocity = ptr(self.position_field), ptr(self.velocity_field)
+        c.nearest = ptr(self.nearest_eul_grid_index_to_lag_grid)
+        c.weights = ptr(self.interp_weights)
+        c.flow_velocity_lag = ptr(self.lag_grid_flow_velocity_field)
+        c.velocity_mismatch, c.position_mismatch = ptr(self._du), ptr(self._xi)
+        c.lag_forcing = ptr(self.lag_grid_forcing_field)
+        c.stiffness = float(self.virtual_boundary_stiffness_coeff)
+        c.damping = float(self.virtual_boundary_damping_coeff)
+        c.flow_dt, c.flow_time = float(flow_dt), float(flow_time)
+        c.dev_scalars, c.dev_time_end = dev_scalars, dev_time
+        c.max_rod_dt, c.damping_rate = float(rod_dt), float(damping_rate)
+        if self._drive is not None:
+            amp, freq, phases, axis = self._drive
+            c.drive_phase = phases.data_ptr()
+            c.drive_amplitude, c.drive_frequency = amp, freq
+            c.drive_axis[:] = [float(a) for a in axis]
+        c.status = ptr(self._status)
+        return c
+
+    def advance_rods(self, flow_dt: float, rod_dt: float, flow_time: float = None, damping_rate: float = 0.0) -> int:
+        """The rod loop of one flow step (flow_past_rod_case.py:231-243) for every rod, in one launch;
+        returns the number of rod sub-steps, int(flow_dt / min(flow_dt, rod_dt))."""
+        self._flush_time_step()
+        if flow_time is None:
+            flow_time = self.time
+        c = self._coupling(flow_dt, flow_time, rod_dt, damping_rate)
+        _lib.call("sg_rod_batch_coupled_substeps", ctypes.byref(self.rod_batch._batch), ctypes.byref(c),
+                  stream_ptr(self.device))
+        self.time += flow_dt
+        return int(flow_dt / min(flow_dt, rod_dt))
+
+    def device_call(self, dev_scalars: int, dev_time: int, rod_dt: float, time_origin: float = 0.0,
+                    damping_rate: float = 0.0) -> None:
+        """``advance_rods`` and ``__call__`` with the flow step's dt and time read on the GPU.
+
+        ``dev_scalars`` is the device address ``device_stable_timestep`` returned, ``dev_time`` the
+        flow plan's device time slot (``sg_flow_device_time_slot``) and ``time_origin`` the time it
+        counts from.  Nothing here reads the GPU back, so the call can be captured in a CUDA graph."""
+        self._flush_time_step()
+        c = self._coupling(0.0, time_origin, rod_dt, damping_rate, dev_scalars=dev_scalars, dev_time=dev_time)
+        _lib.call("sg_rod_batch_coupled_substeps", ctypes.byref(self.rod_batch._batch), ctypes.byref(c),
+                  stream_ptr(self.device))
+        self.compute_lag_grid_kinematics()
+        self._interaction(self.eul_grid_velocity_field, self.position_field, self.velocity_field)
+        self._spread(self.eul_grid_forcing_field, reset=self.enable_eul_grid_forcing_reset)
+
+    def get_grid_deviation_error_l2_norm(self) -> float:
+        """immersed_body_flow_interaction.py:133-141."""
+        xi = self.lag_grid_position_mismatch_field.double()
+        return float(torch.linalg.vector_norm(xi).item()) / np.sqrt(self.num_lag_nodes)

@@ -241,7 +241,8 @@ def test_reverse_sweep_equals_operator_composition(width):
 # ---------------------------------------------------------------- step level
 
 
-def _drag_problem(real_t, ny=32, nx=64, n_steps=6, checkpoint_every=4, use_graphs=False, n_mk=24, dt=None):
+def _drag_problem(real_t, ny=32, nx=64, n_steps=6, checkpoint_every=4, use_graphs=False, n_mk=24, dt=None,
+                  radius=0.1, amplitude=0.1):
     """The oracle's tiny drag problem and the same problem on the GPU path."""
     import sopht_gb300.simulator as sps
     from oracle.adjoint import DragProblem2D
@@ -249,7 +250,6 @@ def _drag_problem(real_t, ny=32, nx=64, n_steps=6, checkpoint_every=4, use_graph
     r = np.random.default_rng(42)
     w0 = r.normal(0.0, 1e-3, (ny, nx))
     nu = 5e-4
-    radius = 0.1
     centre = (0.25, 0.5 * ny / nx)
 
     def make_flow():
@@ -263,7 +263,7 @@ def _drag_problem(real_t, ny=32, nx=64, n_steps=6, checkpoint_every=4, use_graph
     dts = [0.1 * dx if dt is None else dt] * n_steps
     prob = DragProblem2D(make_flow, cyl_o.position_field, -5e4 * h, -20.0 * h, dts, (1.0, 0.0))
     theta = np.linspace(0, 2 * np.pi, n_mk, endpoint=False)
-    V = 0.1 * np.stack([-np.sin(theta), np.cos(theta)]) * r.uniform(0, 1, n_mk)
+    V = amplitude * np.stack([-np.sin(theta), np.cos(theta)]) * r.uniform(0, 1, n_mk)
 
     sim = sps.UnboundedNavierStokesFlowSimulator2D((ny, nx), 1.0, nu, real_t=real_t, with_forcing=True,
                                                    with_free_stream_flow=True)
@@ -322,3 +322,32 @@ def test_autograd_function_and_fd_on_gpu():
     hn = 1e-8
     fdn = (obj.forward(Vt.detach(), nu + hn).item() - obj.forward(Vt.detach(), nu - hn).item()) / (2 * hn)
     assert fdn == pytest.approx(gnu, rel=1e-5)
+
+
+def test_gradient_at_the_configuration_step_with_frozen_branches():
+    """The drag gradient of the 256 x 512 cylinder flow (96 markers with a tangential wall velocity of
+    amplitude up to 0.2, 200 frozen-dt steps, checkpoint every 20) on the GPU in FP64, against central
+    differences at the configuration's step h = 1e-3 of the oracle's forward map with every ENO3
+    upwind choice held to the base trajectory's (without that, steps of 1e-3 cross upwind switches and
+    plain differences are off by several per cent): within 1e-3, in two directions and for nu."""
+    from oracle.adjoint import frozen_branches
+    prob, obj, V, nu = _drag_problem(np.float64, ny=256, nx=512, n_steps=200, checkpoint_every=20, n_mk=96,
+                                     dt=1.9e-4, radius=0.05, amplitude=0.2)
+    _, gV, gnu = obj.value_and_grad(torch.as_tensor(V, device="cuda"), nu)
+    gV = gV.cpu().numpy()
+    with frozen_branches() as fb:
+        prob.loss(V, nu)
+    h = 1e-3
+    r = np.random.default_rng(17)
+    for _ in range(2):
+        dV = r.standard_normal(V.shape)
+        with fb.replay():
+            lp = prob.loss(V + h * dV, nu)
+        with fb.replay():
+            lm = prob.loss(V - h * dV, nu)
+        assert (lp - lm) / (2 * h) == pytest.approx(float(np.sum(gV * dV)), rel=1e-3)
+    with fb.replay():
+        lp = prob.loss(V, nu * (1 + h))
+    with fb.replay():
+        lm = prob.loss(V, nu * (1 - h))
+    assert (lp - lm) / (2 * h * nu) == pytest.approx(gnu, rel=1e-3)

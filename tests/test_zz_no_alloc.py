@@ -63,3 +63,27 @@ def test_noalloc_rejects_grids_beyond_its_limit():
                                             torch.cuda.current_stream().cuda_stream)
     assert status == _lib.SG_ERR_SHAPE
     assert b"limit" in lib.sg_last_error()
+
+
+def test_noalloc_grid_changes_rebuild_the_table():
+    """Grids A, B, then A again: each call rebuilds the shared Green's table for its own grid, and
+    each result matches the plan-based solve of that grid."""
+    from sopht_gb300 import _lib
+
+    lib = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    gen = torch.Generator(device="cuda").manual_seed(99)
+    for ny, nx, x_range in ((64, 128, 1.0), (96, 160, 0.8), (64, 128, 1.0)):
+        plan = ctypes.c_void_p()
+        assert lib.sg_poisson_plan_create(2, 1, ny, nx, x_range, _lib.SG_F32, 1, ctypes.byref(plan)) == 0
+        try:
+            rhs = torch.randn((ny, nx), generator=gen, device="cuda", dtype=torch.float32)
+            ref = torch.empty_like(rhs)
+            out = torch.full_like(rhs, float("nan"))
+            assert lib.sg_poisson_solve(plan, rhs.data_ptr(), ref.data_ptr(), 1, 0, stream) == 0
+            assert lib.sg_poisson2d_solve_noalloc(ny, nx, x_range, rhs.data_ptr(), out.data_ptr(), stream) == 0, \
+                lib.sg_last_error()
+            torch.cuda.synchronize()
+            assert _rel_l2(out, ref) < 1e-5, (ny, nx, x_range)
+        finally:
+            lib.sg_poisson_plan_destroy(plan)
