@@ -24,6 +24,8 @@
 // phase by phase (barriers between phases) and check the index arithmetic without a GPU.
 #pragma once
 
+#include <algorithm>
+
 #include "fft_fast.cuh"
 
 #ifdef __CUDACC__
@@ -58,6 +60,9 @@ struct RegLinesParams {
     // components of the z pass share their Green's table rows through L2); needs slab_lines % 16 == 0
     // and n_lines == interleave * slab_lines
     int interleave;
+    // forward and convolution passes with a zero-padded input: the persistent kernel that streams
+    // each block's next line group into shared memory while it transforms the current one
+    int persistent;
 };
 
 enum { RL_FWD = 0, RL_INV = 1, RL_CONV = 2 };
@@ -269,6 +274,31 @@ SG_RL_FN void green_b(const RegLinesParams& p, const Line& L, int t, float2* v) 
         }
 }
 
+// ---- prefetched input of the persistent kernels: stage[n * 16 + l] holds point n < N/2 of line l
+// of the next group, copied asynchronously while the current group is transformed.
+template <int N> struct Pipe {
+    static constexpr int NIN = N / 2;                 // zero-padded input: points >= N/2 are zero
+    static constexpr int COPIES = NIN * kLines / kThreads;  // 8-byte copies per thread
+    static constexpr size_t smem_bytes = Shape<N>::smem_bytes + sizeof(float2) * (size_t)NIN * kLines;
+};
+
+// Copy c of thread tid for line group grp: the destination slot and the source element, or
+// src = -1 where the point is zero (a dead line, or n >= n_in).
+template <int N> SG_RL_FN void stage_copy(const RegLinesParams& p, int grp, int tid, int c, int& slot,
+                                          int64_t& src) {
+    const int idx = tid + c * kThreads;
+    const int l = idx & (kLines - 1), n = idx / kLines;
+    const Line L = line_of(p, grp, l);
+    slot = n * kLines + l;
+    src = (L.live && n < p.n_in) ? L.base + (int64_t)n * p.stride : -1;
+}
+
+template <int N> SG_RL_FN void load_a_staged(const float2* stage, int l, int g, float2* v) {
+    constexpr int E = Shape<N>::E;
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = j < E / 2 ? stage[(g + 16 * j) * kLines + l] : cmake<float2>(0.f, 0.f);
+}
+
 }  // namespace rl
 
 #ifdef __CUDACC__
@@ -314,6 +344,71 @@ __global__ void __launch_bounds__(rl::kThreads, (N == 512 ? 2 : 3)) reg_lines_ke
     }
 }
 
+namespace rl {
+__device__ __forceinline__ void cp_async8(float2* dst, const float2* src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <int N> __device__ __forceinline__ void prefetch(const RegLinesParams& p, int grp, float2* stage) {
+#pragma unroll
+    for (int c = 0; c < Pipe<N>::COPIES; ++c) {
+        int slot;
+        int64_t src;
+        stage_copy<N>(p, grp, threadIdx.x, c, slot, src);
+        cp_async8(stage + slot, p.in + (src < 0 ? 0 : src), src >= 0);
+    }
+    cp_async_commit();
+}
+}  // namespace rl
+
+// Persistent form of the forward and convolution passes with a zero-padded input (n_in <= N/2):
+// each block walks line groups grp = blockIdx.x, blockIdx.x + gridDim.x, ..., and while it
+// transforms one group the input of its next group streams into shared memory with cp.async, so
+// the global-load latency is hidden behind the arithmetic instead of stalling every block at its
+// start.  The arithmetic is the per-block kernel's, phase for phase.
+template <int N, int MODE, bool HOUT>
+__global__ void __launch_bounds__(rl::kThreads, 2) reg_lines_pipe_kernel(RegLinesParams p, int n_groups) {
+    static_assert(MODE != RL_INV, "the persistent form prefetches a zero-padded input");
+    extern __shared__ __align__(16) float2 rl_buf[];
+    float2* tw_a = rl_buf + N * rl::kLines;
+    float2* stage = tw_a + rl::Shape<N>::TW;
+    const int tid = threadIdx.x, l = tid & (rl::kLines - 1), q = tid / rl::kLines;
+    float2 v[rl::Shape<N>::E];
+    int grp = blockIdx.x;
+    if (grp < n_groups) rl::prefetch<N>(p, grp, stage);
+    rl::stage_twiddles<N>(p, tw_a, tid, rl::kThreads);
+    for (; grp < n_groups; grp += gridDim.x) {
+        const rl::Line L = rl::line_of(p, grp, l);
+        rl::cp_async_wait_all();
+        __syncthreads();  // this group's input (and, first time, the twiddles) in place
+        rl::load_a_staged<N>(stage, l, q, v);
+        __syncthreads();  // the stage is free for the next group
+        if (grp + (int)gridDim.x < n_groups) rl::prefetch<N>(p, grp + gridDim.x, stage);
+        rl::fwd_a<N, true>(tw_a, q, v);
+        rl::write_a<N>(rl_buf, l, q, v);
+        __syncthreads();
+        rl::read_b<N>(rl_buf, l, q, v);
+        rl::dft_b<N, false>(v);
+        if constexpr (MODE == RL_FWD) {
+            rl::store_b<N>(p, L, q, v);
+        } else {
+            rl::green_b<N>(p, L, q, v);
+            rl::dft_b<N, true>(v);
+            __syncthreads();
+            rl::write_b<N>(rl_buf, l, q, v);
+            __syncthreads();
+            rl::read_a<N>(rl_buf, l, q, v);
+            rl::inv_a<N, HOUT>(tw_a, q, v);
+            rl::store_a<N, HOUT>(p, L, q, v);
+        }
+    }
+    rl::cp_async_wait_all();  // nothing left in flight when the block exits
+}
+
 // Launches the pass when N is one of the register lengths; returns SG_ERR_UNSUPPORTED otherwise so
 // the caller can take the shared-memory kernels.
 template <int MODE>
@@ -339,6 +434,28 @@ int launch_reg_lines(const RegLinesParams& p, int N, cudaStream_t stream) {
         if (hin) return run(reg_lines_kernel<NN, MODE, MODE != RL_INV, false>, smem);                      \
         if (hout) return run(reg_lines_kernel<NN, MODE, false, MODE != RL_FWD>, smem);                     \
         return run(reg_lines_kernel<NN, MODE, false, false>, smem);                                         \
+    }
+    if constexpr (MODE != RL_INV) if (hin && p.persistent) {
+        // one block per pair of resident slots: the grid is sized to the GPU, not to the lines
+        auto run_pipe = [&](auto kern, size_t smem) -> int {
+            SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                               "register lines smem attribute"));
+            SG_TRY(fast_max_carveout(kern, "register lines carveout attribute"));
+            int dev = 0, sms = 0, per_sm = 0;
+            SG_TRY(cuda_status(cudaGetDevice(&dev), "register lines device"));
+            SG_TRY(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
+            SG_TRY(cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, rl::kThreads, smem),
+                               "register lines occupancy"));
+            const int grid = (int)std::min<long long>((long long)sms * (per_sm > 0 ? per_sm : 1), blocks);
+            kern<<<grid, rl::kThreads, smem, stream>>>(p, (int)blocks);
+            return launch_status("register lines (persistent)");
+        };
+        if (N == 512)
+            return hout ? run_pipe(reg_lines_pipe_kernel<512, MODE, MODE != RL_FWD>, rl::Pipe<512>::smem_bytes)
+                        : run_pipe(reg_lines_pipe_kernel<512, MODE, false>, rl::Pipe<512>::smem_bytes);
+        if (N == 256)
+            return hout ? run_pipe(reg_lines_pipe_kernel<256, MODE, MODE != RL_FWD>, rl::Pipe<256>::smem_bytes)
+                        : run_pipe(reg_lines_pipe_kernel<256, MODE, false>, rl::Pipe<256>::smem_bytes);
     }
     if (N == 512) SG_RL_PICK(512)
     if (N == 256) SG_RL_PICK(256)

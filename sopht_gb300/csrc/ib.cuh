@@ -9,22 +9,16 @@
 
 namespace sg {
 
-// numpy floor_divide for doubles (divmod-based: fmod, exact quotient
-// adjustment, then floor with a round-to-nearest correction).
+// numpy's floor_divide of doubles (b > 0): the exact floor of the real quotient a / b.  numpy
+// forms it from fmod (an exact remainder) and a rounding correction; here the rounded quotient's
+// floor is corrected by the signs of two exactly rounded remainders a - q b (fused multiply-adds
+// keep the sign of the exact value), which needs no fmod loop -- the double-precision pipe of
+// this GPU is narrow, and the IB kernels evaluate this once per marker axis.
 __device__ __forceinline__ double np_floor_divide(double a, double b) {
-    double mod = fmod(a, b);
-    double div = (a - mod) / b;
-    if (mod != 0.0) {
-        if ((b < 0) != (mod < 0)) div -= 1.0;
-    }
-    double fl;
-    if (div != 0.0) {
-        fl = floor(div);
-        if (div - fl > 0.5) fl += 1.0;
-    } else {
-        fl = copysign(0.0, a / b);
-    }
-    return fl;
+    double q = floor(a / b);
+    if (fma(-q, b, a) < 0.0) q -= 1.0;
+    else if (fma(-(q + 1.0), b, a) >= 0.0) q += 1.0;
+    return q;
 }
 
 template <typename T> __device__ __forceinline__ T dev_cos(T x);

@@ -111,22 +111,33 @@ SG_ROD_FN Scratch carve(double* base, int n) {
 
 // ---------------------------------------------------------------- rotations
 
-// exp([a]x) by Rodrigues' formula, row-major 3x3.
+// exp([a]x) by Rodrigues' formula, row-major 3x3: I + (sin t / t) [a]x + ((1 - cos t) / t^2) [a]x^2,
+// t = |a|.  The rotations of a sub-step are small (t = |omega| dt / 2), and for t < 0.1 both
+// coefficients come from their Taylor series in t^2 (the omitted terms are below 3e-18 relative):
+// no square root, division, sine or cosine, which cost tens of operations each on this GPU's
+// narrow double-precision pipe.
 SG_ROD_FN void rotation_exp(const double a[3], double r[9]) {
-    const double theta = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-    const double safe = theta < 1e-12 ? 1.0 : theta;
-    const double k0 = a[0] / safe, k1 = a[1] / safe, k2 = a[2] / safe;
-    const double s = sin(theta), c1 = 1.0 - cos(theta);
-    const double kx[9] = {0.0, -k2, k1, k2, 0.0, -k0, -k1, k0, 0.0};
+    const double t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    double sa, ca;  // sin t / t and (1 - cos t) / t^2
+    if (t2 < 0.01) {
+        sa = 1.0 + t2 * (-1.0 / 6.0 + t2 * (1.0 / 120.0 + t2 * (-1.0 / 5040.0 + t2 * (1.0 / 362880.0))));
+        ca = 0.5 + t2 * (-1.0 / 24.0 + t2 * (1.0 / 720.0 + t2 * (-1.0 / 40320.0 + t2 * (1.0 / 3628800.0))));
+    } else {
+        const double t = sqrt(t2);
+        sa = sin(t) / t;
+        ca = (1.0 - cos(t)) / t2;
+    }
+    const double ax[9] = {0.0, -a[2], a[1], a[2], 0.0, -a[0], -a[1], a[0], 0.0};
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
-            double k2ij = 0.0;
-            for (int m = 0; m < 3; ++m) k2ij += kx[i * 3 + m] * kx[m * 3 + j];
-            r[i * 3 + j] = (i == j ? 1.0 : 0.0) + s * kx[i * 3 + j] + c1 * k2ij;
+            double a2ij = 0.0;
+            for (int m = 0; m < 3; ++m) a2ij += ax[i * 3 + m] * ax[m * 3 + j];
+            r[i * 3 + j] = (i == j ? 1.0 : 0.0) + sa * ax[i * 3 + j] + ca * a2ij;
         }
 }
 
-// The rotation vector of r (angle below pi).
+// The rotation vector of r (angle below pi), the angle taken from the trace as the rod model does
+// (the trace and the antisymmetric part give different angles once r drifts from orthogonality).
 SG_ROD_FN void rotation_log(const double r[9], double a[3]) {
     double cosv = (r[0] + r[4] + r[8] - 1.0) / 2.0;
     cosv = cosv < -1.0 ? -1.0 : (cosv > 1.0 ? 1.0 : cosv);
@@ -216,16 +227,18 @@ SG_ROD_FN void element_pass(const View& r, const Scratch& s, int e) {
     const int n = r.n, nn = n + 1;
     double d[3], t[3], qt[3], sig[3], stress[3];
     for (int a = 0; a < 3; ++a) d[a] = r.x[a * nn + e + 1] - r.x[a * nn + e];
+    // divisions by their reciprocals: a double division is an iteration of many operations here
     const double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    for (int a = 0; a < 3; ++a) t[a] = d[a] / len;
-    const double dil = len / r.l0[e];
+    const double inv_len = 1.0 / len, inv_l0 = 1.0 / r.l0[e];
+    for (int a = 0; a < 3; ++a) t[a] = d[a] * inv_len;
+    const double dil = len * inv_l0, inv_dil = 1.0 / dil;
     matvec(r.q, n, e, t, qt);
     for (int a = 0; a < 3; ++a) sig[a] = dil * qt[a] - (a == 2 ? 1.0 : 0.0) - r.sigma0[a * n + e];
     matvec(r.shear, n, e, sig, stress);
     for (int a = 0; a < 3; ++a) {  // Q^T n / e
         double acc = 0.0;
         for (int b = 0; b < 3; ++b) acc += r.q[(b * 3 + a) * n + e] * stress[b];
-        s.nlab[a * n + e] = acc / dil;
+        s.nlab[a * n + e] = acc * inv_dil;
     }
     double sc[3];
     cross(qt, stress, sc);
@@ -236,10 +249,10 @@ SG_ROD_FN void element_pass(const View& r, const Scratch& s, int e) {
     cross(jw, w, tr);
     double rate = 0.0;
     for (int a = 0; a < 3; ++a) rate += t[a] * (r.v[a * nn + e + 1] - r.v[a * nn + e]);
-    rate /= r.l0[e];
+    rate *= inv_l0;
     for (int a = 0; a < 3; ++a) {
-        s.transport[a * n + e] = tr[a] / dil;
-        s.dil_c[a * n + e] = jw[a] / (dil * dil) * rate;
+        s.transport[a * n + e] = tr[a] * inv_dil;
+        s.dil_c[a * n + e] = jw[a] * (inv_dil * inv_dil) * rate;
     }
     s.e[e] = dil;
     s.len[e] = len;
@@ -255,26 +268,28 @@ SG_ROD_FN void voronoi_pass(const View& r, const Scratch& s, int k) {
             rel[i * 3 + j] = acc;
         }
     rotation_log(rel, lg);
-    for (int a = 0; a < 3; ++a) kappa[a] = -lg[a] / r.d0[k];
-    const double eps = 0.5 * (s.len[k + 1] + s.len[k]) / r.d0[k];
-    const double eps3 = eps * eps * eps;
+    const double inv_d0 = 1.0 / r.d0[k];
+    for (int a = 0; a < 3; ++a) kappa[a] = -lg[a] * inv_d0;
+    const double eps = 0.5 * (s.len[k + 1] + s.len[k]) * inv_d0;
+    const double inv_eps3 = 1.0 / (eps * eps * eps);
     double dk[3];
     for (int a = 0; a < 3; ++a) dk[a] = kappa[a] - r.kappa0[a * nv + k];
     matvec(r.bend, nv, k, dk, m);
     cross(kappa, m, km);
     for (int a = 0; a < 3; ++a) {
-        s.bend_c[a * nv + k] = m[a] / eps3;
-        s.twist_c[a * nv + k] = km[a] * r.d0[k] / eps3;
+        s.bend_c[a * nv + k] = m[a] * inv_eps3;
+        s.twist_c[a * nv + k] = km[a] * r.d0[k] * inv_eps3;
     }
 }
 
 SG_ROD_FN void node_update(View& r, const Scratch& s, int i, double dt, double decay) {
     const int n = r.n, nn = n + 1;
+    const double inv_m = 1.0 / r.mass[i];
     for (int a = 0; a < 3; ++a) {
         double f = 0.0;
         if (i < n) f += s.nlab[a * n + i];
         if (i > 0) f -= s.nlab[a * n + i - 1];
-        r.v[a * nn + i] += dt * (f + r.f_ext[a * nn + i]) / r.mass[i];
+        r.v[a * nn + i] += dt * (f + r.f_ext[a * nn + i]) * inv_m;
         r.v[a * nn + i] *= decay;
     }
     if (r.clamped && i == 0) clamp_node0(r);

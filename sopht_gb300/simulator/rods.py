@@ -118,6 +118,8 @@ class CosseratRodBatch:
             raise ValueError("rods of 1 to 1024 elements")
         self.n_rods, self.n_elems = len(rods), n
         self.device = torch.device(device) if device is not None else default_device()
+        if self.device.type == "cuda" and self.device.index is None:  # tensors report their device index
+            self.device = torch.device("cuda", torch.cuda.current_device())
         self.arrays = {}
         for name in STATE + MATERIAL + LOADS:
             host = np.stack([np.asarray(getattr(r, name), dtype=np.float64) for r in rods])
