@@ -339,6 +339,18 @@ int sg_ib_interaction(int dtype, int dim, int nz, int ny, int nx, double dx, dou
 int sg_ib_spread(int dtype, int dim, int nz, int ny, int nx, int n_lag,
                  const int32_t* nearest, const void* weights, const void* forcing,
                  void* eul_forcing, int reset, void* stream);
+/* The same spreading for many markers, in O(n log n): every (marker, window
+ * cell) pair keyed by its cell, a stable radix sort by key, then one thread per
+ * cell summing its pairs in ascending marker order -- the sums are bitwise
+ * those of sg_ib_spread, whose owner test scans the lower-index markers and so
+ * grows quadratically (surface grids, batch-wide rod grids).  `scratch` is
+ * caller-owned device memory of sg_ib_spread_sorted_scratch_bytes bytes (< 0:
+ * unsupported sizes); the call allocates nothing. */
+int64_t sg_ib_spread_sorted_scratch_bytes(int dim, int nz, int ny, int nx, int n_lag);
+int sg_ib_spread_sorted(int dtype, int dim, int nz, int ny, int nx, int n_lag,
+                        const int32_t* nearest, const void* weights, const void* forcing,
+                        void* eul_forcing, int reset, void* scratch, int64_t scratch_bytes,
+                        void* stream);
 /* VirtualBoundaryForcing.time_step (:276-283): xi += dt * dU. */
 int sg_ib_mismatch_step(int dtype, int n, void* position_mismatch,
                         const void* velocity_mismatch, double dt, void* stream);

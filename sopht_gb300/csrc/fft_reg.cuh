@@ -24,8 +24,6 @@
 // phase by phase (barriers between phases) and check the index arithmetic without a GPU.
 #pragma once
 
-#include <algorithm>
-
 #include "fft_fast.cuh"
 
 #ifdef __CUDACC__
@@ -60,9 +58,6 @@ struct RegLinesParams {
     // components of the z pass share their Green's table rows through L2); needs slab_lines % 16 == 0
     // and n_lines == interleave * slab_lines
     int interleave;
-    // forward and convolution passes with a zero-padded input: the persistent kernel that streams
-    // each block's next line group into shared memory while it transforms the current one
-    int persistent;
 };
 
 enum { RL_FWD = 0, RL_INV = 1, RL_CONV = 2 };
@@ -274,34 +269,106 @@ SG_RL_FN void green_b(const RegLinesParams& p, const Line& L, int t, float2* v) 
         }
 }
 
-// ---- prefetched input of the persistent kernels: stage[n * 16 + l] holds point n < N/2 of line l
-// of the next group, copied asynchronously while the current group is transformed.
-template <int N> struct Pipe {
-    static constexpr int NIN = N / 2;                 // zero-padded input: points >= N/2 are zero
-    static constexpr int COPIES = NIN * kLines / kThreads;  // 8-byte copies per thread
-    static constexpr size_t smem_bytes = Shape<N>::smem_bytes + sizeof(float2) * (size_t)NIN * kLines;
+// ---- rows: the x pass's complex-to-real transform (M = 256 complex points of a 512-real row), 16
+// rows per block, 16 threads per row.  Thread (row, t) reads bins k = t + 16 k1 and M - k, forms
+// the packed spectrum Z[k] of the half-length transform, takes the inverse length-16 DFTs over k1,
+// one exchange ([g][row][k2], a one-point pad per g so the stage-A reads hit distinct banks), and
+// thread (row, g) finishes the inverse over k2 with the twiddles w_M^(-g k2), holding z[g + 16 j]
+// = x[2n] + i x[2n+1], n = g + 16 j.  Only n < n_out / 2 is stored (the crop).
+constexpr int kRowM = 256;
+SG_RL_FN int row_slot(int g, int row, int k2) { return g * (kLines * 16 + 1) + row * 16 + k2; }
+constexpr int kRowSlots = 16 * (kLines * 16 + 1);
+
+struct RowLine {
+    int64_t in_off, out_off;
+    bool live;
 };
 
-// Copy c of thread tid for line group grp: the destination slot and the source element, or
-// src = -1 where the point is zero (a dead line, or n >= n_in).
-template <int N> SG_RL_FN void stage_copy(const RegLinesParams& p, int grp, int tid, int c, int& slot,
-                                          int64_t& src) {
-    const int idx = tid + c * kThreads;
-    const int l = idx & (kLines - 1), n = idx / kLines;
-    const Line L = line_of(p, grp, l);
-    slot = n * kLines + l;
-    src = (L.live && n < p.n_in) ? L.base + (int64_t)n * p.stride : -1;
+SG_RL_FN RowLine row_of(const RowsC2RParams<float>& p, int block, int row) {
+    RowLine R;
+    const int q = block * kLines + row;
+    R.live = q < p.n_rows;
+    R.in_off = R.live ? p.in_map.offset(q) : 0;
+    R.out_off = R.live ? p.out_map.offset(q) : 0;
+    return R;
 }
 
-template <int N> SG_RL_FN void load_a_staged(const float2* stage, int l, int g, float2* v) {
-    constexpr int E = Shape<N>::E;
+// w_M^(g k2) for the row transform: tw_m[m] = exp(-2 pi i m / M).
+SG_RL_FN void stage_row_twiddles(const RowsC2RParams<float>& p, float2* tw_a, int tid, int nt) {
+    for (int i = tid; i < 256; i += nt) tw_a[i] = p.tw_m[(i / 16) * (i % 16)];
+}
+
+SG_RL_FN void c2r_load_b(const RowsC2RParams<float>& p, const RowLine& R, int t, float2* v) {
 #pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = j < E / 2 ? stage[(g + 16 * j) * kLines + l] : cmake<float2>(0.f, 0.f);
+    for (int k1 = 0; k1 < 16; ++k1) {
+        const int k = t + 16 * k1;
+        v[k1] = cmake<float2>(0.f, 0.f);
+        if (!R.live) continue;
+        float2 xk = p.in[R.in_off + k];
+        float2 xm = p.in[R.in_off + kRowM - k];
+        if (k == 0) {
+            xk.y = 0.f;
+            xm.y = 0.f;
+        }
+        const float2 xc = cconj(xm);
+        float2 w = p.tw_l[k];
+        w.y = -w.y;
+        const float2 sm = cadd(xk, xc);
+        const float2 wd = cmul(w, csub(xk, xc));
+        v[k1] = cmake<float2>(sm.x - wd.y, sm.y + wd.x);
+    }
+}
+
+SG_RL_FN void c2r_write_b(float2* buf, int row, int t, const float2* v) {
+#pragma unroll
+    for (int gg = 0; gg < 16; ++gg) buf[row_slot(gg, row, t)] = v[gg];
+}
+
+SG_RL_FN void c2r_read_a(const float2* buf, int row, int g, float2* v) {
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) v[k2] = buf[row_slot(g, row, k2)];
+}
+
+SG_RL_FN void c2r_inv_a(const float2* tw_a, int g, float2* v) {
+#pragma unroll
+    for (int k2 = 1; k2 < 16; ++k2) v[k2] = cmul(v[k2], cconj(tw_a[g * 16 + k2]));
+    dft16<true>(v);
+}
+
+SG_RL_FN void c2r_store_a(const RowsC2RParams<float>& p, const RowLine& R, int g, const float2* v) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int n = g + 16 * j;
+        if (R.live && 2 * n < p.n_out) *reinterpret_cast<float2*>(p.out + R.out_off + 2 * n) = v[j];
+    }
 }
 
 }  // namespace rl
 
 #ifdef __CUDACC__
+// The x pass's complex-to-real rows (M = 256, n_out <= M reals kept) in registers.
+__global__ void __launch_bounds__(rl::kThreads, 3) reg_rows_c2r_kernel(RowsC2RParams<float> p) {
+    __shared__ __align__(16) float2 buf[rl::kRowSlots];
+    __shared__ __align__(16) float2 tw_a[256];
+    const int tid = threadIdx.x, row = tid / 16, q = tid & 15;
+    const rl::RowLine R = rl::row_of(p, blockIdx.x, row);
+    float2 v[16];
+    rl::stage_row_twiddles(p, tw_a, tid, rl::kThreads);
+    rl::c2r_load_b(p, R, q, v);
+    dft16<true>(v);
+    rl::c2r_write_b(buf, row, q, v);
+    __syncthreads();
+    rl::c2r_read_a(buf, row, q, v);
+    rl::c2r_inv_a(tw_a, q, v);
+    rl::c2r_store_a(p, R, q, v);
+}
+
+inline int launch_reg_rows_c2r(const RowsC2RParams<float>& p, cudaStream_t stream) {
+    if (p.n_rows <= 0) return SG_OK;
+    reg_rows_c2r_kernel<<<ceil_div(p.n_rows, rl::kLines), rl::kThreads, 0, stream>>>(p);
+    return launch_status("register rows c2r");
+}
+
 // One pass over 16 lines per block.  RL_FWD: forward transform, spectrum stored (HIN prunes a
 // zero upper input half).  RL_INV: inverse transform of a full spectrum (HOUT keeps the lower
 // output half).  RL_CONV: forward, Green's factor, inverse, in registers between the exchanges.
@@ -344,71 +411,6 @@ __global__ void __launch_bounds__(rl::kThreads, (N == 512 ? 2 : 3)) reg_lines_ke
     }
 }
 
-namespace rl {
-__device__ __forceinline__ void cp_async8(float2* dst, const float2* src, bool valid) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-template <int N> __device__ __forceinline__ void prefetch(const RegLinesParams& p, int grp, float2* stage) {
-#pragma unroll
-    for (int c = 0; c < Pipe<N>::COPIES; ++c) {
-        int slot;
-        int64_t src;
-        stage_copy<N>(p, grp, threadIdx.x, c, slot, src);
-        cp_async8(stage + slot, p.in + (src < 0 ? 0 : src), src >= 0);
-    }
-    cp_async_commit();
-}
-}  // namespace rl
-
-// Persistent form of the forward and convolution passes with a zero-padded input (n_in <= N/2):
-// each block walks line groups grp = blockIdx.x, blockIdx.x + gridDim.x, ..., and while it
-// transforms one group the input of its next group streams into shared memory with cp.async, so
-// the global-load latency is hidden behind the arithmetic instead of stalling every block at its
-// start.  The arithmetic is the per-block kernel's, phase for phase.
-template <int N, int MODE, bool HOUT>
-__global__ void __launch_bounds__(rl::kThreads, 2) reg_lines_pipe_kernel(RegLinesParams p, int n_groups) {
-    static_assert(MODE != RL_INV, "the persistent form prefetches a zero-padded input");
-    extern __shared__ __align__(16) float2 rl_buf[];
-    float2* tw_a = rl_buf + N * rl::kLines;
-    float2* stage = tw_a + rl::Shape<N>::TW;
-    const int tid = threadIdx.x, l = tid & (rl::kLines - 1), q = tid / rl::kLines;
-    float2 v[rl::Shape<N>::E];
-    int grp = blockIdx.x;
-    if (grp < n_groups) rl::prefetch<N>(p, grp, stage);
-    rl::stage_twiddles<N>(p, tw_a, tid, rl::kThreads);
-    for (; grp < n_groups; grp += gridDim.x) {
-        const rl::Line L = rl::line_of(p, grp, l);
-        rl::cp_async_wait_all();
-        __syncthreads();  // this group's input (and, first time, the twiddles) in place
-        rl::load_a_staged<N>(stage, l, q, v);
-        __syncthreads();  // the stage is free for the next group
-        if (grp + (int)gridDim.x < n_groups) rl::prefetch<N>(p, grp + gridDim.x, stage);
-        rl::fwd_a<N, true>(tw_a, q, v);
-        rl::write_a<N>(rl_buf, l, q, v);
-        __syncthreads();
-        rl::read_b<N>(rl_buf, l, q, v);
-        rl::dft_b<N, false>(v);
-        if constexpr (MODE == RL_FWD) {
-            rl::store_b<N>(p, L, q, v);
-        } else {
-            rl::green_b<N>(p, L, q, v);
-            rl::dft_b<N, true>(v);
-            __syncthreads();
-            rl::write_b<N>(rl_buf, l, q, v);
-            __syncthreads();
-            rl::read_a<N>(rl_buf, l, q, v);
-            rl::inv_a<N, HOUT>(tw_a, q, v);
-            rl::store_a<N, HOUT>(p, L, q, v);
-        }
-    }
-    rl::cp_async_wait_all();  // nothing left in flight when the block exits
-}
-
 // Launches the pass when N is one of the register lengths; returns SG_ERR_UNSUPPORTED otherwise so
 // the caller can take the shared-memory kernels.
 template <int MODE>
@@ -434,28 +436,6 @@ int launch_reg_lines(const RegLinesParams& p, int N, cudaStream_t stream) {
         if (hin) return run(reg_lines_kernel<NN, MODE, MODE != RL_INV, false>, smem);                      \
         if (hout) return run(reg_lines_kernel<NN, MODE, false, MODE != RL_FWD>, smem);                     \
         return run(reg_lines_kernel<NN, MODE, false, false>, smem);                                         \
-    }
-    if constexpr (MODE != RL_INV) if (hin && p.persistent) {
-        // one block per pair of resident slots: the grid is sized to the GPU, not to the lines
-        auto run_pipe = [&](auto kern, size_t smem) -> int {
-            SG_TRY(cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                               "register lines smem attribute"));
-            SG_TRY(fast_max_carveout(kern, "register lines carveout attribute"));
-            int dev = 0, sms = 0, per_sm = 0;
-            SG_TRY(cuda_status(cudaGetDevice(&dev), "register lines device"));
-            SG_TRY(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
-            SG_TRY(cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, rl::kThreads, smem),
-                               "register lines occupancy"));
-            const int grid = (int)std::min<long long>((long long)sms * (per_sm > 0 ? per_sm : 1), blocks);
-            kern<<<grid, rl::kThreads, smem, stream>>>(p, (int)blocks);
-            return launch_status("register lines (persistent)");
-        };
-        if (N == 512)
-            return hout ? run_pipe(reg_lines_pipe_kernel<512, MODE, MODE != RL_FWD>, rl::Pipe<512>::smem_bytes)
-                        : run_pipe(reg_lines_pipe_kernel<512, MODE, false>, rl::Pipe<512>::smem_bytes);
-        if (N == 256)
-            return hout ? run_pipe(reg_lines_pipe_kernel<256, MODE, MODE != RL_FWD>, rl::Pipe<256>::smem_bytes)
-                        : run_pipe(reg_lines_pipe_kernel<256, MODE, false>, rl::Pipe<256>::smem_bytes);
     }
     if (N == 512) SG_RL_PICK(512)
     if (N == 256) SG_RL_PICK(256)

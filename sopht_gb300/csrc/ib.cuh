@@ -155,6 +155,86 @@ __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i)
     }
 }
 
+// The same interaction with one thread per marker, for kernels that hold only a few warps (the
+// coupled rod sub-steps: one block per rod).  The warp-per-marker form leaves 20 of 32 lanes idle in
+// the double-precision nearest-index and feedback arithmetic, which on this GPU's narrow FP64 pipe
+// costs as much as full warps; here every lane works on its own marker and the 4^dim window is
+// summed in cell order (the warp form sums it as a shuffle tree, so the two round differently).
+template <typename T, int DIM>
+__device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int i) {
+    constexpr int CELLS = DIM == 2 ? 16 : 64;
+    if (i >= p.n_lag) return;
+    const int n = p.n_lag;
+    const T dxT = (T)p.dx;
+    int near[DIM];
+    T phi[DIM][4];
+    bool inside = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const double X = p.pos[d * n + i];
+        near[d] = (int)np_floor_divide(X - p.shift, p.dx);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const T r = (T)((double)(near[d] + k - 1) * p.dx + p.shift - X);
+            const T rn = r / dxT;
+            phi[d][k] = p.kernel == 0 ? T(1) + dev_cos<T>((T)(0.5 * 3.14159265358979323846) * rn)
+                                      : peskin_phi<T>(fabs(rn));
+        }
+        const int ext = d == 0 ? p.nx : (d == 1 ? p.ny : p.nz);
+        if (near[d] - 1 < 0 || near[d] + 2 > ext - 1) inside = false;
+        p.nearest[d * n + i] = near[d];
+    }
+    const int xi_step = p.dyn ? p.dyn->xi_step : p.xi_step;
+    if (xi_step) {
+        const T dt = (T)(p.dev ? p.dev->dt : (p.dyn ? p.dyn->xi_dt : p.xi_dt));
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            p.pos_mismatch[d * n + i] = p.pos_mismatch[d * n + i] + dt * p.vel_mismatch[d * n + i];
+    }
+    if (!inside) {
+        atomicExch(p.status, SG_ERR_OUT_OF_DOMAIN);
+        for (int c = 0; c < CELLS; ++c) p.weights[c * n + i] = T(0);
+        return;
+    }
+    T pref;
+    if (p.kernel == 0) {
+        const T q = T(0.25) / dxT;
+        pref = DIM == 2 ? q * q : (T)((double)q * (double)q * (double)q);
+    } else {
+        const T q = T(0.125) / dxT;
+        pref = DIM == 2 ? q * q : (T)((double)q * (double)q * (double)q);
+    }
+    const int64_t plane = (int64_t)p.ny * p.nx;
+    const int64_t ncell = plane * (DIM == 3 ? p.nz : 1);
+    T acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = T(0);
+#pragma unroll 4
+    for (int c = 0; c < CELLS; ++c) {
+        const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
+        T w = pref * phi[0][bx] * phi[1][by];
+        int gz = 0;
+        if constexpr (DIM == 3) {
+            w = w * phi[2][bz];
+            gz = near[2] - 1 + bz;
+        }
+        p.weights[c * n + i] = w;
+        const int64_t g = (int64_t)gz * plane + (int64_t)(near[1] - 1 + by) * p.nx + (near[0] - 1 + bx);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += p.u[d * ncell + g] * w;
+    }
+    const T dxd = DIM == 2 ? dxT * dxT : dxT * dxT * dxT;
+    const double K = p.dyn ? p.dyn->K : p.K, C = p.dyn ? p.dyn->C : p.C;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const T U = acc[d] * dxd;
+        p.flow_vel[d * n + i] = U;
+        const T dU = (T)((double)U - p.body_vel[d * n + i]);
+        p.vel_mismatch[d * n + i] = dU;
+        p.forcing[d * n + i] = (T)(K * (double)p.pos_mismatch[d * n + i] + C * (double)dU);
+    }
+}
+
 template <typename T, int DIM>
 __global__ void __launch_bounds__(256) ib_interaction_kernel(IBParams<T> p) {
     ib_interaction_body<T, DIM>(p, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);

@@ -13,7 +13,6 @@
 // normalisation and dx^dim folded in.  It is built in FP64 on the GPU with the
 // same kernels instantiated for double, then rounded to the field precision.
 #include <cmath>
-#include <cstdlib>
 #include <vector>
 
 #include "poisson.cuh"
@@ -256,21 +255,12 @@ int poisson_spectral_passes(sg_poisson_plan_s* p, int ncomp, cudaStream_t stream
 // fp32 y and z passes of lengths 256 and 512 on the register line kernels (fft_reg.cuh): y lines
 // are slabs of nx + 1 adjacent lines per (component, z plane), z lines one slab of 2 ny (nx + 1)
 // lines per component.  Returns SG_ERR_UNSUPPORTED for the other lengths.
-static int reg_persistent() {
-    static const int v = [] {
-        const char* e = getenv("SG_RL_PERSISTENT");
-        return e ? atoi(e) : 1;
-    }();
-    return v;
-}
-
 static int reg_pass3d(sg_poisson_plan_s* p, int ncomp, int pass, cudaStream_t stream) {
     float2* spec = reinterpret_cast<float2*>(p->spec);
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     RegLinesParams r{};
     r.in = spec;
     r.out = spec;
-    r.persistent = reg_persistent();
     if (pass == 1) {
         const int64_t plane = (int64_t)2 * ny * (nx + 1);
         SG_REQUIRE((int64_t)ncomp * plane < (1LL << 31), SG_ERR_SHAPE, "z pass: too many lines");
@@ -371,6 +361,9 @@ int poisson_store_rows(sg_poisson_plan_s* p, T* sol, int ncomp, int64_t comp_str
         r.in_map = row_map(p->ny, p->nx + 1, p->nz, (int64_t)2 * p->ny * (p->nx + 1), p->spec_comp_elems);
         r.out_map = row_map(p->ny, p->nx, p->nz, (int64_t)p->ny * p->nx, comp_stride);
         r.n_rows = ncomp * p->nz * p->ny;
+        // 3D fp32 rows of 256 complex points: the register row kernel (fft_reg.cuh)
+        if constexpr (sizeof(T) == 4)
+            if (p->nx == rl::kRowM && r.n_out <= p->nx) return launch_reg_rows_c2r(r, stream);
     }
     return launch_rows_c2r<T>(r, stream);
 }

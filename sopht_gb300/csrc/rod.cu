@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     const int r = blockIdx.x, n = b.n_elems, t = threadIdx.x, nt = blockDim.x;
     rod::View v = rod::view_of(b, r);
     const rod::Scratch s = rod::carve(rod_smem, n);
-    double* clamp = rod_smem + rod::scratch_doubles(n);  // q (9), w (3) of a driven clamp
+    // q (9), w (3) of a driven clamp at the half step, then at the end of the sub-step
+    double* clamp = rod_smem + rod::scratch_doubles(n);
     const bool driven = c.drive_phase != nullptr && v.clamped;
     if (driven) {
         v.clamp_q = clamp;
@@ -93,13 +94,19 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     const double h = dt / n_sub;
     const double decay = c.damping_rate != 0.0 ? exp(-c.damping_rate * h) : 1.0;
     const int64_t n_markers = (int64_t)b.n_rods * n;
-    const int warp = t >> 5, n_warps = nt >> 5;
     const double* q0 = b.clamp_directors + r * 9;
     const double phase = driven ? c.drive_phase[r] : 0.0;
     for (int k = 0; k < n_sub; ++k) {
         const double tk = t0 + k * h;
-        if (driven && t == 0) rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + 0.5 * h, clamp,
-                                                clamp + 9);
+        // both frames of the sub-step at once, by the first lane of two warps
+        if (driven && (t == 0 || t == 32)) {
+            double* fr = t == 0 ? clamp : clamp + 12;
+            rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + (t == 0 ? 0.5 * h : h), fr, fr + 9);
+        }
+        if (driven) {
+            v.clamp_q = clamp;
+            v.clamp_w = clamp + 9;
+        }
         __syncthreads();
         for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
         for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
@@ -107,7 +114,7 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
         // FlowForces.apply_forces at the half step: markers, interaction, reaction
         for (int e = t; e < n; e += nt) rod::element_marker(v, r, e, 3, n_markers, c.marker_pos, c.marker_vel);
         __syncthreads();
-        for (int e = warp; e < n; e += n_warps) ib_interaction_body<T, 3>(c.ib, r * n + e);
+        for (int e = t; e < n; e += nt) ib_interaction_thread<T, 3>(c.ib, r * n + e);
         __syncthreads();
         for (int i = t; i <= n; i += nt)
             rod::element_reaction(v, r, i, 3, n_markers, c.ib.forcing, b.external_forces + (int64_t)r * 3 * (n + 1),
@@ -120,9 +127,10 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
         for (int i = t; i <= n; i += nt) rod::node_update(v, s, i, h, decay);
         for (int e = t; e < n; e += nt) rod::element_update(v, s, e, h, decay);
         __syncthreads();
-        if (driven && t == 0) rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + h, clamp,
-                                                clamp + 9);
-        __syncthreads();
+        if (driven) {
+            v.clamp_q = clamp + 12;
+            v.clamp_w = clamp + 21;
+        }
         for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
         for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
         // VirtualBoundaryForcing.time_step(local_rod_dt) of this rod's markers
@@ -132,6 +140,7 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
                 const int64_t m = d * n_markers + (int64_t)r * n + e;
                 c.ib.pos_mismatch[m] = c.ib.pos_mismatch[m] + hT * c.ib.vel_mismatch[m];
             }
+        __syncthreads();  // element 0's last clamp frame is read before the next sub-step rewrites it
     }
 }
 
@@ -244,7 +253,7 @@ static int rod_coupled_launch(const sg_rod_batch& b, const sg_rod_coupling& cp, 
     c.drive_amp = cp.drive_amplitude;
     c.drive_freq = cp.drive_frequency;
     for (int a = 0; a < 3; ++a) c.axis[a] = cp.drive_axis[a];
-    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 12) * sizeof(double);
+    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 24) * sizeof(double);
     if (smem > 48 * 1024)
         SG_TRY(cuda_status(cudaFuncSetAttribute(rod_coupled_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem),

@@ -261,9 +261,28 @@ class VirtualBoundaryForcing:
                   float(self.virtual_boundary_damping_coeff), int(xi_step), float(xi_dt), dev_scalars,
                   ptr(self._status), stream_ptr(self.device))
 
+    # from this many markers on, spreading sorts the (marker, cell) pairs by cell (O(n log n)) instead of
+    # scanning the lower-index markers of every pair (O(n^2)); both sum each cell in marker order
+    SORTED_SPREAD_MIN_MARKERS = 512
+    _sorted_scratch = None
+
     def _spread(self, eul_forcing, reset: bool):
         nz, ny, nx = self._extent(eul_forcing)
-        _lib.call("sg_ib_spread", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, self.num_lag_nodes,
+        n = self.num_lag_nodes
+        if n >= self.SORTED_SPREAD_MIN_MARKERS:
+            key = (nz, ny, nx)
+            if self._sorted_scratch is None or self._sorted_scratch[0] != key:
+                nbytes = int(_lib.load().sg_ib_spread_sorted_scratch_bytes(self.grid_dim, nz, ny, nx, n))
+                if nbytes > 0:
+                    self._sorted_scratch = (key, torch.empty(nbytes, dtype=torch.uint8, device=self.device))
+            if self._sorted_scratch is not None and self._sorted_scratch[0] == key:
+                scratch = self._sorted_scratch[1]
+                _lib.call("sg_ib_spread_sorted", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, n,
+                          ptr(self.nearest_eul_grid_index_to_lag_grid), ptr(self.interp_weights),
+                          ptr(self.lag_grid_forcing_field), ptr(eul_forcing), int(reset), scratch.data_ptr(),
+                          scratch.numel(), stream_ptr(self.device))
+                return
+        _lib.call("sg_ib_spread", sg_dtype(self.real_t), self.grid_dim, nz, ny, nx, n,
                   ptr(self.nearest_eul_grid_index_to_lag_grid), ptr(self.interp_weights),
                   ptr(self.lag_grid_forcing_field), ptr(eul_forcing), int(reset), stream_ptr(self.device))
 

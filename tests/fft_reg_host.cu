@@ -114,3 +114,38 @@ extern "C" int rl_host_pass(int mode, int N, const float* in, float* out, int n_
     }
     return -1;
 }
+
+// The register complex-to-real row kernel: rows of M + 1 = 257 bins (pitch 257) to rows of n_out
+// reals (pitch out_pitch), phase by phase.
+extern "C" int rl_host_rows_c2r(const float* in, float* out, int n_rows, int out_pitch, int n_out, const float* tw_m,
+                                const float* tw_l) {
+    RowsC2RParams<float> p{};
+    p.in = reinterpret_cast<const float2*>(in);
+    p.in_map = row_map(n_rows, rl::kRowM + 1);
+    p.out = out;
+    p.out_map = row_map(n_rows, out_pitch);
+    p.n_out = n_out;
+    p.n_rows = n_rows;
+    p.tw_m = reinterpret_cast<const float2*>(tw_m);
+    p.tw_l = reinterpret_cast<const float2*>(tw_l);
+    std::vector<float2> buf(rl::kRowSlots), tw_a(256), regs((size_t)rl::kThreads * 16);
+    rl::stage_row_twiddles(p, tw_a.data(), 0, 1);
+    const int blocks = (n_rows + rl::kLines - 1) / rl::kLines;
+    for (int blk = 0; blk < blocks; ++blk) {
+        for (int tid = 0; tid < rl::kThreads; ++tid) {
+            float2* v = regs.data() + (size_t)tid * 16;
+            const int row = tid / 16, q = tid & 15;
+            rl::c2r_load_b(p, rl::row_of(p, blk, row), q, v);
+            dft16<true>(v);
+            rl::c2r_write_b(buf.data(), row, q, v);
+        }
+        for (int tid = 0; tid < rl::kThreads; ++tid) {
+            float2* v = regs.data() + (size_t)tid * 16;
+            const int row = tid / 16, q = tid & 15;
+            rl::c2r_read_a(buf.data(), row, q, v);
+            rl::c2r_inv_a(tw_a.data(), q, v);
+            rl::c2r_store_a(p, rl::row_of(p, blk, row), q, v);
+        }
+    }
+    return 0;
+}

@@ -1,9 +1,8 @@
 """Generate the golden fixtures in this directory by running the reference SophT code.
 
-Run in a container that has the reference checkout (read-only) at
-``/root/reference``::
+Run where a checkout of the reference is available (read only), giving its path::
 
-    python tests/golden/make_golden.py [/path/to/reference [group ...]]
+    python tests/golden/make_golden.py /path/to/reference [group ...]
 
 The reference is imported through the test-only stand-ins in ``ref_shims.py``
 (pystencils kernels evaluated with numpy, pyfftw replaced by scipy.fft, numba's
@@ -966,7 +965,7 @@ def write_signatures() -> None:
     print(f"{path.name}: {len(out)} callables")
 
 
-def main(ref_root: str = "/root/reference", *groups: str) -> None:
+def main(ref_root: str, *groups: str) -> None:
     """Validate the stand-ins, then write every group's fixtures (or only the named ``groups``)."""
     spne, spib, sps = _import_reference(ref_root)
     if not groups or "signatures" in groups:
@@ -987,4 +986,6 @@ def main(ref_root: str = "/root/reference", *groups: str) -> None:
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py /path/to/reference [group ...]")
     main(*sys.argv[1:])

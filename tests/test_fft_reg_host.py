@@ -117,3 +117,24 @@ def test_y_inverse_pass(lib, N, ncomp, nz, nx, half_out):
     assert _rel(buf[:, :, :n_out], ref) < 2e-6
     if half_out:  # points beyond the crop are left as they were
         np.testing.assert_array_equal(buf[:, :, n_out:], spec[:, :, n_out:])
+
+
+@pytest.mark.parametrize("n_rows,n_out", [(40, 256), (16, 200)])
+def test_rows_complex_to_real(lib, n_rows, n_out):
+    """Rows of 257 bins (the x spectrum of 512-real rows) back to their first n_out reals, against
+    numpy's irfft scaled by the unnormalised length (the library folds 1/N into the Green's table)."""
+    lib.rl_host_rows_c2r.restype = ctypes.c_int
+    lib.rl_host_rows_c2r.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+    M = 256
+    rng = np.random.default_rng(n_rows)
+    x = rng.standard_normal((n_rows, 2 * M))
+    spec = np.fft.rfft(x, axis=1).astype(np.complex64)  # (n_rows, M + 1)
+    tw_m = np.exp(-2j * np.pi * np.arange(M) / M).astype(np.complex64)
+    tw_l = np.exp(-2j * np.pi * np.arange(M + 1) / (2 * M)).astype(np.complex64)
+    out = np.full((n_rows, M), np.nan, np.float32)
+    assert lib.rl_host_rows_c2r(spec.ctypes.data, out.ctypes.data, n_rows, M, n_out, tw_m.ctypes.data,
+                                tw_l.ctypes.data) == 0
+    ref = np.fft.irfft(spec.astype(np.complex128), n=2 * M, axis=1) * (2 * M)
+    assert _rel(out[:, :n_out].astype(np.float64), ref[:, :n_out]) < 2e-6
+    assert np.isnan(out[:, n_out:]).all()
