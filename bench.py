@@ -456,7 +456,16 @@ def run_gpu(args, wl: Workload, rank, world):
                 "traffic": traffic_from_profiles(wl.name, top), "algorithmic_bytes_per_launch": algo}
     step_ms = elapsed_ms / steps
     step_bytes = STEP_BYTES[wl.dim] * cells
-    launches_per_step = (2 + (5 if wl.kind == "rods" else 2 * len(wl.bodies)) + (9 if wl.dim == 3 else 5))
+    # this library's kernels per step: the device dt; for rods the coupled sub-step kernel, the element
+    # markers, the interaction and the spreading (the sorted form for a batch of 512 markers or more:
+    # its pair and group kernels, plus the radix sort's own); per cylinder an interaction and a spread;
+    # then the flow step (3D: forcing curl, rotational update, diffusion, load, y FFT, z convolution,
+    # y inverse, x C2R, curl; 2D: sweep, load, column convolution, x C2R, curl)
+    if wl.kind == "rods":
+        body_launches = 3 + (2 if wl.bodies and len(wl.bodies) * wl.bodies[0]["n_elem"] >= 512 else 1)
+    else:
+        body_launches = 2 * len(wl.bodies)
+    launches_per_step = 1 + body_launches + (9 if wl.dim == 3 else 5)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "flow steps/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -484,8 +493,10 @@ def run_gpu(args, wl: Workload, rank, world):
         "kernels": kernels,
         "e2e": {"value": round(world * steps / e2e_s, 2), "unit": "flow steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "note": "public API per step: host dt (sync), the rod loop and interaction, the flow step, the "
-                        "Lagrangian forcing read back"},
+                "note": ("public API per step: host dt (sync), the rod loop and interaction, the flow step, the "
+                         "Lagrangian forcing read back" if wl.kind == "rods" else
+                         "public API per step: host dt (sync), marker kinematics up from pinned memory, the "
+                         "interaction, the flow step, the Lagrangian forcing read back")},
         "gpu_launches": launches_per_step * steps,
         "clocks": clock_info,
         "accuracy": accuracy,

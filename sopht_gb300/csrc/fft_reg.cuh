@@ -347,7 +347,7 @@ SG_RL_FN void c2r_store_a(const RowsC2RParams<float>& p, const RowLine& R, int g
 
 #ifdef __CUDACC__
 // The x pass's complex-to-real rows (M = 256, n_out <= M reals kept) in registers.
-__global__ void __launch_bounds__(rl::kThreads, 3) reg_rows_c2r_kernel(RowsC2RParams<float> p) {
+static __global__ void __launch_bounds__(rl::kThreads, 3) reg_rows_c2r_kernel(RowsC2RParams<float> p) {
     __shared__ __align__(16) float2 buf[rl::kRowSlots];
     __shared__ __align__(16) float2 tw_a[256];
     const int tid = threadIdx.x, row = tid / 16, q = tid & 15;
@@ -373,7 +373,7 @@ inline int launch_reg_rows_c2r(const RowsC2RParams<float>& p, cudaStream_t strea
 // zero upper input half).  RL_INV: inverse transform of a full spectrum (HOUT keeps the lower
 // output half).  RL_CONV: forward, Green's factor, inverse, in registers between the exchanges.
 template <int N, int MODE, bool HIN, bool HOUT>
-__global__ void __launch_bounds__(rl::kThreads, (N == 512 ? 2 : 3)) reg_lines_kernel(RegLinesParams p) {
+__global__ void __launch_bounds__(rl::kThreads, (N == 512 && MODE != RL_FWD ? 2 : 3)) reg_lines_kernel(RegLinesParams p) {
     extern __shared__ __align__(16) float2 rl_buf[];
     float2* tw_a = rl_buf + N * rl::kLines;
     const int tid = threadIdx.x, l = tid & (rl::kLines - 1), q = tid / rl::kLines;

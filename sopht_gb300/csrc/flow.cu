@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "flow_plan.cuh"
+#include "flow_load_reg.cuh"
 
 
 
@@ -83,6 +84,9 @@ int launch_fast_flow_load(const FlowLoadParams<T>& p, cudaStream_t stream) {
 
 template <typename T>
 int launch_flow_load(FlowLoadParams<T> p, cudaStream_t stream) {
+    // 3D fp32 rows of 256 reals: the register load pass (flow_load_reg.cuh)
+    if constexpr (sizeof(T) == 4)
+        if (p.dim == 3 && p.nx == rl::kRowM && p.st.n == rl::kRowM) return launch_reg_flow_load(p, stream);
 #define SG_CALL(NN, WW) launch_fast_flow_load<T, NN, WW>(p, stream)
     SG_FAST_DISPATCH(p.st.n, p.n_rows, SG_CALL)
 #undef SG_CALL

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../sopht_gb300/csrc/fft_reg.cuh"
+#include "../sopht_gb300/csrc/flow_load_reg.cuh"
 
 namespace {
 
@@ -145,6 +146,60 @@ extern "C" int rl_host_rows_c2r(const float* in, float* out, int n_rows, int out
             rl::c2r_read_a(buf.data(), row, q, v);
             rl::c2r_inv_a(tw_a.data(), q, v);
             rl::c2r_store_a(p, rl::row_of(p, blk, row), q, v);
+        }
+    }
+    return 0;
+}
+
+// The register load pass of the 3D flow step (penalise, write back, zero the forcing, x R2C) on a
+// (3, nz, ny, 256) field, phase by phase; the split's shuffle reads the partner thread's registers.
+extern "C" int rl_host_flow_load(int nz, int ny, int width, const float* src, float* dst, float* forcing,
+                                 const float* cx, const float* cy, const float* cz, float* spec, const float* tw_m,
+                                 const float* tw_l) {
+    const int nx = rl::kRowM;
+    FlowLoadParams<float> p{};
+    p.dim = 3;
+    p.nz = nz;
+    p.ny = ny;
+    p.nx = nx;
+    p.width = width;
+    p.src = src;
+    p.dst = dst;
+    p.forcing = forcing;
+    p.zero_ncomp = 1;
+    p.cx = cx;
+    p.cy = cy;
+    p.cz = cz;
+    p.comp_stride = (int64_t)nz * ny * nx;
+    p.spec = reinterpret_cast<float2*>(spec);
+    p.spec_map = row_map(ny, nx + 1, nz, (int64_t)2 * ny * (nx + 1), (int64_t)nz * 2 * ny * (nx + 1));
+    p.n_rows = 3 * nz * ny;
+    p.st.n = nx;
+    p.tw_m = reinterpret_cast<const float2*>(tw_m);
+    p.tw_l = reinterpret_cast<const float2*>(tw_l);
+    std::vector<float2> buf(rl::kRowSlots), tw_a(256), regs((size_t)rl::kThreads * 16);
+    rl::stage_load_twiddles(p, tw_a.data(), 0, 1);
+    const int blocks = (p.n_rows + rl::kLines - 1) / rl::kLines;
+    for (int blk = 0; blk < blocks; ++blk) {
+        for (int tid = 0; tid < rl::kThreads; ++tid) {
+            float2* v = regs.data() + (size_t)tid * 16;
+            const int row = tid / 16, q = tid & 15;
+            rl::load_row_a(p, rl::load_row_of(p, blk, row), q, v);
+            rl::r2c_fwd_a(tw_a.data(), q, v);
+            rl::r2c_write_a(buf.data(), row, q, v);
+        }
+        for (int tid = 0; tid < rl::kThreads; ++tid) {
+            float2* v = regs.data() + (size_t)tid * 16;
+            const int row = tid / 16, q = tid & 15;
+            rl::r2c_read_b(buf.data(), row, q, v);
+            dft16<false>(v);
+        }
+        for (int tid = 0; tid < rl::kThreads; ++tid) {
+            const float2* v = regs.data() + (size_t)tid * 16;
+            const int row = tid / 16, q = tid & 15;
+            const int partner = row * 16 + ((16 - q) & 15);
+            const float2* pv = regs.data() + (size_t)partner * 16;
+            rl::r2c_split_store(p, rl::load_row_of(p, blk, row), q, v, [&](int r) { return pv[r]; });
         }
     }
     return 0;

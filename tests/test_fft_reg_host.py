@@ -138,3 +138,46 @@ def test_rows_complex_to_real(lib, n_rows, n_out):
     ref = np.fft.irfft(spec.astype(np.complex128), n=2 * M, axis=1) * (2 * M)
     assert _rel(out[:, :n_out].astype(np.float64), ref[:, :n_out]) < 2e-6
     assert np.isnan(out[:, n_out:]).all()
+
+
+@pytest.mark.parametrize("width", [0, 2])
+def test_flow_load_pass(lib, width):
+    """The 3D load pass on a (3, 5, 3, 256) field: penalised vorticity written back (the fast load's
+    arithmetic, bitwise), the forcing zeroed, and the x spectrum of each penalised row against
+    numpy's rfft of the row zero-padded to 512 reals."""
+    lib.rl_host_flow_load.restype = ctypes.c_int
+    lib.rl_host_flow_load.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 9
+    nz, ny, nx = 5, 3, 256
+    rng = np.random.default_rng(width)
+    src = rng.standard_normal((3, nz, ny, nx)).astype(np.float32)
+    dst = np.full_like(src, np.nan)
+    forcing = np.ones_like(src)
+    cx = rng.uniform(0.2, 1.0, nx).astype(np.float32)
+    cy = rng.uniform(0.2, 1.0, ny).astype(np.float32)
+    cz = rng.uniform(0.2, 1.0, nz).astype(np.float32)
+    spec = np.zeros((3, nz, 2 * ny, nx + 1), np.complex64)
+    tw_m = np.exp(-2j * np.pi * np.arange(nx) / nx).astype(np.complex64)
+    tw_l = np.exp(-2j * np.pi * np.arange(nx + 1) / (2 * nx)).astype(np.complex64)
+    assert lib.rl_host_flow_load(nz, ny, width, src.ctypes.data, dst.ctypes.data, forcing.ctypes.data,
+                                 cx.ctypes.data, cy.ctypes.data, cz.ctypes.data, spec.ctypes.data,
+                                 tw_m.ctypes.data, tw_l.ctypes.data) == 0
+
+    def band(i, n):
+        return i if width <= 0 else min(max(i, width - 1), n - width)
+
+    pen = np.empty_like(src)
+    for z in range(nz):
+        for y in range(ny):
+            row = src[:, band(z, nz), band(y, ny)][:, [band(x, nx) for x in range(nx)]]
+            if width > 0:
+                row = row * cx[None]
+                row = row * cy[y]
+                row = row * cz[z]
+            pen[:, z, y] = row
+    np.testing.assert_array_equal(dst, pen)
+    assert not forcing.any()
+    padded = np.zeros((3, nz, ny, 2 * nx))
+    padded[..., :nx] = pen
+    ref = np.fft.rfft(padded, axis=-1)
+    assert _rel(spec[:, :, :ny].astype(np.complex128), ref) < 2e-6
+    assert not spec[:, :, ny:].any()
