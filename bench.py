@@ -457,12 +457,14 @@ def run_gpu(args, wl: Workload, rank, world):
     step_ms = elapsed_ms / steps
     step_bytes = STEP_BYTES[wl.dim] * cells
     # this library's kernels per step: the device dt; for rods the coupled sub-step kernel, the element
-    # markers, the interaction and the spreading (the sorted form for a batch of 512 markers or more:
-    # its pair and group kernels, plus the radix sort's own); per cylinder an interaction and a spread;
+    # markers, the interaction and the spreading (the sorted form from SORTED_SPREAD_MIN_MARKERS markers
+    # on: its pair and group kernels, plus the radix sort's own); per cylinder an interaction and a spread;
     # then the flow step (3D: forcing curl, rotational update, diffusion, load, y FFT, z convolution,
     # y inverse, x C2R, curl; 2D: sweep, load, column convolution, x C2R, curl)
     if wl.kind == "rods":
-        body_launches = 3 + (2 if wl.bodies and len(wl.bodies) * wl.bodies[0]["n_elem"] >= 512 else 1)
+        from sopht_gb300.numeric import VirtualBoundaryForcing
+        n_markers = len(wl.bodies) * wl.bodies[0]["n_elem"] if wl.bodies else 0
+        body_launches = 3 + (2 if n_markers >= VirtualBoundaryForcing.SORTED_SPREAD_MIN_MARKERS else 1)
     else:
         body_launches = 2 * len(wl.bodies)
     launches_per_step = 1 + body_launches + (9 if wl.dim == 3 else 5)

@@ -554,7 +554,8 @@ int sg_rod_batch_element_loads(const sg_rod_batch* batch, int dim, int dtype, co
  * compute_interaction_force_on_lag_grid (VirtualBoundaryForcing.py:187-230)
  * and its reaction as the rods' external forces -- followed by
  * VirtualBoundaryForcing.time_step (xi += dt dU, :276-283).  One launch, one
- * CTA per rod; the sub-step count is read on the device, so the call can be
+ * CTA per rod, 1 to 256 elements per rod (one thread per element and marker;
+ * more return SG_ERR_SHAPE); the sub-step count is read on the device, so the call can be
  * part of a step whose dt never leaves the GPU.  Lagrangian fields are
  * (3, n_rods * n_elems) in the flow precision `dtype`; marker positions and
  * velocities float64.  A driven clamp (drive_phase not NULL) turns each

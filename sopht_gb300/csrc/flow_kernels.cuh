@@ -478,6 +478,29 @@ __device__ __forceinline__ bool cell3(const Grid3& G, int& x, int& y, int& z, in
     return x < G.nx && y < G.ny;
 }
 
+// Step scalars in the field precision for every thread of a block, converted once: thread 0
+// converts and the block reads them from shared memory.  A double-to-float conversion runs on this
+// GPU's narrow double-precision pipe, and one per thread kept that pipe busy a fifth (one scalar)
+// to two thirds (three) of the time in the 3D cell kernels; converting once made the forcing curl,
+// rotational update and diffusion 1.8 % faster together (0.445 -> 0.437 ms at 256^3).  Every thread of the block calls it at
+// the same point, before any early return (it holds a barrier); get(i) is called by thread 0 only.
+// The kernels call it after issuing their loads, so that the barrier waits with the loads in
+// flight.  The values are the same roundings as a conversion in each thread.
+template <typename T, int N, typename F>
+__device__ __forceinline__ void block_scalars(F get, T (&out)[N]) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) out[i] = (T)get(i);
+    } else {
+        __shared__ T s[N];
+        if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0)
+            for (int i = 0; i < N; ++i) s[i] = (T)get(i);
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < N; ++i) out[i] = s[i];
+    }
+}
+
 // out = w + pf * curl_h(v) on [1:-1]^3 (w elsewhere)  — per component as
 // update_vorticity_from_velocity_forcing_3d.py:29-94 writes it.
 template <typename T>
@@ -498,7 +521,7 @@ template <typename T> struct Stencil3DParams {
     ScalarSrc sc;
     T prefactor;
     int mode;
-    int ncomp;       // components of the diffusion (0 means 3)
+    int ncomp;       // components of the diffusion, 1 to 3 (0 means 3)
 };
 
 // w1 = w + pf curl(f)  (mode 0; f may be null -> copy)
@@ -508,13 +531,21 @@ __global__ void __launch_bounds__(256) forcing_curl3d_kernel(Stencil3DParams<T> 
     const int64_t n = G.n();
     int x, y, z;
     int64_t g;
-    if (!cell3(G, x, y, z, g)) return;
+    const bool live = cell3(G, x, y, z, g);
+    const bool in = live && p.b && G.interior(z, y, x);
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
-    T w0 = p.a[g], w1 = p.a[n + g], w2 = p.a[2 * n + g];
-    if (p.b && G.interior(z, y, x)) {
-        const T pf = p.mode == 0 ? (T)p.sc.forcing() : p.prefactor;
-        T c[3];
-        curl3_at(p.b, g, n, sy, sz, c);
+    T w0 = T(0), w1 = T(0), w2 = T(0), c[3] = {T(0), T(0), T(0)};
+    if (live) {
+        w0 = p.a[g];
+        w1 = p.a[n + g];
+        w2 = p.a[2 * n + g];
+    }
+    if (in) curl3_at(p.b, g, n, sy, sz, c);
+    T pfs[1];
+    block_scalars<T, 1>([&](int) { return p.mode == 0 ? p.sc.forcing() : (double)p.prefactor; }, pfs);
+    if (!live) return;
+    if (in) {
+        const T pf = pfs[0];
         w0 = w0 + pf * c[0];
         w1 = w1 + pf * c[1];
         w2 = w2 + pf * c[2];
@@ -541,11 +572,16 @@ __global__ void __launch_bounds__(256) rotational_update3d_kernel(Stencil3DParam
     const int64_t n = G.n();
     int x, y, z;
     int64_t g;
-    if (!cell3(G, x, y, z, g)) return;
+    const bool live = cell3(G, x, y, z, g);
+    const bool in = live && G.interior(z, y, x);
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
-    T w0 = p.a[g], w1 = p.a[n + g], w2 = p.a[2 * n + g];
-    if (G.interior(z, y, x)) {
-        const T pc = (T)p.sc.advection();
+    T w0 = T(0), w1 = T(0), w2 = T(0), r0 = T(0), r1 = T(0), r2 = T(0);
+    if (live) {
+        w0 = p.a[g];
+        w1 = p.a[n + g];
+        w2 = p.a[2 * n + g];
+    }
+    if (in) {
         T cyp[3], cym[3], czp[3], czm[3], cxp[3], cxm[3];
         cross_at(p.b, p.a, g + sy, n, cyp);
         cross_at(p.b, p.a, g - sy, n, cym);
@@ -553,9 +589,18 @@ __global__ void __launch_bounds__(256) rotational_update3d_kernel(Stencil3DParam
         cross_at(p.b, p.a, g - sz, n, czm);
         cross_at(p.b, p.a, g + 1, n, cxp);
         cross_at(p.b, p.a, g - 1, n, cxm);
-        w0 = w0 + pc * (cyp[2] - cym[2] - czp[1] + czm[1]);
-        w1 = w1 + pc * (czp[0] - czm[0] - cxp[2] + cxm[2]);
-        w2 = w2 + pc * (cxp[1] - cxm[1] - cyp[0] + cym[0]);
+        r0 = cyp[2] - cym[2] - czp[1] + czm[1];
+        r1 = czp[0] - czm[0] - cxp[2] + cxm[2];
+        r2 = cxp[1] - cxm[1] - cyp[0] + cym[0];
+    }
+    T pcs[1];
+    block_scalars<T, 1>([&](int) { return p.sc.advection(); }, pcs);
+    if (!live) return;
+    if (in) {
+        const T pc = pcs[0];
+        w0 = w0 + pc * r0;
+        w1 = w1 + pc * r1;
+        w2 = w2 + pc * r2;
     }
     p.out[g] = w0;
     p.out[n + g] = w1;
@@ -569,21 +614,27 @@ __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) 
     const int64_t n = G.n();
     int x, y, z;
     int64_t g;
-    if (!cell3(G, x, y, z, g)) return;
+    const bool live = cell3(G, x, y, z, g);
+    const bool in = live && G.interior(z, y, x);
     const int64_t sy = G.nx, sz = (int64_t)G.nx * G.ny;
-    const T k = p.mode == 0 ? (T)p.sc.diffusion() : p.prefactor;
-    const bool in = G.interior(z, y, x);
     const int nc = p.ncomp ? p.ncomp : 3;
-#pragma unroll 3
-    for (int c = 0; c < nc; ++c) {
+    T v[3] = {T(0), T(0), T(0)}, lap[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (c >= nc || !live) continue;
         const T* f = p.a + c * n;
-        T v = f[g];
-        if (in) {
-            // diffusion_flux_3d.py:34-43 term order: z+1, z-1, y+1, y-1, x+1, x-1
-            const T lap = f[g + sz] + f[g - sz] + f[g + sy] + f[g - sy] + f[g + 1] + f[g - 1] - T(6) * f[g];
-            v = v + k * lap;
-        }
-        p.out[c * n + g] = v;
+        v[c] = f[g];
+        // diffusion_flux_3d.py:34-43 term order: z+1, z-1, y+1, y-1, x+1, x-1
+        if (in) lap[c] = f[g + sz] + f[g - sz] + f[g + sy] + f[g - sy] + f[g + 1] + f[g - 1] - T(6) * f[g];
+    }
+    T ks[1];
+    block_scalars<T, 1>([&](int) { return p.mode == 0 ? p.sc.diffusion() : (double)p.prefactor; }, ks);
+    if (!live) return;
+    const T k = ks[0];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (c >= nc) continue;
+        p.out[c * n + g] = in ? v[c] + k * lap[c] : v[c];
     }
 }
 
@@ -693,6 +744,8 @@ __global__ void __launch_bounds__(256) curl3d_kernel(Curl3DParams<T> p) {
     int x, y, z;
     int64_t g;
     T m = T(0);
+    // the free stream is converted in every thread: a block-wide conversion (block_scalars) made this
+    // kernel slower (0.128 -> 0.133 ms at 256^3), its barrier costing more than the conversions
     if (cell3(G, x, y, z, g)) {
         T c[3] = {T(0), T(0), T(0)};
         if (G.interior(z, y, x)) {

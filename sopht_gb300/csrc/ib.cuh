@@ -158,10 +158,21 @@ __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i)
 // The same interaction with one thread per marker, for kernels that hold only a few warps (the
 // coupled rod sub-steps: one block per rod).  The warp-per-marker form leaves 20 of 32 lanes idle in
 // the double-precision nearest-index and feedback arithmetic, which on this GPU's narrow FP64 pipe
-// costs as much as full warps; here every lane works on its own marker and the 4^dim window is
+// costs as much as full warps (a warp's double-precision instruction holds its SM sub-partition's
+// FP64 unit for about 64 cycles, however many lanes are active); here every lane works on its own
+// marker and the 4^dim window is
 // summed in cell order (the warp form sums it as a shuffle tree, so the two round differently).
+//
+// The form the rod sub-steps take: X and V are the marker's position and body velocity, xi its
+// position mismatch, all in the caller's registers (the caller owns the marker for the whole launch
+// and keeps xi += dt dU itself, so p.xi_step is not read); dU returns the velocity mismatch.  Only
+// the forcing is stored every call: the reaction of the neighbouring nodes reads it.  The nearest
+// indices, weights, interpolated velocity and velocity mismatch are stored when `keep` is set (the
+// last sub-step: they are the interactor's state the reference leaves after its rod loop).  The
+// flow velocity is read through the read-only path, 16 cells (48 loads) at a time.
 template <typename T, int DIM>
-__device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int i) {
+__device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int i, const double* Xs,
+                                                      const double* Vs, const T* xi, T* dU_out, bool keep) {
     constexpr int CELLS = DIM == 2 ? 16 : 64;
     if (i >= p.n_lag) return;
     const int n = p.n_lag;
@@ -171,7 +182,7 @@ __device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int 
     bool inside = true;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        const double X = p.pos[d * n + i];
+        const double X = Xs[d];
         near[d] = (int)np_floor_divide(X - p.shift, p.dx);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -182,18 +193,12 @@ __device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int 
         }
         const int ext = d == 0 ? p.nx : (d == 1 ? p.ny : p.nz);
         if (near[d] - 1 < 0 || near[d] + 2 > ext - 1) inside = false;
-        p.nearest[d * n + i] = near[d];
-    }
-    const int xi_step = p.dyn ? p.dyn->xi_step : p.xi_step;
-    if (xi_step) {
-        const T dt = (T)(p.dev ? p.dev->dt : (p.dyn ? p.dyn->xi_dt : p.xi_dt));
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-            p.pos_mismatch[d * n + i] = p.pos_mismatch[d * n + i] + dt * p.vel_mismatch[d * n + i];
+        if (keep) p.nearest[d * n + i] = near[d];
     }
     if (!inside) {
         atomicExch(p.status, SG_ERR_OUT_OF_DOMAIN);
         for (int c = 0; c < CELLS; ++c) p.weights[c * n + i] = T(0);
+        for (int d = 0; d < DIM; ++d) dU_out[d] = T(0);
         return;
     }
     T pref;
@@ -206,32 +211,40 @@ __device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int 
     }
     const int64_t plane = (int64_t)p.ny * p.nx;
     const int64_t ncell = plane * (DIM == 3 ? p.nz : 1);
+    // the window's first cell, per component
+    const int64_t g0 = (DIM == 3 ? (int64_t)(near[DIM - 1] - 1) * plane : 0) + (int64_t)(near[1] - 1) * p.nx +
+                       (near[0] - 1);
+    const T* ud[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ud[d] = p.u + d * ncell + g0;
     T acc[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) acc[d] = T(0);
-#pragma unroll 4
+#pragma unroll 16
     for (int c = 0; c < CELLS; ++c) {
         const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
         T w = pref * phi[0][bx] * phi[1][by];
-        int gz = 0;
+        int64_t off = (int64_t)by * p.nx + bx;
         if constexpr (DIM == 3) {
             w = w * phi[2][bz];
-            gz = near[2] - 1 + bz;
+            off += bz * plane;
         }
-        p.weights[c * n + i] = w;
-        const int64_t g = (int64_t)gz * plane + (int64_t)(near[1] - 1 + by) * p.nx + (near[0] - 1 + bx);
+        if (keep) p.weights[c * n + i] = w;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) acc[d] += p.u[d * ncell + g] * w;
+        for (int d = 0; d < DIM; ++d) acc[d] += __ldg(ud[d] + off) * w;
     }
     const T dxd = DIM == 2 ? dxT * dxT : dxT * dxT * dxT;
     const double K = p.dyn ? p.dyn->K : p.K, C = p.dyn ? p.dyn->C : p.C;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         const T U = acc[d] * dxd;
-        p.flow_vel[d * n + i] = U;
-        const T dU = (T)((double)U - p.body_vel[d * n + i]);
-        p.vel_mismatch[d * n + i] = dU;
-        p.forcing[d * n + i] = (T)(K * (double)p.pos_mismatch[d * n + i] + C * (double)dU);
+        const T dU = (T)((double)U - Vs[d]);
+        dU_out[d] = dU;
+        if (keep) {
+            p.flow_vel[d * n + i] = U;
+            p.vel_mismatch[d * n + i] = dU;
+        }
+        p.forcing[d * n + i] = (T)(K * (double)xi[d] + C * (double)dU);
     }
 }
 

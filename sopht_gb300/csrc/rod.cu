@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256) rod_loads_kernel(sg_rod_batch b, int dim,
 // One flow step of the rod loop of the reference examples for every rod of a batch (one CTA per
 // rod): rod_time_steps = int(dt / min(dt, max_rod_dt)) position-Verlet sub-steps of dt /
 // rod_time_steps, each with the flow forces of the half-step configuration (the element-centric
-// markers, the virtual-boundary interaction of ib_interaction_body on those markers, the reaction
+// markers, the virtual-boundary interaction of ib_interaction_thread on those markers, the reaction
 // on the nodes) and followed by xi += dt_sub dU.  The sub-step count comes from the device dt, so
 // a captured step needs no host value.
 template <typename T> struct RodCouplingArgs {
@@ -75,19 +75,22 @@ template <typename T> struct RodCouplingArgs {
     double axis[3];
 };
 
+// The passes of a sub-step, each ended by a barrier: drift and rotate; the markers with their
+// interaction, in the same thread (and the next sub-step's driven-clamp frames); the reaction loads
+// and the element pass; the Voronoi pass; the node and element updates; drift, rotate and the
+// mismatch step.  Thread e owns marker e for the whole launch and keeps its position mismatch in
+// registers.  The clamp frames of sub-step k + 1 are computed during sub-step k into the other half
+// of a double buffer, by the first lanes of two warps that hold no nodes when the block has such
+// warps (they would only wait at the barriers otherwise), in the longest pass.
 template <typename T>
 __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCouplingArgs<T> c) {
     extern __shared__ double rod_smem[];
     const int r = blockIdx.x, n = b.n_elems, t = threadIdx.x, nt = blockDim.x;
     rod::View v = rod::view_of(b, r);
     const rod::Scratch s = rod::carve(rod_smem, n);
-    // q (9), w (3) of a driven clamp at the half step, then at the end of the sub-step
+    // [sub-step parity][half step, end of sub-step][q (9), w (3)] of a driven clamp
     double* clamp = rod_smem + rod::scratch_doubles(n);
     const bool driven = c.drive_phase != nullptr && v.clamped;
-    if (driven) {
-        v.clamp_q = clamp;
-        v.clamp_w = clamp + 9;
-    }
     const double dt = c.dev ? c.dev->dt : c.host_dt;
     const double t0 = c.dev ? c.host_time + (*c.dev_time_end - dt) : c.host_time;
     const int n_sub = dt > c.max_rod_dt ? (int)(dt / c.max_rod_dt) : 1;
@@ -96,30 +99,49 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     const int64_t n_markers = (int64_t)b.n_rods * n;
     const double* q0 = b.clamp_directors + r * 9;
     const double phase = driven ? c.drive_phase[r] : 0.0;
+    const int fa = n + 1 <= nt - 64 ? nt - 64 : 0;  // the frame threads: fa and fa + 32
+    const T hT = (T)h;
+    auto frames = [&](int k) {
+        if (driven && (t == fa || t == fa + 32)) {
+            double* fr = clamp + (k & 1) * 24 + (t == fa ? 0 : 12);
+            const double tk = t0 + k * h;
+            rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + (t == fa ? 0.5 * h : h), fr, fr + 9);
+        }
+    };
+    frames(0);
+    // the position mismatch of the thread's marker (n <= 256 = blockDim: one marker per thread)
+    T xi[3] = {T(0), T(0), T(0)};
+    const int64_t own = (int64_t)r * n + t;
+    if (t < n)
+        for (int d = 0; d < 3; ++d) xi[d] = c.ib.pos_mismatch[d * n_markers + own];
+    __syncthreads();
     for (int k = 0; k < n_sub; ++k) {
-        const double tk = t0 + k * h;
-        // both frames of the sub-step at once, by the first lane of two warps
-        if (driven && (t == 0 || t == 32)) {
-            double* fr = t == 0 ? clamp : clamp + 12;
-            rod::driven_clamp(q0, c.axis, c.drive_amp, c.drive_freq, phase, tk + (t == 0 ? 0.5 * h : h), fr, fr + 9);
-        }
+        double* fr = clamp + (k & 1) * 24;
+        const bool last = k + 1 == n_sub;
         if (driven) {
-            v.clamp_q = clamp;
-            v.clamp_w = clamp + 9;
+            v.clamp_q = fr;
+            v.clamp_w = fr + 9;
         }
-        __syncthreads();
         for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
         for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
         __syncthreads();
-        // FlowForces.apply_forces at the half step: markers, interaction, reaction
-        for (int e = t; e < n; e += nt) rod::element_marker(v, r, e, 3, n_markers, c.marker_pos, c.marker_vel);
+        // FlowForces.apply_forces at the half step: each marker, then its interaction
+        if (!last) frames(k + 1);
+        T dU[3] = {T(0), T(0), T(0)};
+        if (t < n) {
+            double X[3], V[3];
+            rod::element_marker_at(v, t, 3, X, V);
+            for (int d = 0; d < 3; ++d) {
+                c.marker_pos[d * n_markers + own] = X[d];
+                c.marker_vel[d * n_markers + own] = V[d];
+            }
+            ib_interaction_thread<T, 3>(c.ib, (int)own, X, V, xi, dU, last);
+        }
         __syncthreads();
-        for (int e = t; e < n; e += nt) ib_interaction_thread<T, 3>(c.ib, r * n + e);
-        __syncthreads();
+        // the reaction on the nodes, and the element pass (which reads neither the loads nor the markers)
         for (int i = t; i <= n; i += nt)
             rod::element_reaction(v, r, i, 3, n_markers, c.ib.forcing, b.external_forces + (int64_t)r * 3 * (n + 1),
                                   b.external_torques + (int64_t)r * 3 * n);
-        __syncthreads();
         for (int e = t; e < n; e += nt) rod::element_pass(v, s, e);
         __syncthreads();
         for (int q = t; q < n - 1; q += nt) rod::voronoi_pass(v, s, q);
@@ -128,20 +150,18 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
         for (int e = t; e < n; e += nt) rod::element_update(v, s, e, h, decay);
         __syncthreads();
         if (driven) {
-            v.clamp_q = clamp + 12;
-            v.clamp_w = clamp + 21;
+            v.clamp_q = fr + 12;
+            v.clamp_w = fr + 21;
         }
         for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
         for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
-        // VirtualBoundaryForcing.time_step(local_rod_dt) of this rod's markers
-        const T hT = (T)h;
-        for (int e = t; e < n; e += nt)
-            for (int d = 0; d < 3; ++d) {
-                const int64_t m = d * n_markers + (int64_t)r * n + e;
-                c.ib.pos_mismatch[m] = c.ib.pos_mismatch[m] + hT * c.ib.vel_mismatch[m];
-            }
-        __syncthreads();  // element 0's last clamp frame is read before the next sub-step rewrites it
+        // VirtualBoundaryForcing.time_step(local_rod_dt) of the thread's marker
+        if (t < n)
+            for (int d = 0; d < 3; ++d) xi[d] = xi[d] + hT * dU[d];
+        __syncthreads();  // the next sub-step's frames are written, and this one's no longer read
     }
+    if (t < n)
+        for (int d = 0; d < 3; ++d) c.ib.pos_mismatch[d * n_markers + own] = xi[d];
 }
 
 static int rod_grid_blocks(int64_t items) {
@@ -253,7 +273,7 @@ static int rod_coupled_launch(const sg_rod_batch& b, const sg_rod_coupling& cp, 
     c.drive_amp = cp.drive_amplitude;
     c.drive_freq = cp.drive_frequency;
     for (int a = 0; a < 3; ++a) c.axis[a] = cp.drive_axis[a];
-    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 24) * sizeof(double);
+    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 48) * sizeof(double);
     if (smem > 48 * 1024)
         SG_TRY(cuda_status(cudaFuncSetAttribute(rod_coupled_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem),
@@ -267,7 +287,7 @@ extern "C" int sg_rod_batch_coupled_substeps(const sg_rod_batch* batch, const sg
     SG_TRY(rod_batch_check(batch, 3));
     SG_REQUIRE(cp, SG_ERR_INVALID_ARG, "rod coupling: null coupling");
     const sg_rod_batch& b = *batch;
-    SG_REQUIRE(b.n_elems <= 1024, SG_ERR_SHAPE, "rod coupling: 1 to 1024 elements per rod");
+    SG_REQUIRE(b.n_elems <= 256, SG_ERR_SHAPE, "rod coupling: 1 to 256 elements per rod");
     SG_REQUIRE(b.directors && b.omega && b.rest_lengths && b.shear_matrix && b.mass_second_moment &&
                    b.inv_mass_second_moment && b.rest_sigma,
                SG_ERR_INVALID_ARG, "rod coupling: null rod array");

@@ -138,11 +138,13 @@ SG_ROD_FN void rotation_exp(const double a[3], double r[9]) {
 
 // The rotation vector of r (angle below pi), the angle taken from the trace as the rod model does
 // (the trace and the antisymmetric part give different angles once r drifts from orthogonality).
+// sin(theta) is sqrt((1 - c)(1 + c)) of the same clamped cosine c: the same function of c as the
+// model's sin(arccos(c)), without a second transcendental on the double-precision pipe.
 SG_ROD_FN void rotation_log(const double r[9], double a[3]) {
     double cosv = (r[0] + r[4] + r[8] - 1.0) / 2.0;
     cosv = cosv < -1.0 ? -1.0 : (cosv > 1.0 ? 1.0 : cosv);
     const double theta = acos(cosv);
-    const double s = sin(theta);
+    const double s = sqrt((1.0 - cosv) * (1.0 + cosv));
     const double f = theta < 1e-6 ? 0.5 + theta * theta / 12.0 : theta / (2.0 * (s == 0.0 ? 1.0 : s));
     a[0] = f * (r[7] - r[5]);
     a[1] = f * (r[2] - r[6]);
@@ -340,15 +342,24 @@ SG_ROD_FN double add_rn(double a, double b) {
 #endif
 }
 
-SG_ROD_FN void element_marker(const View& r, int rod, int e, int dim, int64_t n_markers, double* pos,
-                              double* vel) {
+SG_ROD_FN void element_marker_at(const View& r, int e, int dim, double* pos, double* vel) {
     const int n = r.n, nn = n + 1;
-    const int64_t m = (int64_t)rod * n + e;
     const double m0 = r.mass[e], m1 = r.mass[e + 1];
     for (int d = 0; d < dim; ++d) {
-        pos[d * n_markers + m] = (r.x[d * nn + e + 1] + r.x[d * nn + e]) / 2.0;
+        pos[d] = (r.x[d * nn + e + 1] + r.x[d * nn + e]) / 2.0;
         // products rounded before the sum, as numpy does (no fused multiply-add on the device)
-        vel[d * n_markers + m] = add_rn(mul_rn(m1, r.v[d * nn + e + 1]), mul_rn(m0, r.v[d * nn + e])) / (m1 + m0);
+        vel[d] = add_rn(mul_rn(m1, r.v[d * nn + e + 1]), mul_rn(m0, r.v[d * nn + e])) / (m1 + m0);
+    }
+}
+
+SG_ROD_FN void element_marker(const View& r, int rod, int e, int dim, int64_t n_markers, double* pos,
+                              double* vel) {
+    const int64_t m = (int64_t)rod * r.n + e;
+    double p[3], u[3];
+    element_marker_at(r, e, dim, p, u);
+    for (int d = 0; d < dim; ++d) {
+        pos[d * n_markers + m] = p[d];
+        vel[d * n_markers + m] = u[d];
     }
 }
 

@@ -262,8 +262,11 @@ class VirtualBoundaryForcing:
                   ptr(self._status), stream_ptr(self.device))
 
     # from this many markers on, spreading sorts the (marker, cell) pairs by cell (O(n log n)) instead of
-    # scanning the lower-index markers of every pair (O(n^2)); both sum each cell in marker order
-    SORTED_SPREAD_MIN_MARKERS = 512
+    # scanning the lower-index markers of every pair (O(n^2)); both sum each cell in marker order.  On
+    # a 256^3 grid (3D, markers of 100-element rods, launches replayed from a CUDA graph) the scan
+    # takes 36, 75 and 120 us at 1024, 1600 and 2048 markers and the sort 54, 58 and 60 us (its radix
+    # passes dominate), so they cross near 1300.
+    SORTED_SPREAD_MIN_MARKERS = 1300
     _sorted_scratch = None
 
     def _spread(self, eul_forcing, reset: bool):

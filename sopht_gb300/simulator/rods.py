@@ -237,6 +237,8 @@ class CosseratRodBatchFlowInteraction(VirtualBoundaryForcing):
             raise ValueError("eul_grid_forcing_field must be the simulator's CUDA tensor")
         if eul_grid_forcing_field.dim() != 4 or eul_grid_forcing_field.shape[0] != 3:
             raise ValueError("the rod batch couples to a 3D flow: (3, nz, ny, nx) fields")
+        if rod_batch.n_elems > 256:
+            raise ValueError("the coupled rod sub-steps take rods of 1 to 256 elements")
         self.rod_batch = rod_batch
         pos = rod_batch.arrays["position_collection"]
         max_len = float(torch.linalg.vector_norm(pos[:, :, 1:] - pos[:, :, :-1], dim=1).max())

@@ -109,6 +109,17 @@ def test_argument_validation_of_the_operator_entries(lib):
     assert lib.sg_rod_batch_element_markers(ctypes.byref(rb), 3, None, c, None) == 1  # no output
     assert lib.sg_rod_batch_element_loads(ctypes.byref(rb), 3, 7, b, None) == 1  # dtype
     assert lib.sg_rod_batch_element_loads(ctypes.byref(rb), 2, 0, None, None) == 1  # no forcing
+    # the coupled sub-steps hold one element per thread: 1 to 256 elements per rod
+    from sopht_gb300._lib import RodCoupling
+    for field in ("directors", "omega", "rest_lengths", "shear_matrix", "mass_second_moment",
+                  "inv_mass_second_moment", "rest_sigma", "rest_voronoi_lengths", "bend_matrix", "rest_kappa"):
+        setattr(rb, field, a)
+    cp = RodCoupling()
+    rb.n_elems = 300
+    assert lib.sg_rod_batch_coupled_substeps(ctypes.byref(rb), ctypes.byref(cp), None) == 2
+    assert b"256" in lib.sg_last_error()
+    rb.n_elems = 8
+    assert lib.sg_rod_batch_coupled_substeps(ctypes.byref(rb), None, None) == 1  # no coupling
 
 
 def _clamped_penalise(field, width, cx, cy, cz=None):
