@@ -21,6 +21,16 @@ __device__ __forceinline__ double np_floor_divide(double a, double b) {
     return q;
 }
 
+// The same floor from a * (1 / b): the product is within two units in the last place of a / b, so
+// its floor is off by at most one, and the two corrections give the exact floor again (the same
+// integer as np_floor_divide) with a multiplication in place of the division.
+__device__ __forceinline__ double np_floor_divide_recip(double a, double b, double inv_b) {
+    double q = floor(a * inv_b);
+    if (fma(-q, b, a) < 0.0) q -= 1.0;
+    else if (fma(-(q + 1.0), b, a) >= 0.0) q += 1.0;
+    return q;
+}
+
 template <typename T> __device__ __forceinline__ T dev_cos(T x);
 template <> __device__ __forceinline__ float dev_cos<float>(float x) { return cosf(x); }
 template <> __device__ __forceinline__ double dev_cos<double>(double x) { return cos(x); }
@@ -177,13 +187,14 @@ __device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int 
     if (i >= p.n_lag) return;
     const int n = p.n_lag;
     const T dxT = (T)p.dx;
+    const double inv_dx = 1.0 / p.dx;
     int near[DIM];
     T phi[DIM][4];
     bool inside = true;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         const double X = Xs[d];
-        near[d] = (int)np_floor_divide(X - p.shift, p.dx);
+        near[d] = (int)np_floor_divide_recip(X - p.shift, p.dx, inv_dx);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const T r = (T)((double)(near[d] + k - 1) * p.dx + p.shift - X);

@@ -88,8 +88,16 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     const int r = blockIdx.x, n = b.n_elems, t = threadIdx.x, nt = blockDim.x;
     rod::View v = rod::view_of(b, r);
     const rod::Scratch s = rod::carve(rod_smem, n);
-    // [sub-step parity][half step, end of sub-step][q (9), w (3)] of a driven clamp
+    // [sub-step parity][half step, end of sub-step][q (9), w (3)] of a driven clamp, then the
+    // reciprocals of the masses (n + 1), rest lengths (n) and rest Voronoi lengths (n - 1)
     double* clamp = rod_smem + rod::scratch_doubles(n);
+    double* recip = clamp + 48;
+    for (int i = t; i <= n; i += nt) recip[i] = 1.0 / v.mass[i];
+    for (int e = t; e < n; e += nt) recip[n + 1 + e] = 1.0 / v.l0[e];
+    for (int q = t; q < n - 1; q += nt) recip[2 * n + 1 + q] = 1.0 / v.d0[q];
+    v.inv_mass = recip;
+    v.inv_l0 = recip + n + 1;
+    v.inv_d0 = recip + 2 * n + 1;
     const bool driven = c.drive_phase != nullptr && v.clamped;
     const double dt = c.dev ? c.dev->dt : c.host_dt;
     const double t0 = c.dev ? c.host_time + (*c.dev_time_end - dt) : c.host_time;
@@ -273,7 +281,7 @@ static int rod_coupled_launch(const sg_rod_batch& b, const sg_rod_coupling& cp, 
     c.drive_amp = cp.drive_amplitude;
     c.drive_freq = cp.drive_frequency;
     for (int a = 0; a < 3; ++a) c.axis[a] = cp.drive_axis[a];
-    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 48) * sizeof(double);
+    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 48 + 3 * b.n_elems) * sizeof(double);
     if (smem > 48 * 1024)
         SG_TRY(cuda_status(cudaFuncSetAttribute(rod_coupled_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem),

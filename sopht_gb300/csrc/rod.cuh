@@ -52,6 +52,11 @@ struct View {
     const double* clamp_x;
     const double* clamp_q;
     const double* clamp_w;  // angular velocity of a driven clamp (local frame), or null: at rest
+    // 1 / mass, 1 / l0, 1 / d0 computed once by the caller, or null: divided where used (the same
+    // values either way)
+    const double* inv_mass;
+    const double* inv_l0;
+    const double* inv_d0;
 };
 
 SG_ROD_FN View view_of(const sg_rod_batch& b, int r) {
@@ -78,6 +83,9 @@ SG_ROD_FN View view_of(const sg_rod_batch& b, int r) {
     v.clamp_x = b.clamp_position + r * 3;
     v.clamp_q = b.clamp_directors + r * 9;
     v.clamp_w = nullptr;
+    v.inv_mass = nullptr;
+    v.inv_l0 = nullptr;
+    v.inv_d0 = nullptr;
     return v;
 }
 
@@ -127,25 +135,42 @@ SG_ROD_FN void rotation_exp(const double a[3], double r[9]) {
         sa = sin(t) / t;
         ca = (1.0 - cos(t)) / t2;
     }
-    const double ax[9] = {0.0, -a[2], a[1], a[2], 0.0, -a[0], -a[1], a[0], 0.0};
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            double a2ij = 0.0;
-            for (int m = 0; m < 3; ++m) a2ij += ax[i * 3 + m] * ax[m * 3 + j];
-            r[i * 3 + j] = (i == j ? 1.0 : 0.0) + sa * ax[i * 3 + j] + ca * a2ij;
-        }
+    // [a]x = (0, -a2, a1; a2, 0, -a0; -a1, a0, 0) and [a]x^2 = a a^T - t^2 I, written out: 21
+    // operations where the 3x3 products with their zero entries take 45
+    const double p01 = a[0] * a[1], p02 = a[0] * a[2], p12 = a[1] * a[2];
+    const double s0 = sa * a[0], s1 = sa * a[1], s2 = sa * a[2];
+    r[0] = 1.0 + ca * -(a[1] * a[1] + a[2] * a[2]);
+    r[4] = 1.0 + ca * -(a[0] * a[0] + a[2] * a[2]);
+    r[8] = 1.0 + ca * -(a[0] * a[0] + a[1] * a[1]);
+    r[1] = ca * p01 - s2;
+    r[3] = ca * p01 + s2;
+    r[2] = ca * p02 + s1;
+    r[6] = ca * p02 - s1;
+    r[5] = ca * p12 - s0;
+    r[7] = ca * p12 + s0;
 }
 
 // The rotation vector of r (angle below pi), the angle taken from the trace as the rod model does
-// (the trace and the antisymmetric part give different angles once r drifts from orthogonality).
-// sin(theta) is sqrt((1 - c)(1 + c)) of the same clamped cosine c: the same function of c as the
-// model's sin(arccos(c)), without a second transcendental on the double-precision pipe.
+// (the trace and the antisymmetric part give different angles once r drifts from orthogonality):
+// f (r - r^T) with f = theta / (2 sin theta), theta = arccos(c), c the clamped (trace - 1) / 2.
+// For u = 1 - c below 0.01 (theta below 0.1415, the Voronoi rotations of a sub-step) f is the
+// Taylor series of that same function of c in u, 1/2 + u/6 + u^2/15 + u^3/35 + 4u^4/315 +
+// 4u^5/693 + 8u^6/3003 + 8u^7/6435 + 64u^8/109395 (the next term is below 3e-20 of f there), with
+// no arccosine, sine or division on the narrow double-precision pipe; above it, sin theta is
+// sqrt(u (1 + c)).  u is exact (Sterbenz) for c in [1/2, 1].
 SG_ROD_FN void rotation_log(const double r[9], double a[3]) {
     double cosv = (r[0] + r[4] + r[8] - 1.0) / 2.0;
     cosv = cosv < -1.0 ? -1.0 : (cosv > 1.0 ? 1.0 : cosv);
-    const double theta = acos(cosv);
-    const double s = sqrt((1.0 - cosv) * (1.0 + cosv));
-    const double f = theta < 1e-6 ? 0.5 + theta * theta / 12.0 : theta / (2.0 * (s == 0.0 ? 1.0 : s));
+    const double u = 1.0 - cosv;
+    double f;
+    if (u < 0.01) {
+        f = 0.5 + u * (1.0 / 6.0 + u * (1.0 / 15.0 + u * (1.0 / 35.0 + u * (4.0 / 315.0 + u * (4.0 / 693.0 +
+            u * (8.0 / 3003.0 + u * (8.0 / 6435.0 + u * (64.0 / 109395.0))))))));
+    } else {
+        const double theta = acos(cosv);
+        const double s = sqrt(u * (1.0 + cosv));
+        f = theta / (2.0 * (s == 0.0 ? 1.0 : s));
+    }
     a[0] = f * (r[7] - r[5]);
     a[1] = f * (r[2] - r[6]);
     a[2] = f * (r[3] - r[1]);
@@ -231,7 +256,7 @@ SG_ROD_FN void element_pass(const View& r, const Scratch& s, int e) {
     for (int a = 0; a < 3; ++a) d[a] = r.x[a * nn + e + 1] - r.x[a * nn + e];
     // divisions by their reciprocals: a double division is an iteration of many operations here
     const double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const double inv_len = 1.0 / len, inv_l0 = 1.0 / r.l0[e];
+    const double inv_len = 1.0 / len, inv_l0 = r.inv_l0 ? r.inv_l0[e] : 1.0 / r.l0[e];
     for (int a = 0; a < 3; ++a) t[a] = d[a] * inv_len;
     const double dil = len * inv_l0, inv_dil = 1.0 / dil;
     matvec(r.q, n, e, t, qt);
@@ -270,7 +295,7 @@ SG_ROD_FN void voronoi_pass(const View& r, const Scratch& s, int k) {
             rel[i * 3 + j] = acc;
         }
     rotation_log(rel, lg);
-    const double inv_d0 = 1.0 / r.d0[k];
+    const double inv_d0 = r.inv_d0 ? r.inv_d0[k] : 1.0 / r.d0[k];
     for (int a = 0; a < 3; ++a) kappa[a] = -lg[a] * inv_d0;
     const double eps = 0.5 * (s.len[k + 1] + s.len[k]) * inv_d0;
     const double inv_eps3 = 1.0 / (eps * eps * eps);
@@ -286,7 +311,7 @@ SG_ROD_FN void voronoi_pass(const View& r, const Scratch& s, int k) {
 
 SG_ROD_FN void node_update(View& r, const Scratch& s, int i, double dt, double decay) {
     const int n = r.n, nn = n + 1;
-    const double inv_m = 1.0 / r.mass[i];
+    const double inv_m = r.inv_mass ? r.inv_mass[i] : 1.0 / r.mass[i];
     for (int a = 0; a < 3; ++a) {
         double f = 0.0;
         if (i < n) f += s.nlab[a * n + i];
