@@ -55,6 +55,15 @@ template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { ret
 template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
     return cmake<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+// fp32 complex sums on the device as packed two-lane instructions (one FADD2 / FFMA2 for both
+// parts, half the issue slots of two scalar adds): the FFT butterflies are mostly these.  a - b is
+// fma(b, -1, a), which rounds the exact difference once, as a - b does.
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+template <> __host__ __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <> __host__ __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+#endif
 template <typename C> __host__ __device__ __forceinline__ C cconj(C a) { return cmake<C>(a.x, -a.y); }
 template <typename C, typename T> __host__ __device__ __forceinline__ C cscale(C a, T s) { return cmake<C>(a.x * s, a.y * s); }
 // multiply by (0 + i*s): i*(x + i y) = -y + i x
