@@ -98,6 +98,32 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     v.inv_mass = recip;
     v.inv_l0 = recip + n + 1;
     v.inv_d0 = recip + 2 * n + 1;
+    // the rod's state and loads live in shared memory for the launch (each pass reads what other
+    // threads of the block wrote in the one before), copied back at the end
+    double* const gx = v.x;
+    double* const gv = v.v;
+    double* const gq = v.q;
+    double* const gw = v.w;
+    double* const gf = b.external_forces + (int64_t)r * 3 * (n + 1);
+    double* const gc = b.external_torques + (int64_t)r * 3 * n;
+    double* const sx = recip + 3 * n;
+    double* const sv = sx + 3 * (n + 1);
+    double* const sq = sv + 3 * (n + 1);
+    double* const sw = sq + 9 * n;
+    double* const sf = sw + 3 * n;
+    double* const sc = sf + 3 * (n + 1);
+    for (int i = t; i < 3 * (n + 1); i += nt) {
+        sx[i] = gx[i];
+        sv[i] = gv[i];
+    }
+    for (int i = t; i < 9 * n; i += nt) sq[i] = gq[i];
+    for (int i = t; i < 3 * n; i += nt) sw[i] = gw[i];
+    v.x = sx;
+    v.v = sv;
+    v.q = sq;
+    v.w = sw;
+    v.f_ext = sf;
+    v.c_ext = sc;
     const bool driven = c.drive_phase != nullptr && v.clamped;
     const double dt = c.dev ? c.dev->dt : c.host_dt;
     const double t0 = c.dev ? c.host_time + (*c.dev_time_end - dt) : c.host_time;
@@ -147,9 +173,7 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
         }
         __syncthreads();
         // the reaction on the nodes, and the element pass (which reads neither the loads nor the markers)
-        for (int i = t; i <= n; i += nt)
-            rod::element_reaction(v, r, i, 3, n_markers, c.ib.forcing, b.external_forces + (int64_t)r * 3 * (n + 1),
-                                  b.external_torques + (int64_t)r * 3 * n);
+        for (int i = t; i <= n; i += nt) rod::element_reaction(v, r, i, 3, n_markers, c.ib.forcing, sf, sc);
         for (int e = t; e < n; e += nt) rod::element_pass(v, s, e);
         __syncthreads();
         for (int q = t; q < n - 1; q += nt) rod::voronoi_pass(v, s, q);
@@ -170,6 +194,16 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     }
     if (t < n)
         for (int d = 0; d < 3; ++d) c.ib.pos_mismatch[d * n_markers + own] = xi[d];
+    for (int i = t; i < 3 * (n + 1); i += nt) {
+        gx[i] = sx[i];
+        gv[i] = sv[i];
+        gf[i] = sf[i];
+    }
+    for (int i = t; i < 9 * n; i += nt) gq[i] = sq[i];
+    for (int i = t; i < 3 * n; i += nt) {
+        gw[i] = sw[i];
+        gc[i] = sc[i];
+    }
 }
 
 static int rod_grid_blocks(int64_t items) {
@@ -281,7 +315,10 @@ static int rod_coupled_launch(const sg_rod_batch& b, const sg_rod_coupling& cp, 
     c.drive_amp = cp.drive_amplitude;
     c.drive_freq = cp.drive_frequency;
     for (int a = 0; a < 3; ++a) c.axis[a] = cp.drive_axis[a];
-    const size_t smem = (size_t)(rod::scratch_doubles(b.n_elems) + 48 + 3 * b.n_elems) * sizeof(double);
+    // pass scratch, clamp frames, reciprocals, then x, v (3 (n + 1) each), Q (9 n), w (3 n), the
+    // external forces (3 (n + 1)) and torques (3 n)
+    const int ne = b.n_elems;
+    const size_t smem = (size_t)(rod::scratch_doubles(ne) + 48 + 3 * ne + 9 * (ne + 1) + 15 * ne) * sizeof(double);
     if (smem > 48 * 1024)
         SG_TRY(cuda_status(cudaFuncSetAttribute(rod_coupled_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem),
