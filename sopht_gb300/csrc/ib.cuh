@@ -179,15 +179,16 @@ __device__ __forceinline__ void ib_interaction_body(const IBParams<T>& p, int i)
 // the forcing is stored every call: the reaction of the neighbouring nodes reads it.  The nearest
 // indices, weights, interpolated velocity and velocity mismatch are stored when `keep` is set (the
 // last sub-step: they are the interactor's state the reference leaves after its rod loop).  The
-// flow velocity is read through the read-only path, 16 cells (48 loads) at a time.
+// flow velocity is read through the read-only path, 16 cells (48 loads) at a time.  inv_dx is
+// 1 / p.dx, computed once by the caller.
 template <typename T, int DIM>
 __device__ __forceinline__ void ib_interaction_thread(const IBParams<T>& p, int i, const double* Xs,
-                                                      const double* Vs, const T* xi, T* dU_out, bool keep) {
+                                                      const double* Vs, const T* xi, T* dU_out, bool keep,
+                                                      double inv_dx) {
     constexpr int CELLS = DIM == 2 ? 16 : 64;
     if (i >= p.n_lag) return;
     const int n = p.n_lag;
     const T dxT = (T)p.dx;
-    const double inv_dx = 1.0 / p.dx;
     int near[DIM];
     T phi[DIM][4];
     bool inside = true;

@@ -75,10 +75,10 @@ template <typename T> struct RodCouplingArgs {
     double axis[3];
 };
 
-// The passes of a sub-step, each ended by a barrier: drift and rotate; the markers with their
-// interaction, in the same thread (and the next sub-step's driven-clamp frames); the reaction loads
-// and the element pass; the Voronoi pass; the node and element updates; drift, rotate and the
-// mismatch step.  Thread e owns marker e for the whole launch and keeps its position mismatch in
+// The passes of a sub-step, each ended by a barrier: the markers with their interaction, in the same
+// thread (and the next sub-step's driven-clamp frames); the reaction loads and the element pass;
+// the Voronoi pass; the node and element updates; drift, rotate and the mismatch step -- the
+// closing half drift of one sub-step and the opening half drift of the next in one pass.  Thread e owns marker e for the whole launch and keeps its position mismatch in
 // registers.  The clamp frames of sub-step k + 1 are computed during sub-step k into the other half
 // of a double buffer, by the first lanes of two warps that hold no nodes when the block has such
 // warps (they would only wait at the barriers otherwise), in the longest pass.
@@ -148,17 +148,18 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
     const int64_t own = (int64_t)r * n + t;
     if (t < n)
         for (int d = 0; d < 3; ++d) xi[d] = c.ib.pos_mismatch[d * n_markers + own];
+    const double inv_dx = 1.0 / c.ib.dx;
+    __syncthreads();
+    // the first sub-step's opening half drift
+    if (driven) {
+        v.clamp_q = clamp;
+        v.clamp_w = clamp + 9;
+    }
+    for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
+    for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
     __syncthreads();
     for (int k = 0; k < n_sub; ++k) {
-        double* fr = clamp + (k & 1) * 24;
         const bool last = k + 1 == n_sub;
-        if (driven) {
-            v.clamp_q = fr;
-            v.clamp_w = fr + 9;
-        }
-        for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
-        for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
-        __syncthreads();
         // FlowForces.apply_forces at the half step: each marker, then its interaction
         if (!last) frames(k + 1);
         T dU[3] = {T(0), T(0), T(0)};
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
                 c.marker_pos[d * n_markers + own] = X[d];
                 c.marker_vel[d * n_markers + own] = V[d];
             }
-            ib_interaction_thread<T, 3>(c.ib, (int)own, X, V, xi, dU, last);
+            ib_interaction_thread<T, 3>(c.ib, (int)own, X, V, xi, dU, last, inv_dx);
         }
         __syncthreads();
         // the reaction on the nodes, and the element pass (which reads neither the loads nor the markers)
@@ -181,12 +182,21 @@ __global__ void __launch_bounds__(256) rod_coupled_kernel(sg_rod_batch b, RodCou
         for (int i = t; i <= n; i += nt) rod::node_update(v, s, i, h, decay);
         for (int e = t; e < n; e += nt) rod::element_update(v, s, e, h, decay);
         __syncthreads();
+        // this sub-step's closing half drift and the next one's opening half drift in one pass (the
+        // same arithmetic as the two, one rotation exponential), element 0 left at the next
+        // half-step frame; the last sub-step closes with one half drift at the end-of-step frame
+        double* const next = clamp + ((k + 1) & 1) * 24;
         if (driven) {
-            v.clamp_q = fr + 12;
-            v.clamp_w = fr + 21;
+            v.clamp_q = last ? clamp + (k & 1) * 24 + 12 : next;
+            v.clamp_w = last ? clamp + (k & 1) * 24 + 21 : next + 9;
         }
-        for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
-        for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
+        if (last) {
+            for (int i = t; i <= n; i += nt) rod::drift_node(v, i, 0.5 * h);
+            for (int e = t; e < n; e += nt) rod::rotate_element(v, e, 0.5 * h);
+        } else {
+            for (int i = t; i <= n; i += nt) rod::drift_node_twice(v, i, 0.5 * h);
+            for (int e = t; e < n; e += nt) rod::rotate_element_twice(v, e, 0.5 * h);
+        }
         // VirtualBoundaryForcing.time_step(local_rod_dt) of the thread's marker
         if (t < n)
             for (int d = 0; d < 3; ++d) xi[d] = xi[d] + hT * dU[d];

@@ -250,6 +250,39 @@ SG_ROD_FN void rotate_element(View& r, int e, double h) {
     if (r.clamped && e == 0) clamp_element0(r);
 }
 
+// Two consecutive half drifts with the same velocity (the closing one of a sub-step and the opening
+// one of the next: nothing changes v or w between them), computed as the two separately are --
+// two additions, one rotation exp(-h [w]x) applied twice -- so the result is bitwise that of
+// drift_node and rotate_element called twice, without the second rotation's exponential.  A
+// clamped node 0 and element 0 end at the clamp as they would.
+SG_ROD_FN void drift_node_twice(View& r, int i, double h) {
+    const int nn = r.n + 1;
+    for (int a = 0; a < 3; ++a) {
+        r.x[a * nn + i] += h * r.v[a * nn + i];
+        r.x[a * nn + i] += h * r.v[a * nn + i];
+    }
+    if (r.clamped && i == 0) clamp_node0(r);
+}
+
+SG_ROD_FN void rotate_element_twice(View& r, int e, double h) {
+    const int n = r.n;
+    double a[3], rot[9], q[9], p[9];
+    for (int k = 0; k < 3; ++k) a[k] = -h * r.w[k * n + e];
+    rotation_exp(a, rot);
+    for (int k = 0; k < 9; ++k) q[k] = r.q[k * n + e];
+    for (int rep = 0; rep < 2; ++rep) {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double acc = 0.0;
+                for (int m = 0; m < 3; ++m) acc += rot[i * 3 + m] * q[m * 3 + j];
+                p[i * 3 + j] = acc;
+            }
+        for (int k = 0; k < 9; ++k) q[k] = p[k];
+    }
+    for (int k = 0; k < 9; ++k) r.q[k * n + e] = q[k];
+    if (r.clamped && e == 0) clamp_element0(r);
+}
+
 SG_ROD_FN void element_pass(const View& r, const Scratch& s, int e) {
     const int n = r.n, nn = n + 1;
     double d[3], t[3], qt[3], sig[3], stress[3];
@@ -317,7 +350,7 @@ SG_ROD_FN void node_update(View& r, const Scratch& s, int i, double dt, double d
         if (i < n) f += s.nlab[a * n + i];
         if (i > 0) f -= s.nlab[a * n + i - 1];
         r.v[a * nn + i] += dt * (f + r.f_ext[a * nn + i]) * inv_m;
-        r.v[a * nn + i] *= decay;
+        if (decay != 1.0) r.v[a * nn + i] *= decay;  // (x * 1 is x: no multiply without damping)
     }
     if (r.clamped && i == 0) clamp_node0(r);
 }
@@ -340,7 +373,7 @@ SG_ROD_FN void element_update(View& r, const Scratch& s, int e, double dt, doubl
     matvec(r.inv_inertia, n, e, c, alpha);
     for (int a = 0; a < 3; ++a) {
         r.w[a * n + e] += dt * s.e[e] * alpha[a];
-        r.w[a * n + e] *= decay;
+        if (decay != 1.0) r.w[a * n + e] *= decay;
     }
     if (r.clamped && e == 0) clamp_element0(r);
 }
