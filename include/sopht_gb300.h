@@ -593,6 +593,19 @@ typedef struct sg_rod_coupling {
 } sg_rod_coupling;
 int sg_rod_batch_coupled_substeps(const sg_rod_batch* batch, const sg_rod_coupling* coupling, void* stream);
 
+/* The 3D step's rotational-form vorticity update w2 = w1 + prefactor curl(u x w1)
+ * on [1:-1]^3 (w1 elsewhere), as one operator: the reference forms it from
+ * elementwise_cross_product (elementwise_ops_3d.py:406-448) and the curl
+ * kernel (curl_3d.py), navier_stokes_flow_simulators.py:461-471.  staged = 0:
+ * the direct-load kernel; staged = 1: inputs staged in shared memory by tensor
+ * copies (fp32, nx a multiple of 4, 16-byte aligned fields), the same bits; a
+ * copy wait that runs out writes SG_ERR_CUDA to *status (device word). */
+int sg_rotational_update_3d(int dtype, int nz, int ny, int nx, const void* w1, const void* u, void* out,
+                            double prefactor, int staged, int32_t* status, void* stream);
+/* No reference counterpart: the plan's device status word (0, or SG_ERR_CUDA
+ * after a bounded wait inside a step's kernels ran out); blocks. */
+int sg_flow_kernel_status(sg_flow_plan plan, int32_t* host_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -159,6 +159,9 @@ _SIGNATURES = {
     "sg_rod_batch_coupled_substeps": (c_int, [POINTER(RodBatch), POINTER(RodCoupling), c_void_p]),
     "sg_flow_device_time_slot": (c_int, [c_void_p, POINTER(c_void_p)]),
     "sg_event_record": (c_int, [c_void_p, c_void_p]),
+    "sg_rotational_update_3d": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_int,
+                                        c_void_p, c_void_p]),
+    "sg_flow_kernel_status": (c_int, [c_void_p, POINTER(ctypes.c_int32)]),
     "sg_ib_spread_sorted_scratch_bytes": (c_int64, [c_int, c_int, c_int, c_int, c_int]),
     "sg_ib_spread_sorted": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_int, c_void_p, c_int64, c_void_p]),

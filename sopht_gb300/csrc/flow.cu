@@ -261,7 +261,9 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         SG_TRY(launch_status("forcing_curl3d"));
         w1 = A;
     }
-    {
+    if (sizeof(T) == 4 && rot_update_tma_ok(G, w1, u, B)) {
+        SG_TRY(launch_rot_update_tma(G, (const float*)w1, (const float*)u, (float*)B, sc, p->kernel_status(), stream));
+    } else {
         Stencil3DParams<T> s{};
         s.grid = G;
         s.a = w1;
@@ -475,6 +477,12 @@ extern "C" int sg_flow_read_device_time(sg_flow_plan p, double* host_out) {
     SG_REQUIRE(p && host_out, SG_ERR_INVALID_ARG, "read device time: null argument");
     return cuda_status(cudaMemcpy(host_out, p->time_slot(), sizeof(double), cudaMemcpyDeviceToHost),
                        "read device time");
+}
+
+extern "C" int sg_flow_kernel_status(sg_flow_plan p, int32_t* host_out) {
+    SG_REQUIRE(p && host_out, SG_ERR_INVALID_ARG, "kernel status: null argument");
+    return cuda_status(cudaMemcpy(host_out, p->kernel_status(), sizeof(int32_t), cudaMemcpyDeviceToHost),
+                       "read kernel status");
 }
 
 extern "C" int sg_event_record(void* event, void* stream_) {

@@ -607,6 +607,13 @@ __global__ void __launch_bounds__(256) rotational_update3d_kernel(Stencil3DParam
     p.out[2 * n + g] = w2;
 }
 
+// The same update with its inputs staged by tensor copies (stencil_tma.cu; fp32, nx a multiple of
+// 4, 16-byte aligned fields), bitwise the kernel above; a copy wait that runs out writes
+// SG_ERR_CUDA to *status.
+bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void* out);
+int launch_rot_update_tma(const Grid3& G, const float* w1, const float* u, float* out, const ScalarSrc& sc,
+                          int32_t* status, cudaStream_t stream);
+
 // w3 = w2 + k lap(w2) on [1:-1]^3 per component (diffusion_timestep_3d.py)
 template <typename T>
 __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) {

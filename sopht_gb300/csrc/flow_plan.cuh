@@ -17,7 +17,8 @@ struct sg_flow_plan_s {
     void* coef_x = nullptr;
     void* coef_y = nullptr;
     void* coef_z = nullptr;
-    // device block: [0, 64) sg_step_scalars, [64, 72) umax (field type), [72, 80) time
+    // device block: [0, 64) sg_step_scalars, [64, 72) umax (field type), [72, 80) time,
+    // [80, 84) kernel status (a bounded wait that ran out)
     unsigned char* dev_block = nullptr;
     // pinned host word the host-side stable dt reads the max through
     void* host_word = nullptr;
@@ -40,6 +41,7 @@ struct sg_flow_plan_s {
     sg_step_scalars* dev_scalars() const { return reinterpret_cast<sg_step_scalars*>(dev_block); }
     void* umax_slot() const { return dev_block + 64; }
     double* time_slot() const { return reinterpret_cast<double*>(dev_block + 72); }
+    int32_t* kernel_status() const { return reinterpret_cast<int32_t*>(dev_block + 80); }
     int64_t cells() const { return (int64_t)nz * ny * nx; }
 };
 

@@ -214,6 +214,38 @@ extern "C" int sg_diffusion_step_3d(int dtype, int nz, int ny, int nx, const voi
                       stencil3d_op<double>(1, nz, ny, nx, in, nullptr, out, k, s));
 }
 
+// w2 = w1 + pc curl(u x w1) on [1:-1]^3 (w1 elsewhere), the 3D step's rotational-form update
+template <typename T>
+static int rotational_update_op(int nz, int ny, int nx, const void* w1, const void* u, void* out, double pc,
+                                int staged, int32_t* status, cudaStream_t s) {
+    Stencil3DParams<T> p{};
+    p.grid = Grid3{nz, ny, nx};
+    p.a = (const T*)w1;
+    p.b = (const T*)u;
+    p.out = (T*)out;
+    p.sc.host.advection_prefac = pc;
+    if (staged) {
+        if constexpr (sizeof(T) == 4) {
+            SG_REQUIRE(rot_update_tma_ok(p.grid, w1, u, out), SG_ERR_INVALID_ARG,
+                       "rotational update: the staged form needs fp32, nx a multiple of 4 and 16-byte aligned fields");
+            return launch_rot_update_tma(p.grid, (const float*)w1, (const float*)u, (float*)out, p.sc, status, s);
+        }
+        SG_REQUIRE(false, SG_ERR_INVALID_ARG, "rotational update: the staged form is fp32 only");
+    }
+    rotational_update3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
+    return launch_status("rotational update");
+}
+
+extern "C" int sg_rotational_update_3d(int dtype, int nz, int ny, int nx, const void* w1, const void* u, void* out,
+                                       double prefactor, int staged, int32_t* status, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, w1, out));
+    SG_REQUIRE(u && u != out, SG_ERR_INVALID_ARG, "rotational update: null velocity or velocity aliasing out");
+    SG_REQUIRE(!staged || status, SG_ERR_INVALID_ARG, "rotational update: the staged form needs a status word");
+    auto s = (cudaStream_t)stream;
+    SG_DTYPE_DISPATCH(dtype, rotational_update_op<float>(nz, ny, nx, w1, u, out, prefactor, staged, status, s),
+                      rotational_update_op<double>(nz, ny, nx, w1, u, out, prefactor, staged, status, s));
+}
+
 template <typename T>
 static int cross_op(int64_t n, const void* a, const void* b, void* out, cudaStream_t s) {
     cross3d_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(n, (const T*)a, (const T*)b, (T*)out);

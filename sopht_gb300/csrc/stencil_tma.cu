@@ -1,0 +1,275 @@
+// The 3D rotational update w2 = w1 + pc curl(u x w1) with its inputs staged by TMA (fp32).
+//
+// The direct-load kernel (rotational_update3d_kernel) reads u and w1 at the six neighbours of a
+// cell and forms u x w1 six times per cell, 36 loads and six cross products where one of each
+// would do.  Here a block owns a 32 x 8 tile of (x, y) and marches along z through 32 planes (16
+// or 8 on grids too small to give every SM four blocks otherwise):
+//   * the tile's (u, w1) plane with a halo of one cell in y and of four cells before and eight
+//     after in x (the copy starts on a 16-byte boundary) comes into shared memory by one tensor
+//     copy per field, three planes in flight through a ring of stages, each stage completing
+//     an mbarrier;
+//   * u x w1 is formed once per point of the plane (the tile and a one-cell halo) into a ring of
+//     three cross-product planes;
+//   * each output cell then reads its six neighbouring cross products and its own w1 from shared
+//     memory and writes w2 in the direct kernel's arithmetic order, so the two kernels agree to
+//     the bit.
+// Cells outside the grid read as zero (the copies' out-of-range fill) and only interior cells
+// are updated, as in the direct kernel.  Every mbarrier wait is bounded: a wait that runs out
+// records SG_ERR_CUDA in the caller's status word, lets the copies already issued land (again
+// bounded) and leaves the block.
+#include <cuda.h>
+
+#include "flow_kernels.cuh"
+
+namespace sg {
+namespace {
+
+constexpr int kTX = 32, kTY = 8;                // output tile (z planes per block: RotTmaParams::zc)
+constexpr int kBX = 40, kBY = 10;               // copied box: x from x0 - 4, y from y0 - 1
+constexpr int kBoxFloats = 3 * kBY * kBX;       // one field's box, [c][y][x]
+constexpr int kFieldBytes = 4864;               // 4800 bytes of box, padded to 128
+constexpr int kStageBytes = 2 * kFieldBytes;    // w1, then u
+constexpr int kStages = 3;
+constexpr int kCrossFloats = 3 * kBY * kBX;     // u x w1 of one plane on the box grid
+constexpr int kCrossPoints = kBY * (kTX + 2);   // the tile and a one-cell halo in x and y
+// + 64 for the mbarriers, + 128 to align the stages for the copies (under the 48 KB default)
+constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 3 * kCrossFloats * sizeof(float) + 64 + 128;
+static_assert(kSmemBytes <= 48 * 1024, "no dynamic shared-memory attribute needed");
+constexpr int kWaitLimit = 1 << 20;
+static_assert(kBoxFloats * 4 <= kFieldBytes && kFieldBytes % 128 == 0, "stage layout");
+
+struct RotTmaParams {
+    Grid3 grid;
+    float* out;
+    ScalarSrc sc;      // pc = the advection prefactor
+    int32_t* status;
+    int zc;            // z planes per block
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// true when the phase completed within the limit
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try(bar, parity)) return true;
+        if (i > 32) __nanosleep(64);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void copy_box(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];"
+        :
+        : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(0), "r"(bar)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(kTX * kTY) rot_update_tma_kernel(const __grid_constant__ CUtensorMap map_w,
+                                                                   const __grid_constant__ CUtensorMap map_u,
+                                                                   RotTmaParams p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // the copies' destinations on 128-byte boundaries of the shared window
+    unsigned char* smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    float* cross = reinterpret_cast<float*>(smem + kStages * kStageBytes);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes + 3 * kCrossFloats * sizeof(float));
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
+    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+    const int zb = blockIdx.z * p.zc, ze = min(G.nz, zb + p.zc);
+    const int nplanes = ze - zb + 2;  // input plane j is z = zb - 1 + j
+    float pcs[1];
+    block_scalars<float, 1>([&](int) { return p.sc.advection(); }, pcs);
+    const float pc = pcs[0];
+    auto stage = [&](int j) { return reinterpret_cast<float*>(smem + (j % kStages) * kStageBytes); };
+    auto bar = [&](int j) { return smem_addr(bars + j % kStages); };
+    auto issue = [&](int j) {  // thread 0: plane j of w1 and u into its stage
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar(j)), "r"(2 * kBoxFloats * 4)
+                     : "memory");
+        float* s = stage(j);
+        copy_box(smem_addr(s), &map_w, x0 - 4, y0 - 1, zb - 1 + j, bar(j));
+        copy_box(smem_addr(s) + kFieldBytes, &map_u, x0 - 4, y0 - 1, zb - 1 + j, bar(j));
+    };
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bars + s)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int j = 0; j < kStages && j < nplanes; ++j) issue(j);
+    int issued = min(kStages, nplanes), waited = 0;
+    // u x w1 of plane j on the tile and its halo, into cross slot j % 3
+    auto form_cross = [&](int j) {
+        const float* w = stage(j);
+        const float* u = w + kFieldBytes / 4;
+        float* c = cross + (j % 3) * kCrossFloats;
+        for (int k = tid; k < kCrossPoints; k += kTX * kTY) {
+            const int yy = k / (kTX + 2), xx = 3 + k % (kTX + 2);
+            const int o = yy * kBX + xx, pl = kBY * kBX;
+            const float ux = u[o], uy = u[pl + o], uz = u[2 * pl + o];
+            const float wx = w[o], wy = w[pl + o], wz = w[2 * pl + o];
+            // elementwise_ops_3d.py:406-448: r_i = a_j b_k - b_j a_k, as cross_at
+            c[o] = uy * wz - wy * uz;
+            c[pl + o] = uz * wx - wz * ux;
+            c[2 * pl + o] = ux * wy - wx * uy;
+        }
+    };
+    // waits for plane j; false (in every thread) when a wait ran out
+    auto arrive = [&](int j) {
+        const bool ok = mbar_wait(bar(j), (uint32_t)((j / kStages) & 1));
+        waited = j + 1;
+        return ok;
+    };
+    bool ok = arrive(0);
+    ok = ok && arrive(1);
+    const bool bad0 = __syncthreads_or(!ok);
+    if (!bad0) {
+        form_cross(0);
+        form_cross(1);
+    }
+    bool bad = bad0;
+    if (!bad) {
+        __syncthreads();
+        if (tid == 0 && 3 < nplanes) issue(3);
+        issued = min(4, nplanes);
+        for (int j = 1; j + 1 < nplanes; ++j) {
+            const bool got = arrive(j + 1);
+            if (__syncthreads_or(!got)) {
+                bad = true;
+                break;
+            }
+            form_cross(j + 1);
+            __syncthreads();
+            // output plane j: z = zb - 1 + j
+            const int z = zb - 1 + j, x = x0 + tx, y = y0 + ty;
+            if (x < G.nx && y < G.ny) {
+                const int xx = tx + 4, yy = ty + 1, pl = kBY * kBX, o = yy * kBX + xx;
+                const float* w = stage(j);
+                float w0 = w[o], w1 = w[pl + o], w2 = w[2 * pl + o];
+                if (G.interior(z, y, x)) {
+                    const float* cm = cross + ((j + 2) % 3) * kCrossFloats;  // plane j - 1
+                    const float* c0 = cross + (j % 3) * kCrossFloats;
+                    const float* cp = cross + ((j + 1) % 3) * kCrossFloats;  // plane j + 1
+                    float cyp[3], cym[3], czp[3], czm[3], cxp[3], cxm[3];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        cyp[d] = c0[d * pl + o + kBX];
+                        cym[d] = c0[d * pl + o - kBX];
+                        czp[d] = cp[d * pl + o];
+                        czm[d] = cm[d * pl + o];
+                        cxp[d] = c0[d * pl + o + 1];
+                        cxm[d] = c0[d * pl + o - 1];
+                    }
+                    const float r0 = cyp[2] - cym[2] - czp[1] + czm[1];
+                    const float r1 = czp[0] - czm[0] - cxp[2] + cxm[2];
+                    const float r2 = cxp[1] - cxm[1] - cyp[0] + cym[0];
+                    w0 = w0 + pc * r0;
+                    w1 = w1 + pc * r1;
+                    w2 = w2 + pc * r2;
+                }
+                const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
+                p.out[g] = w0;
+                p.out[n + g] = w1;
+                p.out[2 * n + g] = w2;
+            }
+            __syncthreads();
+            if (j + 3 < nplanes) {
+                if (tid == 0) issue(j + 3);
+                issued = j + 4;
+            }
+        }
+    }
+    if (bad) {
+        // a copy did not land in time: record it, give the issued copies a bounded wait, leave
+        if (tid == 0) {
+            atomicExch(p.status, SG_ERR_CUDA);
+            for (int j = waited; j < issued; ++j) mbar_wait(bar(j), (uint32_t)((j / kStages) & 1));
+        }
+        __syncthreads();
+    }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<EncodeTiled>(f);
+    }();
+    return fn;
+}
+
+// the (3, nz, ny, nx) fp32 field as a 4D tensor, boxes of 40 x 10 x 1 x 3
+int encode_field(CUtensorMap* m, const float* base, const Grid3& G) {
+    EncodeTiled fn = encode_fn();
+    SG_REQUIRE(fn, SG_ERR_CUDA, "tensor copies: cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[4] = {(cuuint64_t)G.nx, (cuuint64_t)G.ny, (cuuint64_t)G.nz, 3};
+    const cuuint64_t strides[3] = {(cuuint64_t)G.nx * 4, (cuuint64_t)G.nx * G.ny * 4,
+                                   (cuuint64_t)G.nx * G.ny * G.nz * 4};
+    const cuuint32_t box[4] = {kBX, kBY, 1, 3};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    SG_REQUIRE(r == CUDA_SUCCESS, SG_ERR_CUDA, "tensor copies: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SG_OK;
+}
+
+}  // namespace
+
+bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void* out) {
+    const auto aligned = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+    return G.nx % 4 == 0 && G.nx >= 4 && G.ny >= 3 && G.nz >= 3 && aligned(w1) && aligned(u) && aligned(out) &&
+           encode_fn() != nullptr;
+}
+
+int launch_rot_update_tma(const Grid3& G, const float* w1, const float* u, float* out, const ScalarSrc& sc,
+                          int32_t* status, cudaStream_t stream) {
+    SG_REQUIRE(rot_update_tma_ok(G, w1, u, out), SG_ERR_INVALID_ARG,
+               "tensor-copy rotational update: nx a multiple of 4, 16-byte aligned fields");
+    SG_REQUIRE(status, SG_ERR_INVALID_ARG, "tensor-copy rotational update: null status word");
+    CUtensorMap mw, mu;
+    SG_TRY(encode_field(&mw, w1, G));
+    SG_TRY(encode_field(&mu, u, G));
+    RotTmaParams p{};
+    p.grid = G;
+    p.out = out;
+    p.sc = sc;
+    p.status = status;
+    // the longest z run per block (32, 16 or 8 planes: each block also copies the two planes around
+    // its run) that still gives four blocks per SM
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t tiles = (int64_t)((G.nx + kTX - 1) / kTX) * ((G.ny + kTY - 1) / kTY);
+    p.zc = 32;
+    while (p.zc > 8 && tiles * ((G.nz + p.zc - 1) / p.zc) < 4LL * sms) p.zc /= 2;
+    const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
+                    (unsigned)((G.nz + p.zc - 1) / p.zc));
+    rot_update_tma_kernel<<<grid, dim3(kTX, kTY), kSmemBytes, stream>>>(mw, mu, p);
+    return launch_status("tensor-copy rotational update");
+}
+
+}  // namespace sg
