@@ -603,8 +603,19 @@ int sg_rod_batch_coupled_substeps(const sg_rod_batch* batch, const sg_rod_coupli
 int sg_rotational_update_3d(int dtype, int nz, int ny, int nx, const void* w1, const void* u, void* out,
                             double prefactor, int staged, int32_t* status, void* stream);
 /* No reference counterpart: the plan's device status word (0, or SG_ERR_CUDA
- * after a bounded wait inside a step's kernels ran out); blocks. */
+ * after a bounded wait inside a step's kernels ran out; sticky); blocks. */
 int sg_flow_kernel_status(sg_flow_plan plan, int32_t* host_out);
+/* Replaces diffusion_timestep_3d.py:12-80 for 1 or 3 components with the
+ * kernel chosen: staged = 0 the direct-load kernel (sg_diffusion_step_3d's),
+ * staged = 1 the input staged in shared memory by tensor copies (fp32, nx a
+ * multiple of 4, 16-byte aligned fields), the same bits; a copy wait that runs
+ * out writes SG_ERR_CUDA to *status (device word). */
+int sg_diffusion_3d_staged(int dtype, int nz, int ny, int nx, int ncomp, const void* in, void* out, double k,
+                           int staged, int32_t* status, void* stream);
+/* No reference counterpart: the device status word of the operator entries'
+ * staged kernels (sg_passive_transport_step takes them on fp32 grids); 0, or
+ * SG_ERR_CUDA after a bounded wait ran out (sticky); blocks. */
+int sg_ops_kernel_status(int32_t* host_out);
 
 #ifdef __cplusplus
 }

@@ -273,7 +273,9 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
         rotational_update3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(s);
         SG_TRY(launch_status("rotational_update3d"));
     }
-    {
+    if (sizeof(T) == 4 && diffusion_tma_ok(G, 3, B, A)) {
+        SG_TRY(launch_diffusion_tma(G, 3, (const float*)B, (float*)A, sc, p->kernel_status(), stream));
+    } else {
         Stencil3DParams<T> s{};
         s.grid = G;
         s.a = B;

@@ -614,6 +614,12 @@ bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void
 int launch_rot_update_tma(const Grid3& G, const float* w1, const float* u, float* out, const ScalarSrc& sc,
                           int32_t* status, cudaStream_t stream);
 
+// The diffusion below with its input staged by tensor copies (stencil_tma.cu; fp32, 1 or 3
+// components, nx a multiple of 4, 16-byte aligned fields), bitwise the direct kernel.
+bool diffusion_tma_ok(const Grid3& G, int ncomp, const void* in, const void* out);
+int launch_diffusion_tma(const Grid3& G, int ncomp, const float* in, float* out, const ScalarSrc& sc,
+                         int32_t* status, cudaStream_t stream);
+
 // w3 = w2 + k lap(w2) on [1:-1]^3 per component (diffusion_timestep_3d.py)
 template <typename T>
 __global__ void __launch_bounds__(256) diffusion3d_kernel(Stencil3DParams<T> p) {

@@ -159,6 +159,26 @@ extern "C" int sg_penalise_2d(int dtype, int ny, int nx, const void* in, void* o
                       penalise_op<double>(2, 1, ny, nx, in, out, width, cx, cy, nullptr, 1, s));
 }
 
+// The status word of the operator entries' kernels (a bounded wait that ran out), one per device.
+static __device__ int32_t ops_status_word;
+
+static int32_t* ops_status() {
+    static int32_t* addr[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!addr[dev]) {
+        void* a = nullptr;
+        if (cudaGetSymbolAddress(&a, ops_status_word) != cudaSuccess) return nullptr;
+        addr[dev] = static_cast<int32_t*>(a);
+    }
+    return addr[dev];
+}
+
+extern "C" int sg_ops_kernel_status(int32_t* host_out) {
+    SG_REQUIRE(host_out, SG_ERR_INVALID_ARG, "ops kernel status: null output");
+    return cuda_status(cudaMemcpyFromSymbol(host_out, ops_status_word, sizeof(int32_t)), "read ops kernel status");
+}
+
 static int check3d(int nz, int ny, int nx, const void* a, const void* b) {
     SG_REQUIRE(a && b, SG_ERR_INVALID_ARG, "null field pointer");
     SG_REQUIRE(nz >= 1 && ny >= 1 && nx >= 1, SG_ERR_SHAPE, "bad 3D extent");
@@ -234,6 +254,36 @@ static int rotational_update_op(int nz, int ny, int nx, const void* w1, const vo
     }
     rotational_update3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
     return launch_status("rotational update");
+}
+
+// w3 = w2 + k lap(w2) on [1:-1]^3 for ncomp (1 or 3) components: staged = 0 the direct-load kernel,
+// 1 the tensor-copy-staged one (fp32), the same bits
+extern "C" int sg_diffusion_3d_staged(int dtype, int nz, int ny, int nx, int ncomp, const void* in, void* out,
+                                      double k, int staged, int32_t* status, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, in, out));
+    SG_REQUIRE(ncomp == 1 || ncomp == 3, SG_ERR_INVALID_ARG, "diffusion: 1 or 3 components");
+    auto s = (cudaStream_t)stream;
+    const Grid3 G{nz, ny, nx};
+    if (staged) {
+        SG_REQUIRE(dtype == SG_F32 && status && diffusion_tma_ok(G, ncomp, in, out), SG_ERR_INVALID_ARG,
+                   "diffusion: the staged form needs fp32, a status word, nx a multiple of 4 and 16-byte aligned fields");
+        ScalarSrc sc{};
+        sc.host.diffusion_prefac = k;
+        return launch_diffusion_tma(G, ncomp, (const float*)in, (float*)out, sc, status, s);
+    }
+    auto direct = [&](auto tag) {
+        using T = decltype(tag);
+        Stencil3DParams<T> p{};
+        p.grid = G;
+        p.a = (const T*)in;
+        p.out = (T*)out;
+        p.prefactor = (T)k;
+        p.mode = 1;
+        p.ncomp = ncomp;
+        diffusion3d_kernel<T><<<cell3_grid(p.grid), cell3_block(), 0, s>>>(p);
+        return launch_status("diffusion3d");
+    };
+    SG_DTYPE_DISPATCH(dtype, direct(float{}), direct(double{}));
 }
 
 extern "C" int sg_rotational_update_3d(int dtype, int nz, int ny, int nx, const void* w1, const void* u, void* out,
@@ -324,6 +374,15 @@ static int eno3_3d_launch(int nz, int ny, int nx, int ncomp, const void* field, 
 template <typename T>
 static int diffusion3d_comps_launch(int nz, int ny, int nx, int ncomp, const void* in, void* out, double k,
                                     cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        const Grid3 G{nz, ny, nx};
+        int32_t* status = ops_status();
+        if (status && diffusion_tma_ok(G, ncomp, in, out)) {
+            ScalarSrc sc{};
+            sc.host.diffusion_prefac = k;
+            return launch_diffusion_tma(G, ncomp, (const float*)in, (float*)out, sc, status, s);
+        }
+    }
     Stencil3DParams<T> p{};
     p.grid = Grid3{nz, ny, nx};
     p.a = (const T*)in;

@@ -223,13 +223,13 @@ EncodeTiled encode_fn() {
 }
 
 // the (3, nz, ny, nx) fp32 field as a 4D tensor, boxes of 40 x 10 x 1 x 3
-int encode_field(CUtensorMap* m, const float* base, const Grid3& G) {
+int encode_field(CUtensorMap* m, const float* base, const Grid3& G, int ncomp = 3) {
     EncodeTiled fn = encode_fn();
     SG_REQUIRE(fn, SG_ERR_CUDA, "tensor copies: cuTensorMapEncodeTiled is not available");
-    const cuuint64_t dims[4] = {(cuuint64_t)G.nx, (cuuint64_t)G.ny, (cuuint64_t)G.nz, 3};
+    const cuuint64_t dims[4] = {(cuuint64_t)G.nx, (cuuint64_t)G.ny, (cuuint64_t)G.nz, (cuuint64_t)ncomp};
     const cuuint64_t strides[3] = {(cuuint64_t)G.nx * 4, (cuuint64_t)G.nx * G.ny * 4,
                                    (cuuint64_t)G.nx * G.ny * G.nz * 4};
-    const cuuint32_t box[4] = {kBX, kBY, 1, 3};
+    const cuuint32_t box[4] = {kBX, kBY, 1, (cuuint32_t)ncomp};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -238,7 +238,141 @@ int encode_field(CUtensorMap* m, const float* base, const Grid3& G) {
     return SG_OK;
 }
 
+// ---------------------------------------------------------------- diffusion
+// w3 = w2 + k lap(w2) on [1:-1]^3 per component, the (1 or 3 components of a) plane of the tile
+// with its halo copied as above; five stages: planes j - 1, j, j + 1 in use while plane j is
+// written, two more in flight.
+constexpr int kDStages = 5;
+constexpr size_t kDSmemBytes = (size_t)kDStages * kFieldBytes + 64 + 128;
+static_assert(kDSmemBytes <= 48 * 1024, "no dynamic shared-memory attribute needed");
+
+struct DiffTmaParams {
+    Grid3 grid;
+    float* out;
+    ScalarSrc sc;      // k = the diffusion prefactor
+    int ncomp;
+    int32_t* status;
+    int zc;
+};
+
+__global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_constant__ CUtensorMap map,
+                                                                  DiffTmaParams p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kDStages * kFieldBytes);
+    const Grid3 G = p.grid;
+    const int64_t n = G.n();
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
+    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+    const int zb = blockIdx.z * p.zc, ze = min(G.nz, zb + p.zc);
+    const int nplanes = ze - zb + 2;  // input plane j is z = zb - 1 + j
+    const int nc = p.ncomp;
+    float ks[1];
+    block_scalars<float, 1>([&](int) { return p.sc.diffusion(); }, ks);
+    const float k = ks[0];
+    auto stage = [&](int j) { return reinterpret_cast<const float*>(smem + (j % kDStages) * kFieldBytes); };
+    auto bar = [&](int j) { return smem_addr(bars + j % kDStages); };
+    auto issue = [&](int j) {  // thread 0
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar(j)), "r"(nc * kBY * kBX * 4)
+                     : "memory");
+        copy_box(smem_addr(stage(j)), &map, x0 - 4, y0 - 1, zb - 1 + j, bar(j));
+    };
+    if (tid == 0) {
+        for (int s = 0; s < kDStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bars + s)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int j = 0; j < kDStages && j < nplanes; ++j) issue(j);
+    int issued = min(kDStages, nplanes), waited = 0;
+    auto arrive = [&](int j) {
+        const bool ok = mbar_wait(bar(j), (uint32_t)((j / kDStages) & 1));
+        waited = j + 1;
+        return ok;
+    };
+    bool ok = arrive(0);
+    bool bad = __syncthreads_or(!ok);
+    for (int j = 1; !bad && j + 1 < nplanes; ++j) {
+        // planes j - 1 and j are in (waited for in the iterations before); wait for j + 1
+        const bool got = (j == 1 ? arrive(1) : true) && arrive(j + 1);
+        if (__syncthreads_or(!got)) {
+            bad = true;
+            break;
+        }
+        const int z = zb - 1 + j, x = x0 + tx, y = y0 + ty;
+        if (x < G.nx && y < G.ny) {
+            const int xx = tx + 4, yy = ty + 1, pl = kBY * kBX, o = yy * kBX + xx;
+            const float *cm = stage(j - 1), *c0 = stage(j), *cp = stage(j + 1);
+            const bool in = G.interior(z, y, x);
+            const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
+            for (int c = 0; c < nc; ++c) {
+                const float v = c0[c * pl + o];
+                float r = v;
+                if (in) {
+                    // diffusion_flux_3d.py:34-43 term order: z+1, z-1, y+1, y-1, x+1, x-1
+                    const float lap = cp[c * pl + o] + cm[c * pl + o] + c0[c * pl + o + kBX] + c0[c * pl + o - kBX] +
+                                      c0[c * pl + o + 1] + c0[c * pl + o - 1] - 6.f * v;
+                    r = v + k * lap;
+                }
+                p.out[c * n + g] = r;
+            }
+        }
+        __syncthreads();
+        // plane j - 1 is no longer read: its stage takes plane j + kDStages - 1
+        if (j + kDStages - 1 < nplanes) {
+            if (tid == 0) issue(j + kDStages - 1);
+            issued = j + kDStages;
+        }
+    }
+    if (bad) {
+        if (tid == 0) {
+            atomicExch(p.status, SG_ERR_CUDA);
+            for (int j = waited; j < issued; ++j) mbar_wait(bar(j), (uint32_t)((j / kDStages) & 1));
+        }
+        __syncthreads();
+    }
+}
+
+// the longest z run per block (32, 16 or 8 planes: each block also copies the two planes around its
+// run) that still gives every SM four blocks
+int z_run(const Grid3& G) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t tiles = (int64_t)((G.nx + kTX - 1) / kTX) * ((G.ny + kTY - 1) / kTY);
+    int zc = 32;
+    while (zc > 8 && tiles * ((G.nz + zc - 1) / zc) < 4LL * sms) zc /= 2;
+    return zc;
+}
+
 }  // namespace
+
+bool diffusion_tma_ok(const Grid3& G, int ncomp, const void* in, const void* out) {
+    const auto aligned = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+    return (ncomp == 1 || ncomp == 3) && G.nx % 4 == 0 && G.nx >= 4 && G.ny >= 3 && G.nz >= 3 && aligned(in) &&
+           aligned(out) && encode_fn() != nullptr;
+}
+
+int launch_diffusion_tma(const Grid3& G, int ncomp, const float* in, float* out, const ScalarSrc& sc,
+                         int32_t* status, cudaStream_t stream) {
+    SG_REQUIRE(diffusion_tma_ok(G, ncomp, in, out), SG_ERR_INVALID_ARG,
+               "tensor-copy diffusion: 1 or 3 components, nx a multiple of 4, 16-byte aligned fields");
+    SG_REQUIRE(status, SG_ERR_INVALID_ARG, "tensor-copy diffusion: null status word");
+    CUtensorMap m;
+    SG_TRY(encode_field(&m, in, G, ncomp));
+    DiffTmaParams p{};
+    p.grid = G;
+    p.out = out;
+    p.sc = sc;
+    p.ncomp = ncomp;
+    p.status = status;
+    p.zc = z_run(G);
+    const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
+                    (unsigned)((G.nz + p.zc - 1) / p.zc));
+    diffusion_tma_kernel<<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
+    return launch_status("tensor-copy diffusion");
+}
 
 bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void* out) {
     const auto aligned = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
@@ -259,13 +393,7 @@ int launch_rot_update_tma(const Grid3& G, const float* w1, const float* u, float
     p.out = out;
     p.sc = sc;
     p.status = status;
-    // the longest z run per block (32, 16 or 8 planes: each block also copies the two planes around
-    // its run) that still gives four blocks per SM
-    int dev = 0, sms = 152;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t tiles = (int64_t)((G.nx + kTX - 1) / kTX) * ((G.ny + kTY - 1) / kTY);
-    p.zc = 32;
-    while (p.zc > 8 && tiles * ((G.nz + p.zc - 1) / p.zc) < 4LL * sms) p.zc /= 2;
+    p.zc = z_run(G);
     const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
                     (unsigned)((G.nz + p.zc - 1) / p.zc));
     rot_update_tma_kernel<<<grid, dim3(kTX, kTY), kSmemBytes, stream>>>(mw, mu, p);

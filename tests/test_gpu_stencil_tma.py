@@ -1,12 +1,13 @@
-"""The rotational update with tensor-copy-staged inputs against the direct-load kernel.
+"""The 3D rotational update and diffusion with tensor-copy-staged inputs against the direct-load
+kernels.
 
 ``sg_rotational_update_3d(staged=1)`` stages (u, w1) planes in shared memory by TMA and forms
-u x w1 once per point; ``staged=0`` is the direct-load kernel the 3D step used before.  Both do
-the same arithmetic per cell, so their outputs must agree to the bit, on grids whose x, y and z
-extents are not multiples of the 32 x 8 x 32 block tiles (partial tiles, out-of-range halo
-fills) and on the smallest grid the staged form takes.  The status word stays zero (no copy wait
-ran out), and the 3D step (which takes the staged form at these sizes) leaves its plan's status
-word zero.
+u x w1 once per point, ``sg_diffusion_3d_staged(staged=1)`` stages the diffused field's planes;
+``staged=0`` runs the direct-load kernels.  Each pair does the same arithmetic per cell, so the
+outputs must agree to the bit, on grids whose x, y and z extents are not multiples of the block
+tiles (partial tiles, out-of-range halo fills) and on the smallest grid the staged forms take.
+The status words stay zero (no copy wait ran out): the caller's, the 3D step's plan's and the
+operator entries' (the 3D passive step takes the staged diffusion).
 """
 
 from __future__ import annotations
@@ -87,4 +88,48 @@ def test_three_d_step_leaves_its_status_word_zero():
     torch.cuda.synchronize()
     st = ctypes.c_int32(-1)
     assert L.load().sg_flow_kernel_status(sim._plan, ctypes.byref(st)) == 0
+    assert st.value == 0
+
+
+@pytest.mark.parametrize("ncomp", [1, 3])
+@pytest.mark.parametrize("shape", [(3, 3, 4), (17, 70, 36), (40, 36, 128), (64, 64, 64)])
+def test_staged_diffusion_is_bitwise_the_direct_kernel(shape, ncomp):
+    L = _lib()
+    nz, ny, nx = shape
+    rng = np.random.default_rng(nz + ny + nx + ncomp)
+    w = torch.from_numpy(rng.standard_normal((ncomp, nz, ny, nx)).astype(np.float32)).cuda()
+    direct = torch.full_like(w, np.nan)
+    staged = torch.full_like(w, np.nan)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    k = 0.0931
+    L.call("sg_diffusion_3d_staged", L.SG_F32, nz, ny, nx, ncomp, w.data_ptr(), direct.data_ptr(), k, 0, None, s)
+    L.call("sg_diffusion_3d_staged", L.SG_F32, nz, ny, nx, ncomp, w.data_ptr(), staged.data_ptr(), k, 1,
+           status.data_ptr(), s)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert torch.equal(direct, staged)
+    a = w.cpu().numpy().astype(np.float64)
+    ref = a.copy()
+    i = (slice(None),) + (slice(1, -1),) * 3
+    lap = (a[:, 2:, 1:-1, 1:-1] + a[:, :-2, 1:-1, 1:-1] + a[:, 1:-1, 2:, 1:-1] + a[:, 1:-1, :-2, 1:-1] +
+           a[:, 1:-1, 1:-1, 2:] + a[:, 1:-1, 1:-1, :-2] - 6 * a[i])
+    ref[i] = a[i] + k * lap
+    np.testing.assert_allclose(staged.cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(ref).max())
+
+
+def test_passive_step_takes_the_staged_diffusion_and_leaves_the_status_word_zero():
+    L = _lib()
+    nz, ny, nx = 32, 40, 64
+    rng = np.random.default_rng(5)
+    field = torch.from_numpy(rng.standard_normal((3, nz, ny, nx)).astype(np.float32)).cuda()
+    vel = torch.from_numpy(0.1 * rng.standard_normal((3, nz, ny, nx)).astype(np.float32)).cuda()
+    scratch = torch.empty_like(field)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L.call("sg_passive_transport_step", L.SG_F32, 3, nz, ny, nx, 3, field.data_ptr(), scratch.data_ptr(),
+           vel.data_ptr(), 0.05, 0.01, s)
+    torch.cuda.synchronize()
+    assert torch.isfinite(field).all()
+    st = ctypes.c_int32(-1)
+    assert L.load().sg_ops_kernel_status(ctypes.byref(st)) == 0
     assert st.value == 0
