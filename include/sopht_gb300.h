@@ -612,6 +612,12 @@ int sg_flow_kernel_status(sg_flow_plan plan, int32_t* host_out);
  * out writes SG_ERR_CUDA to *status (device word). */
 int sg_diffusion_3d_staged(int dtype, int nz, int ny, int nx, int ncomp, const void* in, void* out, double k,
                            int staged, int32_t* status, void* stream);
+/* Replaces update_vorticity_from_velocity_forcing_3d.py:12-132 with the
+ * kernel chosen: staged = 0 sg_forcing_curl_update_3d's direct-load kernel,
+ * staged = 1 the forcing staged in shared memory by tensor copies (fp32, nx a
+ * multiple of 4, 16-byte aligned fields), the same bits; *status as above. */
+int sg_forcing_curl_3d_staged(int dtype, int nz, int ny, int nx, const void* in, void* out, const void* forcing,
+                              double prefactor, int staged, int32_t* status, void* stream);
 /* No reference counterpart: the device status word of the operator entries'
  * staged kernels (sg_passive_transport_step takes them on fp32 grids); 0, or
  * SG_ERR_CUDA after a bounded wait ran out (sticky); blocks. */

@@ -250,15 +250,20 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
     mark(p, 0, stream);
     const T* w1 = w;
     if (f) {
-        Stencil3DParams<T> s{};
-        s.grid = G;
-        s.a = w;
-        s.b = f;
-        s.out = A;
-        s.sc = sc;
-        s.mode = 0;
-        forcing_curl3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(s);
-        SG_TRY(launch_status("forcing_curl3d"));
+        if (sizeof(T) == 4 && forcing_curl_tma_ok(G, w, f, A)) {
+            SG_TRY(launch_forcing_curl_tma(G, (const float*)w, (const float*)f, (float*)A, sc, p->kernel_status(),
+                                           stream));
+        } else {
+            Stencil3DParams<T> s{};
+            s.grid = G;
+            s.a = w;
+            s.b = f;
+            s.out = A;
+            s.sc = sc;
+            s.mode = 0;
+            forcing_curl3d_kernel<T><<<cell3_grid(G), cell3_block(), 0, stream>>>(s);
+            SG_TRY(launch_status("forcing_curl3d"));
+        }
         w1 = A;
     }
     if (sizeof(T) == 4 && rot_update_tma_ok(G, w1, u, B)) {

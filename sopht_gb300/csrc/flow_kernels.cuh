@@ -614,6 +614,12 @@ bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void
 int launch_rot_update_tma(const Grid3& G, const float* w1, const float* u, float* out, const ScalarSrc& sc,
                           int32_t* status, cudaStream_t stream);
 
+// The forcing curl above with the forcing staged by tensor copies (stencil_tma.cu; fp32, nx a
+// multiple of 4, 16-byte aligned fields), bitwise forcing_curl3d_kernel with a forcing field.
+bool forcing_curl_tma_ok(const Grid3& G, const void* w, const void* f, const void* out);
+int launch_forcing_curl_tma(const Grid3& G, const float* w, const float* f, float* out, const ScalarSrc& sc,
+                            int32_t* status, cudaStream_t stream);
+
 // The diffusion below with its input staged by tensor copies (stencil_tma.cu; fp32, 1 or 3
 // components, nx a multiple of 4, 16-byte aligned fields), bitwise the direct kernel.
 bool diffusion_tma_ok(const Grid3& G, int ncomp, const void* in, const void* out);

@@ -256,6 +256,27 @@ static int rotational_update_op(int nz, int ny, int nx, const void* w1, const vo
     return launch_status("rotational update");
 }
 
+// w1 = w + pf curl(f) on [1:-1]^3: staged = 0 the direct-load kernel, 1 the forcing staged by
+// tensor copies (fp32), the same bits
+extern "C" int sg_forcing_curl_3d_staged(int dtype, int nz, int ny, int nx, const void* in, void* out,
+                                         const void* forcing, double prefactor, int staged, int32_t* status,
+                                         void* stream) {
+    SG_TRY(check3d(nz, ny, nx, in, out));
+    SG_REQUIRE(forcing && forcing != out, SG_ERR_INVALID_ARG, "forcing curl: null forcing or forcing aliasing out");
+    auto s = (cudaStream_t)stream;
+    const Grid3 G{nz, ny, nx};
+    if (staged) {
+        SG_REQUIRE(dtype == SG_F32 && status && forcing_curl_tma_ok(G, in, forcing, out), SG_ERR_INVALID_ARG,
+                   "forcing curl: the staged form needs fp32, a status word, nx a multiple of 4 and 16-byte aligned "
+                   "fields");
+        ScalarSrc sc{};
+        sc.host.forcing_prefac = prefactor;
+        return launch_forcing_curl_tma(G, (const float*)in, (const float*)forcing, (float*)out, sc, status, s);
+    }
+    SG_DTYPE_DISPATCH(dtype, stencil3d_op<float>(0, nz, ny, nx, in, forcing, out, prefactor, s),
+                      stencil3d_op<double>(0, nz, ny, nx, in, forcing, out, prefactor, s));
+}
+
 // w3 = w2 + k lap(w2) on [1:-1]^3 for ncomp (1 or 3) components: staged = 0 the direct-load kernel,
 // 1 the tensor-copy-staged one (fp32), the same bits
 extern "C" int sg_diffusion_3d_staged(int dtype, int nz, int ny, int nx, int ncomp, const void* in, void* out,

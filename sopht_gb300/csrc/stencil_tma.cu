@@ -249,12 +249,18 @@ static_assert(kDSmemBytes <= 48 * 1024, "no dynamic shared-memory attribute need
 struct DiffTmaParams {
     Grid3 grid;
     float* out;
-    ScalarSrc sc;      // k = the diffusion prefactor
+    ScalarSrc sc;      // k = the diffusion prefactor (pf = the forcing prefactor for the curl)
     int ncomp;
     int32_t* status;
     int zc;
+    const float* w;    // the forcing curl's vorticity (read at the cell), or null
 };
 
+enum { PLANE_DIFFUSE = 0, PLANE_FORCING_CURL = 1 };
+
+// PLANE_DIFFUSE: out = f + k lap(f) per component.  PLANE_FORCING_CURL: out = w + pf curl(f), the
+// copied field f the forcing and w read at the cell (forcing_curl3d_kernel's arithmetic).
+template <int OP>
 __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_constant__ CUtensorMap map,
                                                                   DiffTmaParams p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -268,7 +274,7 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
     const int nplanes = ze - zb + 2;  // input plane j is z = zb - 1 + j
     const int nc = p.ncomp;
     float ks[1];
-    block_scalars<float, 1>([&](int) { return p.sc.diffusion(); }, ks);
+    block_scalars<float, 1>([&](int) { return OP == PLANE_DIFFUSE ? p.sc.diffusion() : p.sc.forcing(); }, ks);
     const float k = ks[0];
     auto stage = [&](int j) { return reinterpret_cast<const float*>(smem + (j % kDStages) * kFieldBytes); };
     auto bar = [&](int j) { return smem_addr(bars + j % kDStages); };
@@ -302,7 +308,25 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
             break;
         }
         const int z = zb - 1 + j, x = x0 + tx, y = y0 + ty;
-        if (x < G.nx && y < G.ny) {
+        if (OP == PLANE_FORCING_CURL && x < G.nx && y < G.ny) {
+            const int xx = tx + 4, yy = ty + 1, pl = kBY * kBX, o = yy * kBX + xx;
+            const float *cm = stage(j - 1), *c0 = stage(j), *cp = stage(j + 1);
+            const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
+            float w0 = p.w[g], w1 = p.w[n + g], w2 = p.w[2 * n + g];
+            if (G.interior(z, y, x)) {
+                // curl3_at's terms: f at y +- 1, z +- 1 and x +- 1 from the three planes
+                const float c0v = c0[2 * pl + o + kBX] - c0[2 * pl + o - kBX] - cp[pl + o] + cm[pl + o];
+                const float c1v = cp[o] - cm[o] - c0[2 * pl + o + 1] + c0[2 * pl + o - 1];
+                const float c2v = c0[pl + o + 1] - c0[pl + o - 1] - c0[o + kBX] + c0[o - kBX];
+                w0 = w0 + k * c0v;
+                w1 = w1 + k * c1v;
+                w2 = w2 + k * c2v;
+            }
+            p.out[g] = w0;
+            p.out[n + g] = w1;
+            p.out[2 * n + g] = w2;
+        }
+        if (OP == PLANE_DIFFUSE && x < G.nx && y < G.ny) {
             const int xx = tx + 4, yy = ty + 1, pl = kBY * kBX, o = yy * kBX + xx;
             const float *cm = stage(j - 1), *c0 = stage(j), *cp = stage(j + 1);
             const bool in = G.interior(z, y, x);
@@ -370,8 +394,33 @@ int launch_diffusion_tma(const Grid3& G, int ncomp, const float* in, float* out,
     p.zc = z_run(G);
     const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
                     (unsigned)((G.nz + p.zc - 1) / p.zc));
-    diffusion_tma_kernel<<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
+    diffusion_tma_kernel<PLANE_DIFFUSE><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
     return launch_status("tensor-copy diffusion");
+}
+
+bool forcing_curl_tma_ok(const Grid3& G, const void* w, const void* f, const void* out) {
+    return diffusion_tma_ok(G, 3, f, out) && (reinterpret_cast<uintptr_t>(w) & 15) == 0;
+}
+
+int launch_forcing_curl_tma(const Grid3& G, const float* w, const float* f, float* out, const ScalarSrc& sc,
+                            int32_t* status, cudaStream_t stream) {
+    SG_REQUIRE(forcing_curl_tma_ok(G, w, f, out), SG_ERR_INVALID_ARG,
+               "tensor-copy forcing curl: nx a multiple of 4, 16-byte aligned fields");
+    SG_REQUIRE(status, SG_ERR_INVALID_ARG, "tensor-copy forcing curl: null status word");
+    CUtensorMap m;
+    SG_TRY(encode_field(&m, f, G, 3));
+    DiffTmaParams p{};
+    p.grid = G;
+    p.out = out;
+    p.sc = sc;
+    p.ncomp = 3;
+    p.status = status;
+    p.zc = z_run(G);
+    p.w = w;
+    const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
+                    (unsigned)((G.nz + p.zc - 1) / p.zc));
+    diffusion_tma_kernel<PLANE_FORCING_CURL><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
+    return launch_status("tensor-copy forcing curl");
 }
 
 bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void* out) {

@@ -2,7 +2,8 @@
 kernels.
 
 ``sg_rotational_update_3d(staged=1)`` stages (u, w1) planes in shared memory by TMA and forms
-u x w1 once per point, ``sg_diffusion_3d_staged(staged=1)`` stages the diffused field's planes;
+u x w1 once per point, ``sg_diffusion_3d_staged(staged=1)`` and ``sg_forcing_curl_3d_staged``
+stage the diffused field's and the forcing's planes;
 ``staged=0`` runs the direct-load kernels.  Each pair does the same arithmetic per cell, so the
 outputs must agree to the bit, on grids whose x, y and z extents are not multiples of the block
 tiles (partial tiles, out-of-range halo fills) and on the smallest grid the staged forms take.
@@ -133,3 +134,34 @@ def test_passive_step_takes_the_staged_diffusion_and_leaves_the_status_word_zero
     st = ctypes.c_int32(-1)
     assert L.load().sg_ops_kernel_status(ctypes.byref(st)) == 0
     assert st.value == 0
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 4), (17, 70, 36), (40, 36, 128), (64, 64, 64)])
+def test_staged_forcing_curl_is_bitwise_the_direct_kernel(shape):
+    L = _lib()
+    nz, ny, nx = shape
+    rng = np.random.default_rng(7 * nz + ny + nx)
+    w = torch.from_numpy(rng.standard_normal((3, nz, ny, nx)).astype(np.float32)).cuda()
+    f = torch.from_numpy(rng.standard_normal((3, nz, ny, nx)).astype(np.float32)).cuda()
+    direct = torch.full_like(w, np.nan)
+    staged = torch.full_like(w, np.nan)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    pf = 0.0217
+    L.call("sg_forcing_curl_3d_staged", L.SG_F32, nz, ny, nx, w.data_ptr(), direct.data_ptr(), f.data_ptr(), pf, 0,
+           None, s)
+    L.call("sg_forcing_curl_3d_staged", L.SG_F32, nz, ny, nx, w.data_ptr(), staged.data_ptr(), f.data_ptr(), pf, 1,
+           status.data_ptr(), s)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert torch.equal(direct, staged)
+    a, b = w.cpu().numpy().astype(np.float64), f.cpu().numpy().astype(np.float64)
+    sh = lambda q, d, k: np.roll(q, -k, axis=d)  # noqa: E731
+    curl = np.stack([sh(b[2], 1, 1) - sh(b[2], 1, -1) - sh(b[1], 0, 1) + sh(b[1], 0, -1),
+                     sh(b[0], 0, 1) - sh(b[0], 0, -1) - sh(b[2], 2, 1) + sh(b[2], 2, -1),
+                     sh(b[1], 2, 1) - sh(b[1], 2, -1) - sh(b[0], 1, 1) + sh(b[0], 1, -1)])
+    ref = a.copy()
+    i = (slice(1, -1),) * 3
+    for d in range(3):
+        ref[d][i] = a[d][i] + pf * curl[d][i]
+    np.testing.assert_allclose(staged.cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(ref).max())
