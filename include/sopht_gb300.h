@@ -98,7 +98,9 @@ int sg_poisson_solve(sg_poisson_plan plan, const void* rhs, void* sol, int ncomp
  * rebuilds the Green's table into it, so make that first call before any
  * stream capture; a rebuild asked for on a capturing stream returns
  * SG_ERR_INVALID_ARG and leaves the array as it was.  The array holds the table
- * of the last grid: a call on a new grid replaces it for every later reader.
+ * of the last grid: a call on a new grid replaces it for every later reader,
+ * graphs captured earlier on another grid included (they then read the new
+ * grid's table; replay them only after a call on their own grid).
  * All calls share the array: calls whose GPU work overlaps (other streams,
  * other host threads) race and must be serialised by the caller. */
 int sg_poisson2d_solve_noalloc(int ny, int nx, double x_range, const float* rhs, float* sol,
@@ -618,6 +620,14 @@ int sg_diffusion_3d_staged(int dtype, int nz, int ny, int nx, int ncomp, const v
  * multiple of 4, 16-byte aligned fields), the same bits; *status as above. */
 int sg_forcing_curl_3d_staged(int dtype, int nz, int ny, int nx, const void* in, void* out, const void* forcing,
                               double prefactor, int staged, int32_t* status, void* stream);
+/* Replaces curl_3d.py:13-132 with elementwise_ops_3d.py's add_fixed_val and
+ * the max of sum |u_d| (navier_stokes_flow_simulators.py:212-223) in one pass,
+ * the kernel chosen: u = prefactor curl(psi) on [1:-1]^3 (0 on the ring) +
+ * free_stream (3 host values, or NULL), max into *umax (device, or NULL; not
+ * reset); staged = 0 the direct-load kernel, staged = 1 psi staged by tensor
+ * copies (fp32, nx a multiple of 4, 16-byte aligned fields), the same bits. */
+int sg_curl_3d_staged(int dtype, int nz, int ny, int nx, const void* psi, void* u, double prefactor,
+                      const double* free_stream, void* umax, int staged, int32_t* status, void* stream);
 /* No reference counterpart: the device status word of the operator entries'
  * staged kernels (sg_passive_transport_step takes them on fp32 grids); 0, or
  * SG_ERR_CUDA after a bounded wait ran out (sticky); blocks. */

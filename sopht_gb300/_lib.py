@@ -167,6 +167,8 @@ _SIGNATURES = {
     "sg_ops_kernel_status": (c_int, [POINTER(ctypes.c_int32)]),
     "sg_forcing_curl_3d_staged": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_int,
                                           c_void_p, c_void_p]),
+    "sg_curl_3d_staged": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_int,
+                                  c_void_p, c_void_p]),
     "sg_ib_spread_sorted_scratch_bytes": (c_int64, [c_int, c_int, c_int, c_int, c_int]),
     "sg_ib_spread_sorted": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_int, c_void_p, c_int64, c_void_p]),

@@ -308,7 +308,11 @@ int flow_step_3d(sg_flow_plan_s* p, T* w, T* u, T* f, T* psi, const ScalarSrc& s
     c.sc = sc;
     c.add_free_stream = free_stream;
     c.umax = (T*)p->umax_slot();
-    SG_TRY(launch_curl3d<T>(c, n, stream));
+    if (sizeof(T) == 4 && velocity_curl_tma_ok(G, psi, u))
+        SG_TRY(launch_velocity_curl_tma(G, (const float*)psi, (float*)u, (float)c.prefactor, sc, free_stream,
+                                        (float*)c.umax, p->kernel_status(), stream));
+    else
+        SG_TRY(launch_curl3d<T>(c, n, stream));
     mark(p, 7, stream);
     return SG_OK;
 }

@@ -614,6 +614,12 @@ bool rot_update_tma_ok(const Grid3& G, const void* w1, const void* u, const void
 int launch_rot_update_tma(const Grid3& G, const float* w1, const float* u, float* out, const ScalarSrc& sc,
                           int32_t* status, cudaStream_t stream);
 
+// The velocity curl (curl3d_kernel, below) with psi staged by tensor copies (stencil_tma.cu; fp32,
+// nx a multiple of 4, 16-byte aligned fields), bitwise the direct kernel, the same max.
+bool velocity_curl_tma_ok(const Grid3& G, const void* psi, const void* u);
+int launch_velocity_curl_tma(const Grid3& G, const float* psi, float* u, float prefactor, const ScalarSrc& sc,
+                             int add_free_stream, float* umax, int32_t* status, cudaStream_t stream);
+
 // The forcing curl above with the forcing staged by tensor copies (stencil_tma.cu; fp32, nx a
 // multiple of 4, 16-byte aligned fields), bitwise forcing_curl3d_kernel with a forcing field.
 bool forcing_curl_tma_ok(const Grid3& G, const void* w, const void* f, const void* out);

@@ -256,6 +256,39 @@ static int rotational_update_op(int nz, int ny, int nx, const void* w1, const vo
     return launch_status("rotational update");
 }
 
+// u = prefactor curl(psi) on [1:-1]^3 (0 on the ring) + free_stream (host, 3 values, or null),
+// with max sum |u_d| into *umax (device, or null; not reset here): staged = 0 the direct-load
+// kernel, 1 psi staged by tensor copies (fp32), the same bits
+extern "C" int sg_curl_3d_staged(int dtype, int nz, int ny, int nx, const void* psi, void* u, double prefactor,
+                                 const double* free_stream, void* umax, int staged, int32_t* status, void* stream) {
+    SG_TRY(check3d(nz, ny, nx, psi, u));
+    auto s = (cudaStream_t)stream;
+    const Grid3 G{nz, ny, nx};
+    ScalarSrc sc{};
+    if (free_stream)
+        for (int d = 0; d < 3; ++d) sc.host.free_stream[d] = free_stream[d];
+    if (staged) {
+        SG_REQUIRE(dtype == SG_F32 && status && velocity_curl_tma_ok(G, psi, u), SG_ERR_INVALID_ARG,
+                   "curl: the staged form needs fp32, a status word, nx a multiple of 4 and 16-byte aligned fields");
+        return launch_velocity_curl_tma(G, (const float*)psi, (float*)u, (float)prefactor, sc, free_stream != nullptr,
+                                        (float*)umax, status, s);
+    }
+    auto direct = [&](auto tag) {
+        using T = decltype(tag);
+        Curl3DParams<T> c{};
+        c.grid = G;
+        c.psi = (const T*)psi;
+        c.u = (T*)u;
+        c.prefactor = (T)prefactor;
+        c.sc = sc;
+        c.add_free_stream = free_stream != nullptr;
+        c.umax = (T*)umax;
+        curl3d_kernel<T><<<cell3_grid(c.grid), cell3_block(), 0, s>>>(c);
+        return launch_status("curl3d");
+    };
+    SG_DTYPE_DISPATCH(dtype, direct(float{}), direct(double{}));
+}
+
 // w1 = w + pf curl(f) on [1:-1]^3: staged = 0 the direct-load kernel, 1 the forcing staged by
 // tensor copies (fp32), the same bits
 extern "C" int sg_forcing_curl_3d_staged(int dtype, int nz, int ny, int nx, const void* in, void* out,

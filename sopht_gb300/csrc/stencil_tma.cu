@@ -254,12 +254,18 @@ struct DiffTmaParams {
     int32_t* status;
     int zc;
     const float* w;    // the forcing curl's vorticity (read at the cell), or null
+    float prefactor;   // the velocity curl's 0.5 / dx
+    int add_free_stream;
+    float* umax;       // the velocity curl's max of sum |u_d|, or null
 };
 
-enum { PLANE_DIFFUSE = 0, PLANE_FORCING_CURL = 1 };
+enum { PLANE_DIFFUSE = 0, PLANE_FORCING_CURL = 1, PLANE_VELOCITY_CURL = 2 };
 
 // PLANE_DIFFUSE: out = f + k lap(f) per component.  PLANE_FORCING_CURL: out = w + pf curl(f), the
 // copied field f the forcing and w read at the cell (forcing_curl3d_kernel's arithmetic).
+// PLANE_VELOCITY_CURL: out = prefactor curl(f) on [1:-1]^3 (0 on the ring) + the free stream, with
+// the max over the block's cells of sum |out_d| into *umax (curl3d_kernel's arithmetic; the max
+// is the same whichever cells a block holds).
 template <int OP>
 __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_constant__ CUtensorMap map,
                                                                   DiffTmaParams p) {
@@ -276,6 +282,12 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
     float ks[1];
     block_scalars<float, 1>([&](int) { return OP == PLANE_DIFFUSE ? p.sc.diffusion() : p.sc.forcing(); }, ks);
     const float k = ks[0];
+    float m = 0.f;  // PLANE_VELOCITY_CURL: the thread's max of sum |u_d|
+    // the free stream in fp32, converted once per block (a double-to-float conversion per cell
+    // and plane would hold the double-precision units for as long as the whole pass)
+    float fs[3] = {0.f, 0.f, 0.f};
+    if constexpr (OP == PLANE_VELOCITY_CURL)
+        block_scalars<float, 3>([&](int d) { return p.add_free_stream ? p.sc.free_stream(d) : 0.0; }, fs);
     auto stage = [&](int j) { return reinterpret_cast<const float*>(smem + (j % kDStages) * kFieldBytes); };
     auto bar = [&](int j) { return smem_addr(bars + j % kDStages); };
     auto issue = [&](int j) {  // thread 0
@@ -326,6 +338,28 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
             p.out[n + g] = w1;
             p.out[2 * n + g] = w2;
         }
+        if (OP == PLANE_VELOCITY_CURL && x < G.nx && y < G.ny) {
+            const int xx = tx + 4, yy = ty + 1, pl = kBY * kBX, o = yy * kBX + xx;
+            const float *cm = stage(j - 1), *c0 = stage(j), *cp = stage(j + 1);
+            const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
+            float c[3] = {0.f, 0.f, 0.f};
+            if (G.interior(z, y, x)) {
+                c[0] = c0[2 * pl + o + kBX] - c0[2 * pl + o - kBX] - cp[pl + o] + cm[pl + o];
+                c[1] = cp[o] - cm[o] - c0[2 * pl + o + 1] + c0[2 * pl + o - 1];
+                c[2] = c0[pl + o + 1] - c0[pl + o - 1] - c0[o + kBX] + c0[o - kBX];
+                c[0] = p.prefactor * c[0];
+                c[1] = p.prefactor * c[1];
+                c[2] = p.prefactor * c[2];
+            }
+            if (p.add_free_stream) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) c[d] = c[d] + fs[d];
+            }
+            p.out[g] = c[0];
+            p.out[n + g] = c[1];
+            p.out[2 * n + g] = c[2];
+            m = fmaxf(m, fabsf(c[0]) + fabsf(c[1]) + fabsf(c[2]));
+        }
         if (OP == PLANE_DIFFUSE && x < G.nx && y < G.ny) {
             const int xx = tx + 4, yy = ty + 1, pl = kBY * kBX, o = yy * kBX + xx;
             const float *cm = stage(j - 1), *c0 = stage(j), *cp = stage(j + 1);
@@ -356,6 +390,9 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
             for (int j = waited; j < issued; ++j) mbar_wait(bar(j), (uint32_t)((j / kDStages) & 1));
         }
         __syncthreads();
+    } else if (OP == PLANE_VELOCITY_CURL && p.umax) {
+        m = block_max(m);
+        if (tid == 0) atomic_max_nonneg_filtered(p.umax, m);
     }
 }
 
@@ -396,6 +433,33 @@ int launch_diffusion_tma(const Grid3& G, int ncomp, const float* in, float* out,
                     (unsigned)((G.nz + p.zc - 1) / p.zc));
     diffusion_tma_kernel<PLANE_DIFFUSE><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
     return launch_status("tensor-copy diffusion");
+}
+
+bool velocity_curl_tma_ok(const Grid3& G, const void* psi, const void* u) {
+    return diffusion_tma_ok(G, 3, psi, u);
+}
+
+int launch_velocity_curl_tma(const Grid3& G, const float* psi, float* u, float prefactor, const ScalarSrc& sc,
+                             int add_free_stream, float* umax, int32_t* status, cudaStream_t stream) {
+    SG_REQUIRE(velocity_curl_tma_ok(G, psi, u), SG_ERR_INVALID_ARG,
+               "tensor-copy curl: nx a multiple of 4, 16-byte aligned fields");
+    SG_REQUIRE(status, SG_ERR_INVALID_ARG, "tensor-copy curl: null status word");
+    CUtensorMap m;
+    SG_TRY(encode_field(&m, psi, G, 3));
+    DiffTmaParams p{};
+    p.grid = G;
+    p.out = u;
+    p.sc = sc;
+    p.ncomp = 3;
+    p.status = status;
+    p.zc = z_run(G);
+    p.prefactor = prefactor;
+    p.add_free_stream = add_free_stream;
+    p.umax = umax;
+    const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
+                    (unsigned)((G.nz + p.zc - 1) / p.zc));
+    diffusion_tma_kernel<PLANE_VELOCITY_CURL><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
+    return launch_status("tensor-copy curl");
 }
 
 bool forcing_curl_tma_ok(const Grid3& G, const void* w, const void* f, const void* out) {

@@ -2,8 +2,9 @@
 kernels.
 
 ``sg_rotational_update_3d(staged=1)`` stages (u, w1) planes in shared memory by TMA and forms
-u x w1 once per point, ``sg_diffusion_3d_staged(staged=1)`` and ``sg_forcing_curl_3d_staged``
-stage the diffused field's and the forcing's planes;
+u x w1 once per point; ``sg_diffusion_3d_staged``, ``sg_forcing_curl_3d_staged`` and
+``sg_curl_3d_staged`` stage the diffused field's, the forcing's and the stream function's planes
+(the last with the free stream and the max of sum |u_d| as the step's curl takes them);
 ``staged=0`` runs the direct-load kernels.  Each pair does the same arithmetic per cell, so the
 outputs must agree to the bit, on grids whose x, y and z extents are not multiples of the block
 tiles (partial tiles, out-of-range halo fills) and on the smallest grid the staged forms take.
@@ -165,3 +166,28 @@ def test_staged_forcing_curl_is_bitwise_the_direct_kernel(shape):
     for d in range(3):
         ref[d][i] = a[d][i] + pf * curl[d][i]
     np.testing.assert_allclose(staged.cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("free", [False, True])
+@pytest.mark.parametrize("shape", [(3, 3, 4), (17, 70, 36), (40, 36, 128), (64, 64, 64)])
+def test_staged_velocity_curl_is_bitwise_the_direct_kernel(shape, free):
+    L = _lib()
+    nz, ny, nx = shape
+    rng = np.random.default_rng(11 * nz + ny + nx + free)
+    psi = torch.from_numpy(rng.standard_normal((3, nz, ny, nx)).astype(np.float32)).cuda()
+    direct = torch.full_like(psi, np.nan)
+    staged = torch.full_like(psi, np.nan)
+    umax = torch.zeros(2, dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    fs = (ctypes.c_double * 3)(1.0, -0.25, 0.5) if free else None
+    pref = 0.5 * nx
+    L.call("sg_curl_3d_staged", L.SG_F32, nz, ny, nx, psi.data_ptr(), direct.data_ptr(), pref, fs, umax.data_ptr(),
+           0, None, s)
+    L.call("sg_curl_3d_staged", L.SG_F32, nz, ny, nx, psi.data_ptr(), staged.data_ptr(), pref, fs,
+           umax.data_ptr() + 4, 1, status.data_ptr(), s)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert torch.equal(direct, staged)
+    m = umax.cpu().numpy()
+    assert m[0] == m[1] == np.abs(staged.cpu().numpy()).sum(axis=0).max()
