@@ -58,6 +58,9 @@ struct RegLinesParams {
     // components of the z pass share their Green's table rows through L2); needs slab_lines % 16 == 0
     // and n_lines == interleave * slab_lines
     int interleave;
+    // > 0: each block also asks L2 for the input of block blockIdx + prefetch_ahead (about one
+    // wave of resident blocks later), so that block's loads find it there
+    int prefetch_ahead;
 };
 
 enum { RL_FWD = 0, RL_INV = 1, RL_CONV = 2 };
@@ -226,6 +229,30 @@ template <int N, bool INV> SG_RL_FN void dft_b(float2* v) {
     for (int b = 0; b < Shape<N>::B; ++b) dft16<INV>(v + 16 * b);
 }
 
+// The input points load_a (HIN: the lower half) or load_b would load for line L, asked of L2.
+template <int N, bool HIN, bool STAGE_B>
+SG_RL_FN void prefetch_input(const RegLinesParams& p, const Line& L, int q) {
+#ifdef __CUDA_ARCH__
+    if (!L.live) return;
+    constexpr int E = Shape<N>::E;
+    if constexpr (STAGE_B) {
+#pragma unroll
+        for (int b = 0; b < Shape<N>::B; ++b)
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int k = point_b<N>(q, b, r);
+                if (k < p.n_in) asm volatile("prefetch.global.L2 [%0];" ::"l"(p.in + L.base + (int64_t)k * p.stride));
+            }
+    } else {
+#pragma unroll
+        for (int j = 0; j < (HIN ? E / 2 : E); ++j) {
+            const int n = q + 16 * j;
+            if (n < p.n_in) asm volatile("prefetch.global.L2 [%0];" ::"l"(p.in + L.base + (int64_t)n * p.stride));
+        }
+    }
+#endif
+}
+
 template <int N>
 SG_RL_FN void load_b(const RegLinesParams& p, const Line& L, int t, float2* v) {
 #pragma unroll
@@ -383,6 +410,8 @@ __global__ void __launch_bounds__(rl::kThreads, 3) reg_lines_kernel(RegLinesPara
     const rl::Line L = rl::line_of(p, blockIdx.x, l);
     float2 v[rl::Shape<N>::E];
     rl::stage_twiddles<N>(p, tw_a, tid, rl::kThreads);
+    if (MODE != RL_CONV && p.prefetch_ahead > 0 && blockIdx.x + p.prefetch_ahead < gridDim.x)
+        rl::prefetch_input<N, HIN, MODE == RL_INV>(p, rl::line_of(p, blockIdx.x + p.prefetch_ahead, l), q);
     if constexpr (MODE == RL_INV) {
         rl::load_b<N>(p, L, q, v);
         rl::dft_b<N, true>(v);

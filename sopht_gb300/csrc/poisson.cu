@@ -286,6 +286,11 @@ static int reg_pass3d(sg_poisson_plan_s* p, int ncomp, int pass, cudaStream_t st
     r.slab_stride = (int64_t)2 * ny * (nx + 1);
     r.stride = nx + 1;
     r.tw = (const float2*)p->tw_y;
+    // the y passes wait on their own input (long-scoreboard bound): each block asks L2 for the
+    // block one wave of resident blocks (three per SM) ahead
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    r.prefetch_ahead = 3 * sms;
     if (pass == 0) {
         r.n_in = ny;
         r.n_out = 2 * ny;
