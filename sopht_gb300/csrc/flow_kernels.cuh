@@ -188,6 +188,7 @@ template <typename T> struct FlowLoadParams {
     FFTStages st;
     const cplx_t<T>* tw_m;
     const cplx_t<T>* tw_l;
+    int prefetch_ahead;      // register load pass: > 0 asks L2 for the rows of the block this far ahead
 };
 
 __device__ __forceinline__ int clamp_band(int i, int n, int w) {

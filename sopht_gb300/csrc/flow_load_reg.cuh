@@ -147,6 +147,11 @@ static __global__ void __launch_bounds__(rl::kThreads, 3) reg_flow_load_kernel(F
     const int tid = threadIdx.x, row = tid / 16, q = tid & 15;
     const rl::LoadRow R = rl::load_row_of(p, blockIdx.x, row);
     float2 v[16];
+    // the source rows of the block one wave ahead, asked of L2: 256 floats, 8 lines of 128 bytes
+    if (p.prefetch_ahead > 0 && blockIdx.x + p.prefetch_ahead < gridDim.x && q < 8) {
+        const rl::LoadRow Ra = rl::load_row_of(p, blockIdx.x + p.prefetch_ahead, row);
+        if (Ra.live) asm volatile("prefetch.global.L2 [%0];" ::"l"(p.src + Ra.src_off + q * 32));
+    }
     rl::stage_load_twiddles(p, tw_a, tid, rl::kThreads);
     rl::load_row_a(p, R, q, v);
     __syncthreads();  // the twiddle table
@@ -164,8 +169,11 @@ static __global__ void __launch_bounds__(rl::kThreads, 3) reg_flow_load_kernel(F
     });
 }
 
-inline int launch_reg_flow_load(const FlowLoadParams<float>& p, cudaStream_t stream) {
+inline int launch_reg_flow_load(FlowLoadParams<float> p, cudaStream_t stream) {
     if (p.n_rows <= 0) return SG_OK;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    p.prefetch_ahead = 3 * sms;  // one wave of resident blocks (three per SM)
     reg_flow_load_kernel<<<ceil_div(p.n_rows, rl::kLines), rl::kThreads, 0, stream>>>(p);
     return launch_status("register flow load");
 }
