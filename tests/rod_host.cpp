@@ -28,6 +28,36 @@ extern "C" int rod_host_step(const sg_rod_batch* b, int n_substeps, double dt, d
     return 0;
 }
 
+// The same sub-steps with the coupled kernel's pass structure: the closing half drift of one
+// sub-step and the opening half drift of the next in one pass (drift_node_twice,
+// rotate_element_twice), a lone half drift at either end.
+extern "C" int rod_host_step_merged(const sg_rod_batch* b, int n_substeps, double dt, double decay) {
+    using namespace sg::rod;
+    const int n = b->n_elems;
+    std::vector<double> work(scratch_doubles(n));
+    for (int r = 0; r < b->n_rods; ++r) {
+        View v = view_of(*b, r);
+        const Scratch s = carve(work.data(), n);
+        const double h = 0.5 * dt;
+        for (int i = 0; i <= n; ++i) drift_node(v, i, h);
+        for (int e = 0; e < n; ++e) rotate_element(v, e, h);
+        for (int k = 0; k < n_substeps; ++k) {
+            for (int e = 0; e < n; ++e) element_pass(v, s, e);
+            for (int q = 0; q < n - 1; ++q) voronoi_pass(v, s, q);
+            for (int i = 0; i <= n; ++i) node_update(v, s, i, dt, decay);
+            for (int e = 0; e < n; ++e) element_update(v, s, e, dt, decay);
+            if (k + 1 < n_substeps) {
+                for (int i = 0; i <= n; ++i) drift_node_twice(v, i, h);
+                for (int e = 0; e < n; ++e) rotate_element_twice(v, e, h);
+            } else {
+                for (int i = 0; i <= n; ++i) drift_node(v, i, h);
+                for (int e = 0; e < n; ++e) rotate_element(v, e, h);
+            }
+        }
+    }
+    return 0;
+}
+
 // The element-centric markers and reaction loads of the batch, in the kernels' order.
 extern "C" int rod_host_markers(const sg_rod_batch* b, int dim, double* pos, double* vel) {
     using namespace sg::rod;
