@@ -266,7 +266,8 @@ enum { PLANE_DIFFUSE = 0, PLANE_FORCING_CURL = 1, PLANE_VELOCITY_CURL = 2 };
 // PLANE_VELOCITY_CURL: out = prefactor curl(f) on [1:-1]^3 (0 on the ring) + the free stream, with
 // the max over the block's cells of sum |out_d| into *umax (curl3d_kernel's arithmetic; the max
 // is the same whichever cells a block holds).
-template <int OP>
+// NC: the components (3, or 1 for a scalar diffusion), fixed so that the per-component loop unrolls.
+template <int OP, int NC = 3>
 __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_constant__ CUtensorMap map,
                                                                   DiffTmaParams p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
     const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
     const int zb = blockIdx.z * p.zc, ze = min(G.nz, zb + p.zc);
     const int nplanes = ze - zb + 2;  // input plane j is z = zb - 1 + j
-    const int nc = p.ncomp;
+    constexpr int nc = NC;
     float ks[1];
     block_scalars<float, 1>([&](int) { return OP == PLANE_DIFFUSE ? p.sc.diffusion() : p.sc.forcing(); }, ks);
     const float k = ks[0];
@@ -365,6 +366,7 @@ __global__ void __launch_bounds__(kTX * kTY) diffusion_tma_kernel(const __grid_c
             const float *cm = stage(j - 1), *c0 = stage(j), *cp = stage(j + 1);
             const bool in = G.interior(z, y, x);
             const int64_t g = ((int64_t)z * G.ny + y) * G.nx + x;
+#pragma unroll
             for (int c = 0; c < nc; ++c) {
                 const float v = c0[c * pl + o];
                 float r = v;
@@ -431,7 +433,8 @@ int launch_diffusion_tma(const Grid3& G, int ncomp, const float* in, float* out,
     p.zc = z_run(G);
     const dim3 grid((unsigned)((G.nx + kTX - 1) / kTX), (unsigned)((G.ny + kTY - 1) / kTY),
                     (unsigned)((G.nz + p.zc - 1) / p.zc));
-    diffusion_tma_kernel<PLANE_DIFFUSE><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
+    if (ncomp == 1) diffusion_tma_kernel<PLANE_DIFFUSE, 1><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
+    else diffusion_tma_kernel<PLANE_DIFFUSE, 3><<<grid, dim3(kTX, kTY), kDSmemBytes, stream>>>(m, p);
     return launch_status("tensor-copy diffusion");
 }
 
